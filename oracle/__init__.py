@@ -1,0 +1,79 @@
+"""CPU checkers for the CUDA library -- TEST INFRASTRUCTURE ONLY.
+
+* ``liboracle.so``: the project's C restatement of the reference time step
+  (exported with an ``orc_`` prefix).
+* ``_ref/libsbfs_ref.so``: the reference's own time-step sources built against
+  single-rank stand-ins for MPI, SimpleDecomp and FFTW (only where the
+  reference sources were available at build time).
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py may
+import this package, and only to check or to time the CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+from simplebubblyflowsolver_gb300.binding import ReferenceAPI
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libsbfs_ref.so")
+
+
+def build(ref_dir: str | None = None, quiet: bool = True) -> None:
+    """compile liboracle.so, and _ref/libsbfs_ref.so when ref_dir exists"""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-C", HERE, "liboracle.so"], check=True, stdout=out)
+    if ref_dir and os.path.isdir(os.path.join(ref_dir, "src")):
+        subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_dir}"], check=True, stdout=out)
+
+
+class Oracle(ReferenceAPI):
+    def __init__(self):
+        if not os.path.exists(ORACLE_SO):
+            build()
+        lib = C.CDLL(ORACLE_SO)
+        super().__init__(lib, prefix="orc_", name="oracle")
+        lib.orc_set_dt_coefs.argtypes = [C.c_double] * 3
+        lib.orc_set_threads.argtypes = [C.c_int]
+        lib.orc_get_threads.restype = C.c_int
+        lib.orc_max_divergence.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+        lib.orc_vof_stats.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double * 4)]
+
+    def set_dt_coefs(self, adv, dif, itf):
+        self.lib.orc_set_dt_coefs(adv, dif, itf)
+
+    def set_threads(self, n):
+        self.lib.orc_set_threads(int(n))
+
+    def threads(self):
+        return self.lib.orc_get_threads()
+
+    def max_divergence(self, st):
+        out = C.c_double(0.0)
+        self.lib.orc_max_divergence(C.addressof(st.domain), C.addressof(st.fluid), C.byref(out))
+        return out.value
+
+    def vof_stats(self, st):
+        out = (C.c_double * 4)()
+        self.lib.orc_vof_stats(C.addressof(st.domain), C.addressof(st.interface), C.byref(out))
+        return tuple(out)
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class RefShim(ReferenceAPI):
+    """The reference's own sources (one grid per process: they keep
+    function-static solver state)."""
+
+    def __init__(self):
+        lib = C.CDLL(REF_SO)
+        super().__init__(lib, prefix="", name="reference")
+        lib.sbfs_refshim_info.restype = C.c_void_p
+
+    def info(self):
+        return self.lib.sbfs_refshim_info()
