@@ -1,0 +1,139 @@
+/*
+ * GB300 implementation of the SimpleBubblyFlowSolver 2-D time step.
+ *
+ * Drop-in boundary: the entry points below carry the reference solver's
+ * names, prototypes, argument meaning and error convention (0 = success,
+ * non-zero = failure; the reference's caller aborts on failure,
+ * src/main.c:118-120).  A program built against the reference's headers links
+ * this library in place of the reference's src/integrate.c, src/decide_dt.c,
+ * src/fluid/ and src/interface/ objects.  All computation runs in
+ * hand-written sm_103a CUDA kernels on one GPU; there is no CPU fallback.
+ *
+ * Host buffers: every array_t.data is the caller's host buffer, exactly as in
+ * the reference.  The fine-grained operators copy what they read to the GPU
+ * and what they write back, so their observable effect on the structs equals
+ * the reference's (including its pointer swaps of the RK sources and of the
+ * scalar potentials).  integrate() keeps the whole step on the device; by
+ * default it uploads the state (ux, uy, p, psi[0], vof) on entry and writes
+ * it back on exit (see sbfs_set_sync_mode for the device-resident mode).
+ *
+ * Limits: NDIMS == 2; uniform x grid (as the reference requires,
+ * src/domain.c:213-219); ny a power of two >= 8; 4 <= nx <= 8192.
+ */
+#ifndef SBFS_GB300_H
+#define SBFS_GB300_H
+
+#include <stddef.h>
+#include "sbfs_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- time integration (reference include/integrate.h:5-10, src/integrate.c:11-70) */
+int integrate(const domain_t *domain, fluid_t *fluid, interface_t *interface, double *dt);
+
+/* ---- time step size (reference include/decide_dt.h:5-10, src/decide_dt.c:140-169);
+ * safety factors from the environment keys coef_dt_adv, coef_dt_dif,
+ * coef_dt_int on first use, as the reference, unless sbfs_set_dt_coefs was called */
+int decide_dt(const domain_t *domain, const fluid_t *fluid, const interface_t *interface, double *dt);
+
+/* ---- fluid operators (reference include/fluid_solver.h:10-89) */
+int fluid_compute_density(const domain_t *domain, fluid_t *fluid, const interface_t *interface, const size_t index);
+int fluid_compute_viscosity(const domain_t *domain, fluid_t *fluid, const interface_t *interface);
+int fluid_predict_field(const domain_t *domain, const size_t rkstep, const double dt, fluid_t *fluid,
+                        const interface_t *interface);
+int fluid_compute_potential(const domain_t *domain, const double dt_old, const double dt_new, fluid_t *fluid);
+int fluid_correct_velocity(const domain_t *domain, const double dt_old, const double dt_new, fluid_t *fluid);
+int fluid_update_pressure(const domain_t *domain, fluid_t *fluid);
+int fluid_update_boundaries_ux(const domain_t *domain, array_t *array);
+int fluid_update_boundaries_uy(const domain_t *domain, array_t *array);
+int fluid_update_boundaries_p(const domain_t *domain, array_t *array);
+int fluid_update_boundaries_psi(const domain_t *domain, array_t *array);
+
+/* ---- interface operators (reference include/interface_solver.h:8-48) */
+int interface_compute_curvature_tensor(const domain_t *domain, interface_t *interface);
+int interface_compute_force(const domain_t *domain, const fluid_t *fluid, interface_t *interface);
+int interface_compute_mass_flux(const domain_t *domain, const fluid_t *fluid, interface_t *interface);
+int interface_update_vof(const domain_t *domain, const size_t rkstep, const double dt, const fluid_t *fluid,
+                         interface_t *interface);
+int interface_update_boundaries_vof(const domain_t *domain, array_t *vof);
+
+/* ---- initialisation and .npy I/O (reference include/domain.h:32-42,
+ * include/fluid_solver.h:10-22, include/interface_solver.h:8-18,
+ * src/fileio.c:268-508): same file names, shapes and dtypes ('<f8', '<u8').
+ * fluid_init reads Re, Fr, denr, visr and interface_init reads We from the
+ * environment, as the reference.  domain_t.info is left NULL (one process). */
+int domain_init(const char dirname_ic[], domain_t *domain);
+int domain_save(const char dirname[], const domain_t *domain);
+int fluid_init(const char dirname_ic[], const domain_t *domain, fluid_t *fluid);
+int fluid_save(const char dirname[], const domain_t *domain, const fluid_t *fluid);
+int interface_init(const char dirname_ic[], const domain_t *domain, interface_t *interface);
+int interface_save(const char dirname[], const domain_t *domain, const interface_t *interface);
+/* frees what domain_init / fluid_init / interface_init allocated (no
+ * reference counterpart: the reference never frees) */
+int sbfs_free_state(domain_t *domain, fluid_t *fluid, interface_t *interface);
+
+/* ---- GB300 additions (no reference counterpart) */
+
+/* what integrate() copies between host and device:
+ *   SBFS_SYNC_STATE (default): upload ux, uy, p, psi[0], vof on entry; write
+ *     them (and psi[1]) back on exit;
+ *   SBFS_SYNC_ALL: as STATE, and also write back every other array the
+ *     reference leaves filled (den, viscosities, stresses, sources, fluxes,
+ *     interface geometry);
+ *   SBFS_SYNC_NONE: device-resident; the state is uploaded on the first call
+ *     (or after sbfs_invalidate_device) and stays on the GPU between calls;
+ *     call sbfs_sync_to_host before reading host arrays and
+ *     sbfs_invalidate_device after changing them. */
+#define SBFS_SYNC_STATE 0
+#define SBFS_SYNC_ALL 1
+#define SBFS_SYNC_NONE 2
+int sbfs_set_sync_mode(int mode);
+int sbfs_sync_to_host(const domain_t *domain, fluid_t *fluid, interface_t *interface);
+int sbfs_invalidate_device(void);
+
+/* capture each time step into a CUDA graph (default 1) */
+int sbfs_set_use_graphs(int on);
+
+/* safety factors of decide_dt, overriding the environment keys */
+int sbfs_set_dt_coefs(double adv, double dif, double itf);
+
+/* advance nsteps steps device-resident and time them with CUDA events on the
+ * library's stream; *ms = elapsed milliseconds, *dt_last = last dt */
+int sbfs_run_steps_timed(const domain_t *domain, fluid_t *fluid, interface_t *interface, int nsteps, float *ms,
+                         double *dt_last);
+
+/* kernels launched by one integrate() step (for launch accounting) */
+int sbfs_kernels_per_step(void);
+
+/* select the CUDA device for the following calls (drops the current context) */
+int sbfs_set_device(int device);
+
+/* page-lock the state arrays integrate() copies (ux, uy, p, psi[0..1], vof)
+ * so the host<->device copies run at full link speed; unpin before freeing */
+int sbfs_pin_host_state(fluid_t *fluid, interface_t *interface);
+int sbfs_unpin_host_state(fluid_t *fluid, interface_t *interface);
+
+/* per-kernel timing of nsteps device-resident steps launched eagerly with a
+ * CUDA event pair around every launch on the library's stream;
+ * ms_per_class[k] / launches_per_class[k] for k < sbfs_kernel_classes() */
+int sbfs_kernel_classes(void);
+const char *sbfs_kernel_name(int cls);
+int sbfs_profile_steps(const domain_t *domain, fluid_t *fluid, interface_t *interface, int nsteps,
+                       float *ms_per_class, int *launches_per_class);
+
+/* device status bits: 1 = non-finite velocity seen by decide_dt */
+int sbfs_device_status(int *status);
+
+/* message of the last failure ("" if none) */
+const char *sbfs_last_error(void);
+
+/* release all device memory, streams and graphs of the library */
+int sbfs_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -19,22 +19,27 @@ from simplebubblyflowsolver_gb300.binding import ReferenceAPI
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
+ORACLE_FMA_SO = os.path.join(HERE, "liboracle_fma.so")
 REF_SO = os.path.join(HERE, "_ref", "libsbfs_ref.so")
 
 
 def build(ref_dir: str | None = None, quiet: bool = True) -> None:
     """compile liboracle.so, and _ref/libsbfs_ref.so when ref_dir exists"""
     out = subprocess.DEVNULL if quiet else None
-    subprocess.run(["make", "-C", HERE, "liboracle.so"], check=True, stdout=out)
+    subprocess.run(["make", "-C", HERE, "liboracle.so", "liboracle_fma.so"], check=True, stdout=out)
     if ref_dir and os.path.isdir(os.path.join(ref_dir, "src")):
         subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_dir}"], check=True, stdout=out)
 
 
 class Oracle(ReferenceAPI):
-    def __init__(self):
-        if not os.path.exists(ORACLE_SO):
+    """variant "fma": the same sources built with fused multiply-add
+    contraction (a second build that differs only in rounding)"""
+
+    def __init__(self, variant: str = ""):
+        path = ORACLE_FMA_SO if variant == "fma" else ORACLE_SO
+        if not os.path.exists(path):
             build()
-        lib = C.CDLL(ORACLE_SO)
+        lib = C.CDLL(path)
         super().__init__(lib, prefix="orc_", name="oracle")
         lib.orc_set_dt_coefs.argtypes = [C.c_double] * 3
         lib.orc_set_threads.argtypes = [C.c_int]

@@ -1,0 +1,131 @@
+"""GB300 implementation of SimpleBubblyFlowSolver's 2-D two-phase time step.
+
+The product is ``libsbfs_gb300.so``: the reference solver's C entry points
+(integrate, decide_dt, fluid_*, interface_*, *_init, *_save) implemented with
+hand-written sm_103a CUDA kernels.  This package builds it in-tree, binds it
+with ctypes and provides the host-side pieces a Python user needs
+(initial conditions in the reference's .npy schema, a state container).
+There is no CPU fallback: :func:`load_library` raises if the library is
+missing or cannot be loaded.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from ._abi import SolverState
+from .binding import RK_ALPHA, RK_BETA, RK_GAMMA, ReferenceAPI, SolverError, state_from_fields
+from .build import LIB as LIBRARY_PATH
+from .build import build as build_library
+
+SYNC_STATE, SYNC_ALL, SYNC_NONE = 0, 1, 2
+
+__all__ = [
+    "SolverState", "SolverError", "ReferenceAPI", "GpuLibrary", "load_library", "build_library",
+    "state_from_fields", "LIBRARY_PATH", "RK_ALPHA", "RK_BETA", "RK_GAMMA",
+    "SYNC_STATE", "SYNC_ALL", "SYNC_NONE",
+]
+
+_LIB = None
+
+
+class GpuLibrary(ReferenceAPI):
+    """The reference entry points of libsbfs_gb300.so plus its additions."""
+
+    def __init__(self, lib: C.CDLL):
+        super().__init__(lib, prefix="", name="libsbfs_gb300")
+        lib.sbfs_last_error.restype = C.c_char_p
+        lib.sbfs_set_sync_mode.argtypes = [C.c_int]
+        lib.sbfs_set_use_graphs.argtypes = [C.c_int]
+        lib.sbfs_set_dt_coefs.argtypes = [C.c_double] * 3
+        lib.sbfs_sync_to_host.argtypes = [C.c_void_p] * 3
+        lib.sbfs_run_steps_timed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                             C.POINTER(C.c_float), C.POINTER(C.c_double)]
+        lib.sbfs_device_status.argtypes = [C.POINTER(C.c_int)]
+        lib.sbfs_set_device.argtypes = [C.c_int]
+        lib.sbfs_pin_host_state.argtypes = [C.c_void_p, C.c_void_p]
+        lib.sbfs_unpin_host_state.argtypes = [C.c_void_p, C.c_void_p]
+        lib.sbfs_kernel_name.restype = C.c_char_p
+        lib.sbfs_kernel_name.argtypes = [C.c_int]
+        lib.sbfs_profile_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                           C.POINTER(C.c_float), C.POINTER(C.c_int)]
+
+    def _call(self, fn, *args):
+        rc = self._fns[fn](*args)
+        if rc != 0:
+            raise SolverError(f"{fn} failed: {self.last_error()}")
+        return rc
+
+    def _ext(self, fn, *args):
+        rc = getattr(self.lib, fn)(*args)
+        if rc != 0:
+            raise SolverError(f"{fn} failed: {self.last_error()}")
+
+    def last_error(self) -> str:
+        return self.lib.sbfs_last_error().decode()
+
+    def set_sync_mode(self, mode: int):
+        self._ext("sbfs_set_sync_mode", mode)
+
+    def set_use_graphs(self, on: bool):
+        self._ext("sbfs_set_use_graphs", 1 if on else 0)
+
+    def set_dt_coefs(self, adv, dif, itf):
+        self._ext("sbfs_set_dt_coefs", adv, dif, itf)
+
+    def invalidate_device(self):
+        self._ext("sbfs_invalidate_device")
+
+    def sync_to_host(self, st: SolverState):
+        self._ext("sbfs_sync_to_host", *self._ptrs(st))
+
+    def run_steps_timed(self, st: SolverState, nsteps: int):
+        ms = C.c_float(0.0)
+        dt = C.c_double(0.0)
+        self._ext("sbfs_run_steps_timed", *self._ptrs(st), nsteps, C.byref(ms), C.byref(dt))
+        return ms.value, dt.value
+
+    def set_device(self, device: int):
+        self._ext("sbfs_set_device", device)
+
+    def pin_host_state(self, st: SolverState):
+        self._ext("sbfs_pin_host_state", C.addressof(st.fluid), C.addressof(st.interface))
+
+    def unpin_host_state(self, st: SolverState):
+        self._ext("sbfs_unpin_host_state", C.addressof(st.fluid), C.addressof(st.interface))
+
+    def profile_steps(self, st: SolverState, nsteps: int) -> dict:
+        """{kernel name: (total ms, launches)} of nsteps eager device-resident steps"""
+        n = self.lib.sbfs_kernel_classes()
+        ms = (C.c_float * n)()
+        cnt = (C.c_int * n)()
+        self._ext("sbfs_profile_steps", *self._ptrs(st), nsteps, ms, cnt)
+        return {self.lib.sbfs_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n)}
+
+    def kernels_per_step(self) -> int:
+        return self.lib.sbfs_kernels_per_step()
+
+    def device_status(self) -> int:
+        s = C.c_int(0)
+        self._ext("sbfs_device_status", C.byref(s))
+        return s.value
+
+    def release(self):
+        self._ext("sbfs_release")
+
+
+def load_library(path: str | None = None, build_if_missing: bool = False) -> GpuLibrary:
+    """Load libsbfs_gb300.so (built in-tree by :func:`build_library`)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIBRARY_PATH
+    if not os.path.exists(p):
+        if build_if_missing:
+            build_library()
+        else:
+            raise RuntimeError(f"{p} is missing: build it with `python -m simplebubblyflowsolver_gb300.build`")
+    lib = GpuLibrary(C.CDLL(p))
+    if path is None:
+        _LIB = lib
+    return lib

@@ -1,0 +1,932 @@
+// C ABI of the GB300 time step: the reference solver's entry points
+// (include/integrate.h, include/decide_dt.h, include/fluid_solver.h,
+// include/interface_solver.h) on top of the kernels of sbfs_kernels.cu.
+//
+// One device context (grid, metrics, device buffers, stream, graphs) is kept
+// per process and rebuilt when the grid changes; this replaces the
+// reference's function-static solver state (src/fluid/compute_potential.c:
+// 427-437, src/decide_dt.c:19-22).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sbfs_gb300.h"
+#include "sbfs_kernels.cuh"
+
+using namespace sbfs;
+
+namespace {
+
+std::string g_err;
+
+int fail(const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return 1;
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) return fail("%s:%d %s: %s", __FILE__, __LINE__, #call,      \
+                                       cudaGetErrorString(e_));                        \
+  } while (0)
+
+// RK3 coefficients (reference src/runge_kutta.c:8-15)
+const double RK_A[3] = {32. / 60., 25. / 60., 45. / 60.};
+const double RK_B[3] = {0. / 60., -17. / 60., -25. / 60.};
+double rk_g(int k) { return RK_A[k] + RK_B[k]; }
+
+int g_sync_mode = SBFS_SYNC_STATE;
+int g_use_graphs = 1;
+double g_coef[3] = {-1., -1., -1.};
+
+// extra cells of every field (reference include/array_macros/)
+struct Layout {
+  int ax0, ax1, ay0, ay1, nc;
+};
+const Layout L_UX{0, 1, 1, 1, 1}, L_UY{1, 1, 1, 1, 1}, L_P{1, 1, 1, 1, 1}, L_DEN{1, 1, 1, 1, 1};
+const Layout L_VISUX{0, 1, 1, 1, 1}, L_VISUY{1, 1, 1, 1, 1}, L_TXX{0, 0, 1, 1, 1}, L_TXY{0, 1, 1, 1, 1};
+const Layout L_TYY{0, 0, 1, 1, 1}, L_SRCUX{-1, 0, 0, 0, 1}, L_SRCUY{0, 0, 0, 0, 1}, L_VOF{1, 1, 2, 2, 1};
+const Layout L_IFRCX{-1, 0, 0, 0, 1}, L_IFRCY{0, 0, 0, 0, 1}, L_DVOF{0, 1, 1, 2, 2}, L_NORMAL{0, 0, 1, 1, 3};
+const Layout L_CURV{1, 1, 1, 1, 1}, L_FLUXX{0, 1, 1, 1, 1}, L_FLUXY{1, 1, 1, 1, 1}, L_SRC{0, 0, 0, 0, 1};
+
+struct Ctx {
+  int nx = 0, ny = 0;
+  double lx = 0., ly = 0.;
+  Grid g{};
+  Metrics m{};
+  Phys ph{};
+  Bufs b{};
+  cudaStream_t s = nullptr;
+  std::vector<void *> allocs;
+  std::vector<double> hxxf;  // host copy used to detect a changed grid
+  double Re = NAN;
+  double dt_fixed = 0.;
+  double *small_host = nullptr;  // pinned: scalars block read back
+  // metrics arrays (device)
+  double *met = nullptr;
+  // role state of the fused step: current velocity, potential, density,
+  // RK-source buffers
+  double *U[2], *V[2], *PSI[2], *DEN[2], *SX[2], *SY[2], *SV[2];
+  int iu = 0, ipsi = 0, iden = 0, isrc = 0;
+  bool resident = false;  // device holds the current state
+  std::map<int, cudaGraphExec_t> graphs;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+
+  ~Ctx() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (void *p : allocs) cudaFree(p);
+    if (small_host) cudaFreeHost(small_host);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+std::unique_ptr<Ctx> g_ctx;
+
+int dalloc(Ctx &c, double **p, size_t n) {
+  void *q = nullptr;
+  CK(cudaMalloc(&q, n * sizeof(double)));
+  CK(cudaMemsetAsync(q, 0, n * sizeof(double), c.s));
+  c.allocs.push_back(q);
+  *p = static_cast<double *>(q);
+  return 0;
+}
+
+bool layout_ok(const array_t &a, const Layout &l) {
+  if (!a.nadds || !a.data) return false;
+  return a.nadds[0][0] == l.ax0 && a.nadds[0][1] == l.ax1 && a.nadds[1][0] == l.ay0 && a.nadds[1][1] == l.ay1 &&
+         a.size == sizeof(double) * l.nc;
+}
+
+int pitch_of(const Ctx &c, const Layout &l) { return l.nc == 1 ? c.g.p1 : (l.nc == 2 ? c.g.p2 : c.g.p3); }
+
+// host array (reference layout, rows J = 1 - ay0 .. ny + ay1) -> device rows J = 1..ny
+int h2d(Ctx &c, const array_t &a, const Layout &l, double *dev) {
+  if (!layout_ok(a, l)) return fail("array layout does not match the reference's (nadds/size)");
+  const size_t row = (size_t)(c.nx + l.ax0 + l.ax1) * l.nc;
+  const double *src = static_cast<const double *>(a.data) + (size_t)l.ay0 * row;
+  CK(cudaMemcpy2DAsync(dev, sizeof(double) * pitch_of(c, l), src, sizeof(double) * row, sizeof(double) * row, c.ny,
+                       cudaMemcpyHostToDevice, c.s));
+  return 0;
+}
+
+// device rows -> host array, ghost rows filled from the periodic images
+int d2h(Ctx &c, array_t &a, const Layout &l, const double *dev) {
+  if (!layout_ok(a, l)) return fail("array layout does not match the reference's (nadds/size)");
+  const size_t row = (size_t)(c.nx + l.ax0 + l.ax1) * l.nc;
+  const size_t pitch = sizeof(double) * pitch_of(c, l);
+  double *dst = static_cast<double *>(a.data);
+  CK(cudaMemcpy2DAsync(dst + (size_t)l.ay0 * row, sizeof(double) * row, dev, pitch, sizeof(double) * row, c.ny,
+                       cudaMemcpyDeviceToHost, c.s));
+  for (int J = 1 - l.ay0; J <= c.ny + l.ay1; ++J) {
+    if (J >= 1 && J <= c.ny) continue;
+    int r = J - 1;
+    while (r < 0) r += c.ny;
+    while (r >= c.ny) r -= c.ny;
+    CK(cudaMemcpyAsync(dst + (size_t)(J - 1 + l.ay0) * row, reinterpret_cast<const char *>(dev) + pitch * r,
+                       sizeof(double) * row, cudaMemcpyDeviceToHost, c.s));
+  }
+  return 0;
+}
+
+int sync(Ctx &c) {
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c.s));
+  return 0;
+}
+
+int load_coefs() {
+  if (g_coef[0] >= 0. && g_coef[1] >= 0. && g_coef[2] >= 0.) return 0;
+  const char *keys[3] = {"coef_dt_adv", "coef_dt_dif", "coef_dt_int"};
+  for (int k = 0; k < 3; ++k) {
+    const char *v = getenv(keys[k]);
+    if (!v) return fail("%s not found", keys[k]);
+    g_coef[k] = strtod(v, nullptr);
+  }
+  return 0;
+}
+
+int check_domain(const domain_t *d) {
+  if (!d || !d->hxxf || !d->hxxc || !d->jdxf || !d->jdxc) return fail("domain_t is not initialised");
+  const long nx = (long)d->mysizes[0], ny = (long)d->mysizes[1];
+  if (d->glsizes[0] != d->mysizes[0] || d->glsizes[1] != d->mysizes[1])
+    return fail("domain is decomposed; this library runs the whole domain on one GPU");
+  if (nx < 4 || nx > 8192) return fail("nx = %ld outside 4..8192", nx);
+  if (ny < 8 || (ny & (ny - 1)) != 0) return fail("ny = %ld must be a power of two >= 8", ny);
+  // the reference accepts uniform x grids only (src/domain.c:78-98, 213-219)
+  double lo = 1e300, hi = -1e300;
+  for (long i = 0; i < nx; ++i) {
+    lo = fmin(lo, d->hxxc[i]);
+    hi = fmax(hi, d->hxxc[i]);
+  }
+  if (!(fabs(hi - lo) < 1.e-15)) return fail("x grid is not uniform");
+  return 0;
+}
+
+// per-column coefficients with the reference's expressions
+int upload_metrics(Ctx &c, const domain_t *d, double Re) {
+  const int nx = c.nx, n = nx + 3;
+  const double hy = d->hy;
+  const double nu = 1. / Re;
+  std::vector<double> h(13 * (size_t)n, 0.);
+  auto A = [&](int k, int I) -> double & { return h[(size_t)k * n + I]; };
+  for (int I = 1; I <= nx + 1; ++I) {
+    const double hf = d->hxxf[I - 1], jf = d->jdxf[I - 1];
+    A(0, I) = 1. / hf;
+    A(2, I) = 1. / jf;
+    A(4, I) = jf / hf;
+    A(6, I) = jf / hy;
+    A(8, I) = 0.5 * jf / hf;
+    A(10, I) = nu / jf;
+    A(12, I) = hf;
+  }
+  for (int I = 1; I <= nx; ++I) {
+    const double hc = d->hxxc[I - 1], jc = d->jdxc[I - 1];
+    A(1, I) = 1. / hc;
+    A(3, I) = 1. / jc;
+    A(5, I) = jc / hc;
+    A(7, I) = jc / hy;
+    A(9, I) = 0.5 * jc / hy;
+    A(11, I) = nu / jc;
+  }
+  if (!c.met) {
+    if (dalloc(c, &c.met, h.size())) return 1;
+  }
+  CK(cudaMemcpyAsync(c.met, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.s));
+  const double *b = c.met;
+  c.m.ihxxf = b + 0 * n;
+  c.m.ihxxc = b + 1 * n;
+  c.m.ijdxf = b + 2 * n;
+  c.m.ijdxc = b + 3 * n;
+  c.m.qf = b + 4 * n;
+  c.m.qc = b + 5 * n;
+  c.m.qf_hy = b + 6 * n;
+  c.m.qc_hy = b + 7 * n;
+  c.m.hqf = b + 8 * n;
+  c.m.hqc_hy = b + 9 * n;
+  c.m.nu_ijdxf = b + 10 * n;
+  c.m.nu_ijdxc = b + 11 * n;
+  c.m.hxxf = b + 12 * n;
+  c.Re = Re;
+  // the constant part of decide_dt: diffusive and capillary limits
+  // (src/decide_dt.c:79-130)
+  return 0;
+}
+
+void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
+  Phys &p = c.ph;
+  p.denr = f->denr;
+  p.visr = f->visr;
+  p.refden = f->refden;
+  p.den_lo = fmin(1., f->denr);
+  p.den_hi = fmax(1., f->denr);
+  p.vis_lo = fmin(1., f->visr);
+  p.vis_hi = fmax(1., f->visr);
+  p.grav = -1. / f->Fr / f->Fr;
+  p.tension = itf ? 1. / itf->We : 0.;
+  p.force_coef = 2. / (1. + f->denr) * p.tension;
+  p.irefden = 1. / f->refden;
+}
+
+double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
+  double hxmin = 1.79769313486231570e+308;
+  for (int i = 2; i <= c.nx; ++i) hxmin = fmin(hxmin, d->hxxf[i - 1]);
+  const double h[2] = {hxmin, d->hy};
+  const double diffusivity = 1. / f->Re;
+  const double tension = 1. / itf->We;
+  const double pi = 3.1415926535897932384626433832;
+  double out = 1.e300;
+  for (int k = 0; k < 2; ++k) {
+    double dif = fmin(1., f->denr / f->visr) / diffusivity * 0.5 / 2 * pow(h[k], 2.);
+    dif *= g_coef[1];
+    out = fmin(out, dif);
+  }
+  double cap = 1.;
+  for (int k = 0; k < 2; ++k) cap = fmin(cap, sqrt(1. / tension / 4. / pi * pow(h[k], 3.)));
+  cap *= g_coef[2];
+  return fmin(out, cap);
+}
+
+// Thomas pivots of the x operator per y wavenumber and the FFT twiddles
+int upload_poisson(Ctx &c, const domain_t *d) {
+  const int nx = c.nx, ny = c.ny, M1 = ny / 2 + 1;
+  const double pi = 3.14159265358979323846;
+  const double dx = d->lengths[0] / nx;
+  const double offx = 1. / (dx * dx);
+  const double offy = 1. / d->hy / d->hy;
+  std::vector<double2> fac((size_t)nx * M1);
+  for (int m = 0; m < M1; ++m) {
+    const double s = sin(pi * m / ny);
+    const double lam = -4. * offy * s * s;
+    double v_prev = 0.;
+    for (int i = 0; i < nx; ++i) {
+      const double diag = (i == 0 || i == nx - 1 ? -offx : -2. * offx) + lam;
+      const double piv = diag - (i == 0 ? 0. : offx * v_prev);
+      double w = 1. / piv, v = offx * w;
+      if (i == nx - 1 && fabs(piv) < 1.e-10 * offx) {
+        // singular mode (m = 0, Neumann-Neumann): pin the last unknown; the
+        // kernel removes the mean afterwards
+        w = 0.;
+        v = 0.;
+      }
+      fac[(size_t)i * M1 + m] = make_double2(w, v);
+      v_prev = v;
+    }
+  }
+  CK(cudaMemcpyAsync(c.b.tdm_fac, fac.data(), fac.size() * sizeof(double2), cudaMemcpyHostToDevice, c.s));
+  std::vector<double2> tw(M1);
+  for (int m = 0; m < M1; ++m) tw[m] = make_double2(cos(2. * pi * m / ny), -sin(2. * pi * m / ny));
+  CK(cudaMemcpyAsync(c.b.twiddle, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, c.s));
+  // tw and fac are staged from host vectors: make sure the copies finished
+  CK(cudaStreamSynchronize(c.s));
+  return 0;
+}
+
+int make_ctx(const domain_t *d) {
+  g_ctx.reset();
+  auto c = std::make_unique<Ctx>();
+  c->nx = (int)d->mysizes[0];
+  c->ny = (int)d->mysizes[1];
+  c->lx = d->lengths[0];
+  c->ly = d->lengths[1];
+  c->hxxf.assign(d->hxxf, d->hxxf + c->nx + 1);
+  CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&c->e0));
+  CK(cudaEventCreate(&c->e1));
+  cudaError_t e = configure_kernels();
+  if (e != cudaSuccess) return fail("configure_kernels: %s", cudaGetErrorString(e));
+  Grid &g = c->g;
+  g.nx = c->nx;
+  g.ny = c->ny;
+  auto rnd = [](int n) { return (n + 31) / 32 * 32; };
+  g.p1 = rnd(c->nx + 2);
+  g.p2 = rnd(2 * (c->nx + 1));
+  g.p3 = rnd(3 * c->nx);
+  g.hy = d->hy;
+  g.ihy = 1. / d->hy;
+  const size_t n1 = (size_t)g.p1 * g.ny, n2 = (size_t)g.p2 * g.ny, n3 = (size_t)g.p3 * g.ny;
+  Bufs &b = c->b;
+  double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
+                     &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
+                     &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
+                     &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.irhox, &b.irhoy};
+  for (double **p : scal)
+    if (dalloc(*c, p, n1)) return 1;
+  if (dalloc(*c, &b.dvof, n2)) return 1;
+  if (dalloc(*c, &b.normal, n3)) return 1;
+  const int M1 = g.ny / 2 + 1;
+  double *tmp = nullptr;
+  if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1)) return 1;
+  b.spec = reinterpret_cast<double2 *>(tmp);
+  if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1)) return 1;
+  b.tdm_fac = reinterpret_cast<double2 *>(tmp);
+  if (dalloc(*c, &tmp, 2 * (size_t)M1)) return 1;
+  b.twiddle = reinterpret_cast<double2 *>(tmp);
+  if (dalloc(*c, &tmp, (size_t)c->nx + 8)) return 1;
+  b.dt_acc = reinterpret_cast<unsigned long long *>(tmp);
+  if (dalloc(*c, &tmp, kScalars + 2)) return 1;
+  b.scalars = tmp;
+  b.status = reinterpret_cast<int *>(tmp + kScalars);
+  CK(cudaMallocHost(&c->small_host, sizeof(double) * (kScalars + 2)));
+  if (upload_poisson(*c, d)) return 1;
+  c->U[0] = b.ux;
+  c->U[1] = b.ux_star;
+  c->V[0] = b.uy;
+  c->V[1] = b.uy_star;
+  c->PSI[0] = b.psi0;
+  c->PSI[1] = b.psi1;
+  c->DEN[0] = b.den0;
+  c->DEN[1] = b.den1;
+  c->SX[0] = b.srcux[0];
+  c->SX[1] = b.srcux[1];
+  c->SY[0] = b.srcuy[0];
+  c->SY[1] = b.srcuy[1];
+  c->SV[0] = b.srcvof[0];
+  c->SV[1] = b.srcvof[1];
+  g_ctx = std::move(c);
+  return 0;
+}
+
+// context for this domain and physics; rebuilt when the grid changes
+Ctx *get_ctx(const domain_t *d, const fluid_t *f, const interface_t *itf) {
+  if (check_domain(d)) return nullptr;
+  Ctx *c = g_ctx.get();
+  bool same_grid = c && c->nx == (int)d->mysizes[0] && c->ny == (int)d->mysizes[1] && c->lx == d->lengths[0] &&
+                   c->ly == d->lengths[1] && c->g.hy == d->hy &&
+                   memcmp(c->hxxf.data(), d->hxxf, sizeof(double) * (c->nx + 1)) == 0;
+  if (!same_grid) {
+    if (make_ctx(d)) return nullptr;
+    c = g_ctx.get();
+  }
+  const double Re = f ? f->Re : (std::isnan(c->Re) ? 1. : c->Re);
+  if (!c->met || !(c->Re == Re)) {
+    if (upload_metrics(*c, d, Re)) return nullptr;
+  }
+  if (f) set_phys(*c, f, itf);
+  return c;
+}
+
+// scalars block for a fine-grained call: substage k of step size dt, and/or
+// explicit dt_old / dt_new in slot 0
+int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
+  double *h = c.small_host;
+  for (int i = 0; i < kScalars; ++i) h[i] = 0.;
+  h[0] = dt;
+  if (k >= 0) {
+    h[sc_adt(k)] = RK_A[k] * dt;
+    h[sc_bdt(k)] = RK_B[k] * dt;
+    h[sc_gdt(k)] = rk_g(k) * dt;
+  }
+  if (dt_new != 0.) {
+    h[sc_dtold(0)] = dt_old;
+    h[sc_dtnew(0)] = dt_new;
+    h[sc_pdiv(0)] = c.ph.refden / dt_new / c.ny;
+    h[sc_padd(0)] = -(dt_old / dt_new) / c.ny;
+    h[sc_cnew(0)] = dt_new / c.ph.refden;
+    h[sc_cold(0)] = -dt_old;
+  }
+  CK(cudaMemcpyAsync(c.b.scalars, h, sizeof(double) * kScalars, cudaMemcpyHostToDevice, c.s));
+  // h is reused by the next call: wait for the copy
+  CK(cudaStreamSynchronize(c.s));
+  return 0;
+}
+
+void swap_data(array_t &a, array_t &b) {
+  void *t = a.data;
+  a.data = b.data;
+  b.data = t;
+}
+
+// ---------------------------------------------------------------------------
+// fused step
+// ---------------------------------------------------------------------------
+
+// optional per-kernel event timing of the fused step (eager launches only)
+struct Prof {
+  bool on = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  cudaEvent_t get() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+} g_prof;
+
+enum KernelClass {
+  KC_PROPS, KC_NORMAL_CURV, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_STRESS, KC_PREDICT,
+  KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_COUNT
+};
+const char *kKernelNames[KC_COUNT] = {"k_props", "k_normal_curv", "k_flux_force", "k_vof_advance", "k_stress",
+                                      "k_predict", "k_poisson_fwd", "k_poisson_tdm", "k_poisson_inv", "k_correct",
+                                      "k_decide_dt"};
+
+template <class F>
+void timed(Ctx &c, int cls, F &&launch) {
+  if (!g_prof.on) {
+    launch();
+    return;
+  }
+  cudaEvent_t a = g_prof.get(), b = g_prof.get();
+  cudaEventRecord(a, c.s);
+  launch();
+  cudaEventRecord(b, c.s);
+  g_prof.marks.push_back({cls, {a, b}});
+}
+
+void enqueue_substage(Ctx &c, int k) {
+  Bufs &b = c.b;
+  if (k != 0) c.isrc ^= 1;  // stash the previous stage's sources (pointer swap)
+  double *ux = c.U[c.iu], *uy = c.V[c.iu], *uxs = c.U[c.iu ^ 1], *uys = c.V[c.iu ^ 1];
+  double *den0 = c.DEN[c.iden], *den1 = c.DEN[c.iden ^ 1];
+  double *psio = c.PSI[c.ipsi], *psin = c.PSI[c.ipsi ^ 1];
+  double *sxa = c.SX[c.isrc], *sxb = c.SX[c.isrc ^ 1];
+  double *sya = c.SY[c.isrc], *syb = c.SY[c.isrc ^ 1];
+  double *sva = c.SV[c.isrc], *svb = c.SV[c.isrc ^ 1];
+  const double *sc = b.scalars;
+  timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+  timed(c, KC_NORMAL_CURV, [&] { launch_normal_curv(c.s, c.g, c.m, b, true, true); });
+  timed(c, KC_FLUX_FORCE, [&] { launch_flux_force(c.s, c.g, c.m, c.ph, b, ux, uy, den0, true, true); });
+  timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
+  timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
+  timed(c, KC_PREDICT, [&] {
+    launch_predict(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, b.mfluxx, b.mfluxy, den0, den1, sxa, sxb,
+                   nullptr, sya, syb, nullptr);
+  });
+  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, c.m, c.ph, b, sc, k, uxs, uys, psio); });
+  timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
+  timed(c, KC_POISSON_INV, [&] { launch_poisson_inv(c.s, c.g, b, psin); });
+  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, c.ph, b, sc, k, uxs, uys, psin, psio, true); });
+  c.iu ^= 1;
+  c.ipsi ^= 1;
+  c.iden ^= 1;
+}
+
+constexpr int kKernelsPerStep = 1 + 3 * 10;
+
+void enqueue_step(Ctx &c) {
+  timed(c, KC_DECIDE_DT,
+        [&] { launch_decide_dt(c.s, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]); });
+  for (int k = 0; k < 3; ++k) enqueue_substage(c, k);
+}
+
+int role_key(const Ctx &c) { return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3); }
+
+int launch_step(Ctx &c) {
+  if (!g_use_graphs || g_prof.on) {
+    enqueue_step(c);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  const int key = role_key(c);
+  auto it = c.graphs.find(key);
+  if (it == c.graphs.end()) {
+    const int iu = c.iu, ipsi = c.ipsi, iden = c.iden, isrc = c.isrc;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(c);
+    cudaError_t e = cudaStreamEndCapture(c.s, &graph);
+    if (e != cudaSuccess) return fail("graph capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t exec;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail("graph instantiate: %s", cudaGetErrorString(e));
+    it = c.graphs.emplace(key, exec).first;
+    // capturing advanced the roles; restore, the launch below advances them
+    c.iu = iu;
+    c.ipsi = ipsi;
+    c.iden = iden;
+    c.isrc = isrc;
+  }
+  CK(cudaGraphLaunch(it->second, c.s));
+  // roles after one step (3 substages: velocity, potential and density flip
+  // three times, the RK sources twice)
+  c.iu ^= 1;
+  c.ipsi ^= 1;
+  c.iden ^= 1;
+  return 0;
+}
+
+int upload_state(Ctx &c, const fluid_t *f, const interface_t *itf) {
+  if (h2d(c, f->ux, L_UX, c.U[c.iu]) || h2d(c, f->uy, L_UY, c.V[c.iu]) || h2d(c, f->p, L_P, c.b.p) ||
+      h2d(c, f->psi[0], L_P, c.PSI[c.ipsi]) || h2d(c, itf->vof, L_VOF, c.b.vof))
+    return 1;
+  // rho^k of the current vof (src/fluid/density.c)
+  launch_props(c.s, c.g, c.m, c.ph, c.b, true, false, false, c.DEN[c.iden]);
+  c.resident = true;
+  return 0;
+}
+
+int download_state(Ctx &c, fluid_t *f, interface_t *itf, bool all) {
+  // the reference's psi pointers end a step swapped (three swaps)
+  if (d2h(c, f->ux, L_UX, c.U[c.iu]) || d2h(c, f->uy, L_UY, c.V[c.iu]) || d2h(c, f->p, L_P, c.b.p) ||
+      d2h(c, f->psi[0], L_P, c.PSI[c.ipsi]) || d2h(c, f->psi[1], L_P, c.PSI[c.ipsi ^ 1]) ||
+      d2h(c, itf->vof, L_VOF, c.b.vof))
+    return 1;
+  if (all) {
+    Bufs &b = c.b;
+    if (d2h(c, f->den[0], L_DEN, c.DEN[c.iden ^ 1]) || d2h(c, f->den[1], L_DEN, c.DEN[c.iden]) ||
+        d2h(c, f->visux, L_VISUX, b.visux) || d2h(c, f->visuy, L_VISUY, b.visuy) ||
+        d2h(c, f->txx, L_TXX, b.txx) || d2h(c, f->txy, L_TXY, b.txy) || d2h(c, f->tyy, L_TYY, b.tyy) ||
+        d2h(c, f->srcux[0], L_SRCUX, c.SX[c.isrc]) || d2h(c, f->srcux[1], L_SRCUX, c.SX[c.isrc ^ 1]) ||
+        d2h(c, f->srcuy[0], L_SRCUY, c.SY[c.isrc]) || d2h(c, f->srcuy[1], L_SRCUY, c.SY[c.isrc ^ 1]) ||
+        d2h(c, itf->ifrcx, L_IFRCX, b.ifrcx) || d2h(c, itf->ifrcy, L_IFRCY, b.ifrcy) ||
+        d2h(c, itf->dvof, L_DVOF, b.dvof) || d2h(c, itf->normal, L_NORMAL, b.normal) ||
+        d2h(c, itf->curv, L_CURV, b.curv) || d2h(c, itf->fluxx, L_FLUXX, b.mfluxx) ||
+        d2h(c, itf->fluxy, L_FLUXY, b.mfluxy) || d2h(c, itf->src[0], L_SRC, c.SV[c.isrc]) ||
+        d2h(c, itf->src[1], L_SRC, c.SV[c.isrc ^ 1]))
+      return 1;
+  }
+  return 0;
+}
+
+int read_dt_status(Ctx &c, double *dt, int *status) {
+  CK(cudaMemcpyAsync(c.small_host, c.b.scalars, sizeof(double) * (kScalars + 1), cudaMemcpyDeviceToHost, c.s));
+  if (sync(c)) return 1;
+  if (dt) *dt = c.small_host[0];
+  if (status) memcpy(status, c.small_host + kScalars, sizeof(int));
+  return 0;
+}
+
+Ctx *prepare_step(const domain_t *d, fluid_t *f, interface_t *itf) {
+  if (!f || !itf) {
+    fail("null fluid or interface");
+    return nullptr;
+  }
+  if (load_coefs()) return nullptr;
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return nullptr;
+  c->dt_fixed = fixed_dt(*c, d, f, itf);
+  return c;
+}
+
+}  // namespace
+
+// ===========================================================================
+// exported entry points
+// ===========================================================================
+extern "C" {
+
+const char *sbfs_last_error(void) { return g_err.c_str(); }
+
+int sbfs_set_sync_mode(int mode) {
+  if (mode < SBFS_SYNC_STATE || mode > SBFS_SYNC_NONE) return fail("bad sync mode %d", mode);
+  g_sync_mode = mode;
+  return 0;
+}
+
+int sbfs_set_use_graphs(int on) {
+  g_use_graphs = on ? 1 : 0;
+  return 0;
+}
+
+int sbfs_set_dt_coefs(double adv, double dif, double itf) {
+  if (!(adv >= 0.) || !(dif >= 0.) || !(itf >= 0.)) return fail("dt safety factors must be non-negative");
+  g_coef[0] = adv;
+  g_coef[1] = dif;
+  g_coef[2] = itf;
+  return 0;
+}
+
+int sbfs_invalidate_device(void) {
+  if (g_ctx) g_ctx->resident = false;
+  return 0;
+}
+
+int sbfs_kernels_per_step(void) { return kKernelsPerStep; }
+
+int sbfs_set_device(int device) {
+  g_ctx.reset();
+  CK(cudaSetDevice(device));
+  return 0;
+}
+
+int sbfs_pin_host_state(fluid_t *f, interface_t *itf) {
+  void *ptrs[] = {f->ux.data, f->uy.data, f->p.data, f->psi[0].data, f->psi[1].data, itf->vof.data};
+  size_t sizes[] = {f->ux.datasize, f->uy.datasize, f->p.datasize, f->psi[0].datasize, f->psi[1].datasize,
+                    itf->vof.datasize};
+  for (int i = 0; i < 6; ++i) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, ptrs[i]) == cudaSuccess && at.type == cudaMemoryTypeHost) continue;
+    cudaGetLastError();
+    CK(cudaHostRegister(ptrs[i], sizes[i], cudaHostRegisterDefault));
+  }
+  return 0;
+}
+
+int sbfs_unpin_host_state(fluid_t *f, interface_t *itf) {
+  void *ptrs[] = {f->ux.data, f->uy.data, f->p.data, f->psi[0].data, f->psi[1].data, itf->vof.data};
+  for (void *p : ptrs) {
+    if (cudaHostUnregister(p) != cudaSuccess) cudaGetLastError();
+  }
+  return 0;
+}
+
+const char *sbfs_kernel_name(int cls) { return (cls >= 0 && cls < KC_COUNT) ? kKernelNames[cls] : ""; }
+int sbfs_kernel_classes(void) { return KC_COUNT; }
+
+int sbfs_profile_steps(const domain_t *d, fluid_t *f, interface_t *itf, int nsteps, float *ms_per_class,
+                       int *launches_per_class) {
+  Ctx *c = prepare_step(d, f, itf);
+  if (!c) return 1;
+  if (!c->resident) {
+    if (upload_state(*c, f, itf)) return 1;
+  }
+  g_prof.on = true;
+  g_prof.used = 0;
+  g_prof.marks.clear();
+  int rc = 0;
+  for (int n = 0; n < nsteps && !rc; ++n) rc = launch_step(*c);
+  g_prof.on = false;
+  if (rc) return 1;
+  if (sync(*c)) return 1;
+  for (int k = 0; k < KC_COUNT; ++k) {
+    ms_per_class[k] = 0.f;
+    launches_per_class[k] = 0;
+  }
+  for (auto &mk : g_prof.marks) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, mk.second.first, mk.second.second));
+    ms_per_class[mk.first] += ms;
+    launches_per_class[mk.first] += 1;
+  }
+  int status = 0;
+  if (read_dt_status(*c, nullptr, &status)) return 1;
+  return (status & 1) ? fail("non-finite velocity detected by decide_dt") : 0;
+}
+
+int sbfs_release(void) {
+  g_ctx.reset();
+  return 0;
+}
+
+int sbfs_device_status(int *status) {
+  if (!g_ctx) {
+    *status = 0;
+    return 0;
+  }
+  return read_dt_status(*g_ctx, nullptr, status);
+}
+
+int sbfs_sync_to_host(const domain_t *d, fluid_t *f, interface_t *itf) {
+  Ctx *c = g_ctx.get();
+  if (!c || !c->resident) return 0;
+  (void)d;
+  if (download_state(*c, f, itf, g_sync_mode == SBFS_SYNC_ALL)) return 1;
+  return sync(*c);
+}
+
+// reference src/integrate.c:11-70
+int integrate(const domain_t *d, fluid_t *f, interface_t *itf, double *dt) {
+  Ctx *c = prepare_step(d, f, itf);
+  if (!c) return 1;
+  if (g_sync_mode != SBFS_SYNC_NONE || !c->resident) {
+    if (upload_state(*c, f, itf)) return 1;
+  }
+  if (launch_step(*c)) return 1;
+  if (g_sync_mode != SBFS_SYNC_NONE) {
+    swap_data(f->psi[0], f->psi[1]);
+    if (download_state(*c, f, itf, g_sync_mode == SBFS_SYNC_ALL)) return 1;
+  }
+  int status = 0;
+  if (read_dt_status(*c, dt, &status)) return 1;
+  if (status & 1) return fail("non-finite velocity detected by decide_dt");
+  return 0;
+}
+
+int sbfs_run_steps_timed(const domain_t *d, fluid_t *f, interface_t *itf, int nsteps, float *ms, double *dt_last) {
+  Ctx *c = prepare_step(d, f, itf);
+  if (!c) return 1;
+  if (!c->resident) {
+    if (upload_state(*c, f, itf)) return 1;
+  }
+  CK(cudaEventRecord(c->e0, c->s));
+  for (int n = 0; n < nsteps; ++n)
+    if (launch_step(*c)) return 1;
+  CK(cudaEventRecord(c->e1, c->s));
+  if (sync(*c)) return 1;
+  CK(cudaEventElapsedTime(ms, c->e0, c->e1));
+  int status = 0;
+  if (read_dt_status(*c, dt_last, &status)) return 1;
+  if (status & 1) return fail("non-finite velocity detected by decide_dt");
+  return 0;
+}
+
+// reference src/decide_dt.c:140-169
+int decide_dt(const domain_t *d, const fluid_t *f, const interface_t *itf, double *dt) {
+  Ctx *c = prepare_step(d, const_cast<fluid_t *>(f), const_cast<interface_t *>(itf));
+  if (!c) return 1;
+  c->resident = false;
+  if (h2d(*c, f->ux, L_UX, c->b.ux) || h2d(*c, f->uy, L_UY, c->b.uy)) return 1;
+  launch_decide_dt(c->s, c->g, c->m, c->ph, c->b, c->b.ux, c->b.uy, c->dt_fixed, g_coef[0]);
+  int status = 0;
+  if (read_dt_status(*c, dt, &status)) return 1;
+  if (status & 1) {
+    CK(cudaMemsetAsync(c->b.status, 0, sizeof(int), c->s));
+    return fail("non-finite velocity detected by decide_dt");
+  }
+  return 0;
+}
+
+// reference src/fluid/density.c:9-31
+int fluid_compute_density(const domain_t *d, fluid_t *f, const interface_t *itf, const size_t index) {
+  if (index > 1) return fail("density index %zu out of range", index);
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return 1;
+  c->resident = false;
+  if (h2d(*c, itf->vof, L_VOF, c->b.vof)) return 1;
+  launch_props(c->s, c->g, c->m, c->ph, c->b, true, false, false, c->b.den0);
+  if (d2h(*c, f->den[index], L_DEN, c->b.den0)) return 1;
+  return sync(*c);
+}
+
+// reference src/fluid/viscosity.c:93-108
+int fluid_compute_viscosity(const domain_t *d, fluid_t *f, const interface_t *itf) {
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return 1;
+  c->resident = false;
+  if (h2d(*c, itf->vof, L_VOF, c->b.vof)) return 1;
+  launch_props(c->s, c->g, c->m, c->ph, c->b, false, true, false, nullptr);
+  if (d2h(*c, f->visux, L_VISUX, c->b.visux) || d2h(*c, f->visuy, L_VISUY, c->b.visuy)) return 1;
+  return sync(*c);
+}
+
+// reference src/interface/curvature_tensor.c:137-145
+int interface_compute_curvature_tensor(const domain_t *d, interface_t *itf) {
+  Ctx *c = get_ctx(d, nullptr, itf);
+  if (!c) return 1;
+  c->resident = false;
+  // cells outside the interface band keep their previous normal, as in the reference
+  if (h2d(*c, itf->vof, L_VOF, c->b.vof) || h2d(*c, itf->normal, L_NORMAL, c->b.normal)) return 1;
+  launch_props(c->s, c->g, c->m, c->ph, c->b, false, false, true, nullptr);
+  launch_normal_curv(c->s, c->g, c->m, c->b, true, true);
+  if (d2h(*c, itf->dvof, L_DVOF, c->b.dvof) || d2h(*c, itf->normal, L_NORMAL, c->b.normal) ||
+      d2h(*c, itf->curv, L_CURV, c->b.curv))
+    return 1;
+  return sync(*c);
+}
+
+// reference src/interface/force.c:90-98
+int interface_compute_force(const domain_t *d, const fluid_t *f, interface_t *itf) {
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return 1;
+  c->resident = false;
+  if (h2d(*c, f->den[0], L_DEN, c->b.den0) || h2d(*c, itf->vof, L_VOF, c->b.vof) ||
+      h2d(*c, itf->curv, L_CURV, c->b.curv))
+    return 1;
+  launch_flux_force(c->s, c->g, c->m, c->ph, c->b, c->b.ux, c->b.uy, c->b.den0, false, true);
+  if (d2h(*c, itf->ifrcx, L_IFRCX, c->b.ifrcx) || d2h(*c, itf->ifrcy, L_IFRCY, c->b.ifrcy)) return 1;
+  return sync(*c);
+}
+
+// reference src/interface/update/main.c:122-136
+int interface_update_vof(const domain_t *d, const size_t rkstep, const double dt, const fluid_t *f,
+                         interface_t *itf) {
+  if (rkstep > 2) return fail("rkstep %zu out of range", rkstep);
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return 1;
+  c->resident = false;
+  if (rkstep != 0) swap_data(itf->src[0], itf->src[1]);
+  Bufs &b = c->b;
+  if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, itf->vof, L_VOF, b.vof) ||
+      h2d(*c, itf->normal, L_NORMAL, b.normal) || h2d(*c, itf->src[1], L_SRC, b.srcvof[1]))
+    return 1;
+  if (put_scalars(*c, dt, (int)rkstep, 0., 0.)) return 1;
+  launch_flux_force(c->s, c->g, c->m, c->ph, b, b.ux, b.uy, b.den0, true, false);
+  launch_vof_advance(c->s, c->g, c->m, c->ph, b, b.scalars, (int)rkstep, b.srcvof[0], b.srcvof[1], false, b.ux,
+                     b.uy, nullptr);
+  if (d2h(*c, itf->fluxx, L_FLUXX, b.fluxx) || d2h(*c, itf->fluxy, L_FLUXY, b.fluxy) ||
+      d2h(*c, itf->src[0], L_SRC, b.srcvof[0]) || d2h(*c, itf->vof, L_VOF, b.vof))
+    return 1;
+  return sync(*c);
+}
+
+// reference src/interface/mass_flux.c:48-58
+int interface_compute_mass_flux(const domain_t *d, const fluid_t *f, interface_t *itf) {
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return 1;
+  c->resident = false;
+  Bufs &b = c->b;
+  if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, itf->fluxx, L_FLUXX, b.fluxx) ||
+      h2d(*c, itf->fluxy, L_FLUXY, b.fluxy))
+    return 1;
+  launch_mass_flux_inplace(c->s, c->g, c->ph, b, b.ux, b.uy);
+  if (d2h(*c, itf->fluxx, L_FLUXX, b.fluxx) || d2h(*c, itf->fluxy, L_FLUXY, b.fluxy)) return 1;
+  return sync(*c);
+}
+
+// reference src/fluid/predict/main.c:60-80
+int fluid_predict_field(const domain_t *d, const size_t rkstep, const double dt, fluid_t *f,
+                        const interface_t *itf) {
+  if (rkstep > 2) return fail("rkstep %zu out of range", rkstep);
+  Ctx *c = get_ctx(d, f, itf);
+  if (!c) return 1;
+  c->resident = false;
+  if (rkstep != 0) {
+    swap_data(f->srcux[0], f->srcux[1]);
+    swap_data(f->srcuy[0], f->srcuy[1]);
+  }
+  Bufs &b = c->b;
+  if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, f->visux, L_VISUX, b.visux) ||
+      h2d(*c, f->visuy, L_VISUY, b.visuy) || h2d(*c, itf->fluxx, L_FLUXX, b.mfluxx) ||
+      h2d(*c, itf->fluxy, L_FLUXY, b.mfluxy) || h2d(*c, f->p, L_P, b.p) || h2d(*c, itf->ifrcx, L_IFRCX, b.ifrcx) ||
+      h2d(*c, itf->ifrcy, L_IFRCY, b.ifrcy) || h2d(*c, f->den[0], L_DEN, b.den0) ||
+      h2d(*c, f->den[1], L_DEN, b.den1) || h2d(*c, f->srcux[1], L_SRCUX, b.srcux[1]) ||
+      h2d(*c, f->srcuy[1], L_SRCUY, b.srcuy[1]))
+    return 1;
+  if (put_scalars(*c, dt, (int)rkstep, 0., 0.)) return 1;
+  launch_stress(c->s, c->g, c->m, b, b.ux, b.uy);
+  launch_predict(c->s, c->g, c->m, c->ph, b, b.scalars, (int)rkstep, b.ux, b.uy, b.ux_star, b.uy_star, b.mfluxx,
+                 b.mfluxy, b.den0, b.den1, b.srcux[0], b.srcux[1], b.srcux[2], b.srcuy[0], b.srcuy[1], b.srcuy[2]);
+  if (d2h(*c, f->txx, L_TXX, b.txx) || d2h(*c, f->txy, L_TXY, b.txy) || d2h(*c, f->tyy, L_TYY, b.tyy) ||
+      d2h(*c, f->srcux[0], L_SRCUX, b.srcux[0]) || d2h(*c, f->srcux[2], L_SRCUX, b.srcux[2]) ||
+      d2h(*c, f->srcuy[0], L_SRCUY, b.srcuy[0]) || d2h(*c, f->srcuy[2], L_SRCUY, b.srcuy[2]) ||
+      d2h(*c, f->ux, L_UX, b.ux_star) || d2h(*c, f->uy, L_UY, b.uy_star))
+    return 1;
+  return sync(*c);
+}
+
+// reference src/fluid/compute_potential.c:421-469
+int fluid_compute_potential(const domain_t *d, const double dt_old, const double dt_new, fluid_t *f) {
+  Ctx *c = get_ctx(d, f, nullptr);
+  if (!c) return 1;
+  c->resident = false;
+  Bufs &b = c->b;
+  if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, f->psi[0], L_P, b.psi0) ||
+      h2d(*c, f->den[1], L_DEN, b.den1))
+    return 1;
+  if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
+  launch_inv_face_density(c->s, c->g, b.den1, b.irhox, b.irhoy);
+  launch_poisson(c->s, c->g, c->m, c->ph, b, b.scalars, 0, b.ux, b.uy, b.psi0, b.psi1);
+  if (d2h(*c, f->psi[1], L_P, b.psi1)) return 1;
+  return sync(*c);
+}
+
+// reference src/fluid/correct_velocity/main.c:14-28
+int fluid_correct_velocity(const domain_t *d, const double dt_old, const double dt_new, fluid_t *f) {
+  Ctx *c = get_ctx(d, f, nullptr);
+  if (!c) return 1;
+  c->resident = false;
+  Bufs &b = c->b;
+  if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, f->psi[0], L_P, b.psi0) ||
+      h2d(*c, f->psi[1], L_P, b.psi1) || h2d(*c, f->den[1], L_DEN, b.den1))
+    return 1;
+  if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
+  launch_inv_face_density(c->s, c->g, b.den1, b.irhox, b.irhoy);
+  launch_correct(c->s, c->g, c->m, c->ph, b, b.scalars, 0, b.ux, b.uy, b.psi1, b.psi0, false);
+  if (d2h(*c, f->ux, L_UX, b.ux) || d2h(*c, f->uy, L_UY, b.uy)) return 1;
+  return sync(*c);
+}
+
+// reference src/fluid/update_pressure.c:43-53
+int fluid_update_pressure(const domain_t *d, fluid_t *f) {
+  Ctx *c = get_ctx(d, f, nullptr);
+  if (!c) return 1;
+  c->resident = false;
+  if (h2d(*c, f->p, L_P, c->b.p) || h2d(*c, f->psi[1], L_P, c->b.psi1)) return 1;
+  launch_pressure(c->s, c->g, c->b, c->b.psi1);
+  if (d2h(*c, f->p, L_P, c->b.p)) return 1;
+  if (sync(*c)) return 1;
+  swap_data(f->psi[0], f->psi[1]);
+  return 0;
+}
+
+static int bc_call(const domain_t *d, array_t *a, const Layout &l, int kind) {
+  Ctx *c = get_ctx(d, nullptr, nullptr);
+  if (!c) return 1;
+  c->resident = false;
+  double *buf = c->b.txy;  // scratch
+  if (h2d(*c, *a, l, buf)) return 1;
+  if (kind == 0) launch_bc_ux(c->s, c->g, buf);
+  else if (kind == 1) launch_bc_uy(c->s, c->g, buf);
+  else if (kind == 2) launch_bc_neumann(c->s, c->g, buf);
+  else launch_bc_vof(c->s, c->g, buf);
+  if (d2h(*c, *a, l, buf)) return 1;
+  return sync(*c);
+}
+
+// reference src/fluid/boundary/{ux,uy,p,psi}.c, src/interface/boundary.c
+int fluid_update_boundaries_ux(const domain_t *d, array_t *a) { return bc_call(d, a, L_UX, 0); }
+int fluid_update_boundaries_uy(const domain_t *d, array_t *a) { return bc_call(d, a, L_UY, 1); }
+int fluid_update_boundaries_p(const domain_t *d, array_t *a) { return bc_call(d, a, L_P, 2); }
+int fluid_update_boundaries_psi(const domain_t *d, array_t *a) { return bc_call(d, a, L_P, 2); }
+int interface_update_boundaries_vof(const domain_t *d, array_t *a) { return bc_call(d, a, L_VOF, 3); }
+
+}  // extern "C"

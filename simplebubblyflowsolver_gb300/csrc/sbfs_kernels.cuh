@@ -1,0 +1,77 @@
+// Kernel declarations and the device-buffer bundle shared by the host code.
+#pragma once
+
+#include "sbfs_device.cuh"
+
+namespace sbfs {
+
+// device pointers of one case; every scalar field uses pitch Grid::p1,
+// dvof uses Grid::p2 and normal Grid::p3 (doubles)
+struct Bufs {
+  // state
+  double *ux, *uy, *p, *psi0, *psi1, *vof;
+  // second velocity buffers (predictor output) for the fused step
+  double *ux_star, *uy_star;
+  // properties and interface geometry
+  double *den0, *den1, *visux, *visuy, *txx, *txy, *tyy;
+  double *dvof, *normal, *curv, *ifrcx, *ifrcy;
+  // fluxes: vof fluxes (also the reference's fluxx/fluxy) and mass fluxes
+  double *fluxx, *fluxy, *mfluxx, *mfluxy;
+  // RK sources
+  double *srcux[3], *srcuy[3], *srcvof[2];
+  // inverse face densities 1 / rho^{k+1} at ux and uy faces
+  double *irhox, *irhoy;
+  // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
+  double2 *spec, *tdm_fac;
+  double2 *twiddle;  // exp(-2 pi i m / ny), m = 0..ny/2
+  // decide_dt accumulators and per-step scalars
+  unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
+  double *scalars;             // kScalars doubles
+  int *status;                 // device error word
+};
+
+// ---- launch helpers (defined in sbfs_kernels.cu), all on stream `s`
+void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                  bool den, bool vis, bool grad, double *den_out);
+void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv);
+void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                       const double *ux, const double *uy, const double *den0, bool flux, bool force);
+void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                        const double *sc, int k, double *src_a, const double *src_b, bool fused,
+                        const double *ux, const double *uy, double *den1);
+void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b,
+                              const double *ux, const double *uy);
+void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *ux, const double *uy);
+void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                    const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
+                    const double *mfx, const double *mfy, const double *den0, const double *den1,
+                    double *srcux_a, const double *srcux_b, double *srcux_g,
+                    double *srcuy_a, const double *srcuy_b, double *srcuy_g);
+void launch_poisson(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                    const double *sc, int k, const double *ux, const double *uy, const double *psi_old,
+                    double *psi_new);
+void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                        const double *sc, int k, const double *ux, const double *uy, const double *psi_old);
+void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b);
+void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new);
+void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                    const double *sc, int k, double *ux, double *uy, const double *psi_new,
+                    const double *psi_old, bool pressure);
+void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new);
+void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                      const double *ux, const double *uy, double dt_fixed, double coef_adv);
+void launch_inv_face_density(cudaStream_t s, const Grid &g, const double *den, double *irhox, double *irhoy);
+// boundary kernels of the fine-grained entry points
+void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux);
+void launch_bc_uy(cudaStream_t s, const Grid &g, double *uy);
+void launch_bc_neumann(cudaStream_t s, const Grid &g, double *f);
+void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
+
+// smem budget checks (host side)
+int poisson_fft_cols(int ny);
+int poisson_tdm_modes(int nx);
+size_t poisson_fft_smem(int ny);
+size_t poisson_tdm_smem(int nx);
+cudaError_t configure_kernels();
+
+}  // namespace sbfs
