@@ -282,11 +282,14 @@ def main():
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": round(dom_avg_s * 1e3, 4),
                 "share": round(dom_ms / total, 4),
                 "shares": {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+    fp64_peak = lib.measure_fp64_peak()
+    roofline["fp64_peak_gflops"] = round(fp64_peak, 1)
     if tr and tr.get("fp64_flop"):
-        fp64_peak = float(peaks.get("fp64_gflops", 1011.0))
         ach = tr["fp64_flop"] / dom_avg_s / 1e9
-        roofline["fp64"] = {"achieved": round(ach, 1), "peak": fp64_peak, "unit": "GFLOP/s",
-                            "frac": round(ach / fp64_peak, 4), "peak_source": "FMA microbenchmark (profiles/)"}
+        roofline["fp64"] = {"achieved": round(ach, 1), "peak": round(fp64_peak, 1), "unit": "GFLOP/s",
+                            "frac": round(ach / fp64_peak, 4),
+                            "peak_source": "measured live: FMA loop (sbfs_measure_fp64_peak)",
+                            "flop_source": "ncu sass FP64 instruction counts (profiles/kernel_traffic.txt)"}
 
     # ---- end to end through integrate() with page-locked host buffers
     lib.set_sync_mode(SYNC_STATE)

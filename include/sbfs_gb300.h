@@ -107,6 +107,14 @@ int sbfs_run_steps_timed(const domain_t *domain, fluid_t *fluid, interface_t *in
 /* kernels launched by one integrate() step (for launch accounting) */
 int sbfs_kernels_per_step(void);
 
+/* FP64 fused multiply-add throughput of the current GPU in GFLOP/s (the FP64
+ * roofline denominator), from an 8-chain FMA loop timed with CUDA events */
+int sbfs_measure_fp64_peak(double *gflops);
+
+/* the library's Newton-Raphson reciprocal and inverse square root applied
+ * to n host values on the GPU (accuracy test of the device helpers) */
+int sbfs_check_newton_raphson(const double *x, double *rcp, double *rsq, int n);
+
 /* select the CUDA device for the following calls (drops the current context) */
 int sbfs_set_device(int device);
 

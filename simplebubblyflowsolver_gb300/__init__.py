@@ -43,6 +43,8 @@ class GpuLibrary(ReferenceAPI):
                                              C.POINTER(C.c_float), C.POINTER(C.c_double)]
         lib.sbfs_device_status.argtypes = [C.POINTER(C.c_int)]
         lib.sbfs_set_device.argtypes = [C.c_int]
+        lib.sbfs_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+        lib.sbfs_check_newton_raphson.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int]
         lib.sbfs_pin_host_state.argtypes = [C.c_void_p, C.c_void_p]
         lib.sbfs_unpin_host_state.argtypes = [C.c_void_p, C.c_void_p]
         lib.sbfs_kernel_name.restype = C.c_char_p
@@ -84,6 +86,22 @@ class GpuLibrary(ReferenceAPI):
         dt = C.c_double(0.0)
         self._ext("sbfs_run_steps_timed", *self._ptrs(st), nsteps, C.byref(ms), C.byref(dt))
         return ms.value, dt.value
+
+    def check_newton_raphson(self, x):
+        """(1/x, 1/sqrt(x)) from the device helpers, for accuracy tests"""
+        import numpy as np
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        r = np.empty_like(x)
+        q = np.empty_like(x)
+        dp = C.POINTER(C.c_double)
+        self._ext("sbfs_check_newton_raphson", x.ctypes.data_as(dp), r.ctypes.data_as(dp), q.ctypes.data_as(dp),
+                  x.size)
+        return r, q
+
+    def measure_fp64_peak(self) -> float:
+        out = C.c_double(0.0)
+        self._ext("sbfs_measure_fp64_peak", C.byref(out))
+        return out.value
 
     def set_device(self, device: int):
         self._ext("sbfs_set_device", device)

@@ -176,53 +176,36 @@ int check_domain(const domain_t *d) {
   return 0;
 }
 
-// per-column coefficients with the reference's expressions
+// per-column coefficients (see Metrics)
 int upload_metrics(Ctx &c, const domain_t *d, double Re) {
   const int nx = c.nx, n = nx + 3;
   const double hy = d->hy;
   const double nu = 1. / Re;
-  std::vector<double> h(13 * (size_t)n, 0.);
+  const double dx = d->hxxc[0];
+  std::vector<double> h(6 * (size_t)n, 0.);
   auto A = [&](int k, int I) -> double & { return h[(size_t)k * n + I]; };
   for (int I = 1; I <= nx + 1; ++I) {
-    const double hf = d->hxxf[I - 1], jf = d->jdxf[I - 1];
+    const double hf = d->hxxf[I - 1];
     A(0, I) = 1. / hf;
-    A(2, I) = 1. / jf;
-    A(4, I) = jf / hf;
-    A(6, I) = jf / hy;
-    A(8, I) = 0.5 * jf / hf;
-    A(10, I) = nu / jf;
-    A(12, I) = hf;
+    A(2, I) = 0.25 / hf;
+    A(3, I) = 0.25 * dx / (hf * hy);
+    A(4, I) = nu / hf;
+    A(5, I) = hf;
   }
-  for (int I = 1; I <= nx; ++I) {
-    const double hc = d->hxxc[I - 1], jc = d->jdxc[I - 1];
-    A(1, I) = 1. / hc;
-    A(3, I) = 1. / jc;
-    A(5, I) = jc / hc;
-    A(7, I) = jc / hy;
-    A(9, I) = 0.5 * jc / hy;
-    A(11, I) = nu / jc;
-  }
+  for (int I = 1; I <= nx; ++I) A(1, I) = 1. / d->hxxc[I - 1];
   if (!c.met) {
     if (dalloc(c, &c.met, h.size())) return 1;
   }
   CK(cudaMemcpyAsync(c.met, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.s));
+  CK(cudaStreamSynchronize(c.s));
   const double *b = c.met;
   c.m.ihxxf = b + 0 * n;
   c.m.ihxxc = b + 1 * n;
-  c.m.ijdxf = b + 2 * n;
-  c.m.ijdxc = b + 3 * n;
-  c.m.qf = b + 4 * n;
-  c.m.qc = b + 5 * n;
-  c.m.qf_hy = b + 6 * n;
-  c.m.qc_hy = b + 7 * n;
-  c.m.hqf = b + 8 * n;
-  c.m.hqc_hy = b + 9 * n;
-  c.m.nu_ijdxf = b + 10 * n;
-  c.m.nu_ijdxc = b + 11 * n;
-  c.m.hxxf = b + 12 * n;
+  c.m.q4f = b + 2 * n;
+  c.m.q4fy = b + 3 * n;
+  c.m.nuf = b + 4 * n;
+  c.m.hxxf = b + 5 * n;
   c.Re = Re;
-  // the constant part of decide_dt: diffusive and capillary limits
-  // (src/decide_dt.c:79-130)
   return 0;
 }
 
@@ -236,9 +219,9 @@ void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
   p.vis_lo = fmin(1., f->visr);
   p.vis_hi = fmax(1., f->visr);
   p.grav = -1. / f->Fr / f->Fr;
-  p.tension = itf ? 1. / itf->We : 0.;
-  p.force_coef = 2. / (1. + f->denr) * p.tension;
+  p.force_coef = itf ? 2. / (1. + f->denr) / itf->We : 0.;
   p.irefden = 1. / f->refden;
+  p.nu = 1. / f->Re;
 }
 
 double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
@@ -260,37 +243,61 @@ double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interfa
   return fmin(out, cap);
 }
 
-// Thomas pivots of the x operator per y wavenumber and the FFT twiddles
+// Thomas pivots of the x operator per y wavenumber, in the chunked layout of
+// k_poisson_tdm, and the FFT twiddles
 int upload_poisson(Ctx &c, const domain_t *d) {
   const int nx = c.nx, ny = c.ny, M1 = ny / 2 + 1;
+  const int L = tdm_chunk(nx), NP = 32 * L;
   const double pi = 3.14159265358979323846;
   const double dx = d->lengths[0] / nx;
   const double offx = 1. / (dx * dx);
   const double offy = 1. / d->hy / d->hy;
-  std::vector<double2> fac((size_t)nx * M1);
+  std::vector<double> w(NP), v(NP), P(NP), Q(NP);
+  std::vector<double> fac((size_t)M1 * NP * 4);
   for (int m = 0; m < M1; ++m) {
     const double s = sin(pi * m / ny);
     const double lam = -4. * offy * s * s;
     double v_prev = 0.;
-    for (int i = 0; i < nx; ++i) {
+    for (int i = 0; i < NP; ++i) {
+      if (i >= nx) {  // padding rows decouple and solve to zero
+        w[i] = 0.;
+        v[i] = 0.;
+        continue;
+      }
       const double diag = (i == 0 || i == nx - 1 ? -offx : -2. * offx) + lam;
       const double piv = diag - (i == 0 ? 0. : offx * v_prev);
-      double w = 1. / piv, v = offx * w;
       if (i == nx - 1 && fabs(piv) < 1.e-10 * offx) {
         // singular mode (m = 0, Neumann-Neumann): pin the last unknown; the
         // kernel removes the mean afterwards
-        w = 0.;
-        v = 0.;
+        w[i] = 0.;
+        v[i] = 0.;
+      } else {
+        w[i] = 1. / piv;
+        v[i] = offx * w[i];
       }
-      fac[(size_t)i * M1 + m] = make_double2(w, v);
-      v_prev = v;
+      v_prev = v[i];
+    }
+    for (int l = 0; l < 32; ++l) {
+      const int s0 = l * L, e0 = s0 + L - 1;
+      double acc = 1.;
+      for (int i = s0; i <= e0; ++i) P[i] = acc *= -v[i];
+      acc = 1.;
+      for (int i = e0; i >= s0; --i) Q[i] = acc *= -v[i];
+    }
+    for (int i = 0; i < NP; ++i) {
+      const int l = i / L, k = i % L;
+      double *o = &fac[(((size_t)m * L + k) * 32 + l) * 4];
+      o[0] = w[i];
+      o[1] = v[i];
+      o[2] = P[i];
+      o[3] = Q[i];
     }
   }
-  CK(cudaMemcpyAsync(c.b.tdm_fac, fac.data(), fac.size() * sizeof(double2), cudaMemcpyHostToDevice, c.s));
+  CK(cudaMemcpyAsync(c.b.tdm_fac, fac.data(), fac.size() * sizeof(double), cudaMemcpyHostToDevice, c.s));
   std::vector<double2> tw(M1);
   for (int m = 0; m < M1; ++m) tw[m] = make_double2(cos(2. * pi * m / ny), -sin(2. * pi * m / ny));
   CK(cudaMemcpyAsync(c.b.twiddle, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, c.s));
-  // tw and fac are staged from host vectors: make sure the copies finished
+  // the staging vectors die here: wait for the copies
   CK(cudaStreamSynchronize(c.s));
   return 0;
 }
@@ -317,6 +324,8 @@ int make_ctx(const domain_t *d) {
   g.p3 = rnd(3 * c->nx);
   g.hy = d->hy;
   g.ihy = 1. / d->hy;
+  g.dx = d->hxxc[0];
+  g.idx = 1. / d->hxxc[0];
   const size_t n1 = (size_t)g.p1 * g.ny, n2 = (size_t)g.p2 * g.ny, n3 = (size_t)g.p3 * g.ny;
   Bufs &b = c->b;
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
@@ -331,7 +340,7 @@ int make_ctx(const domain_t *d) {
   double *tmp = nullptr;
   if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1)) return 1;
   b.spec = reinterpret_cast<double2 *>(tmp);
-  if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1)) return 1;
+  if (dalloc(*c, &tmp, 4 * (size_t)32 * tdm_chunk(c->nx) * M1)) return 1;
   b.tdm_fac = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, 2 * (size_t)M1)) return 1;
   b.twiddle = reinterpret_cast<double2 *>(tmp);
@@ -380,7 +389,7 @@ Ctx *get_ctx(const domain_t *d, const fluid_t *f, const interface_t *itf) {
 }
 
 // scalars block for a fine-grained call: substage k of step size dt, and/or
-// explicit dt_old / dt_new in slot 0
+// explicit dt_old / dt_new in slot 0 (the same expressions as the step kernel)
 int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
   double *h = c.small_host;
   for (int i = 0; i < kScalars; ++i) h[i] = 0.;
@@ -391,12 +400,17 @@ int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
     h[sc_gdt(k)] = rk_g(k) * dt;
   }
   if (dt_new != 0.) {
+    const Grid &g = c.g;
     h[sc_dtold(0)] = dt_old;
     h[sc_dtnew(0)] = dt_new;
-    h[sc_pdiv(0)] = c.ph.refden / dt_new / c.ny;
-    h[sc_padd(0)] = -(dt_old / dt_new) / c.ny;
-    h[sc_cnew(0)] = dt_new / c.ph.refden;
-    h[sc_cold(0)] = -dt_old;
+    const double cdiv = c.ph.refden / dt_new * (0.5 / g.ny);
+    const double cadd = -(dt_old / dt_new) * (0.5 / g.ny);
+    h[sc_pdx(0)] = cdiv * g.idx;
+    h[sc_pdy(0)] = cdiv * g.ihy;
+    h[sc_pax(0)] = cadd * (g.idx * g.idx);
+    h[sc_pay(0)] = cadd * (g.ihy * g.ihy);
+    h[sc_cnew(0)] = dt_new * c.ph.irefden;
+    h[sc_cold(0)] = -dt_old * c.ph.irefden;
   }
   CK(cudaMemcpyAsync(c.b.scalars, h, sizeof(double) * kScalars, cudaMemcpyHostToDevice, c.s));
   // h is reused by the next call: wait for the copy
@@ -462,18 +476,18 @@ void enqueue_substage(Ctx &c, int k) {
   double *sva = c.SV[c.isrc], *svb = c.SV[c.isrc ^ 1];
   const double *sc = b.scalars;
   timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
-  timed(c, KC_NORMAL_CURV, [&] { launch_normal_curv(c.s, c.g, c.m, b, true, true); });
-  timed(c, KC_FLUX_FORCE, [&] { launch_flux_force(c.s, c.g, c.m, c.ph, b, ux, uy, den0, true, true); });
+  timed(c, KC_NORMAL_CURV, [&] { launch_normal_curv(c.s, c.g, c.m, b, true, true, true); });
+  timed(c, KC_FLUX_FORCE, [&] { launch_flux_force(c.s, c.g, c.m, c.ph, b, ux, uy, den0, true, true, true); });
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
   timed(c, KC_PREDICT, [&] {
     launch_predict(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, b.mfluxx, b.mfluxy, den0, den1, sxa, sxb,
                    nullptr, sya, syb, nullptr);
   });
-  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, c.m, c.ph, b, sc, k, uxs, uys, psio); });
+  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, b, sc, k, uxs, uys, psio); });
   timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
   timed(c, KC_POISSON_INV, [&] { launch_poisson_inv(c.s, c.g, b, psin); });
-  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, c.ph, b, sc, k, uxs, uys, psin, psio, true); });
+  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, b, sc, k, uxs, uys, psin, psio, true); });
   c.iu ^= 1;
   c.ipsi ^= 1;
   c.iden ^= 1;
@@ -611,6 +625,23 @@ int sbfs_invalidate_device(void) {
 }
 
 int sbfs_kernels_per_step(void) { return kKernelsPerStep; }
+
+int sbfs_measure_fp64_peak(double *gflops) {
+  CK(measure_fp64_peak(gflops));
+  return 0;
+}
+
+int sbfs_check_newton_raphson(const double *x, double *rcp, double *rsq, int n) {
+  double *d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * 3 * (size_t)n));
+  cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = nr_check(d, d + n, d + 2 * (size_t)n, n);
+  if (e == cudaSuccess) e = cudaMemcpy(rcp, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(rsq, d + 2 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail("newton-raphson check: %s", cudaGetErrorString(e));
+  return 0;
+}
 
 int sbfs_set_device(int device) {
   g_ctx.reset();
@@ -776,7 +807,7 @@ int interface_compute_curvature_tensor(const domain_t *d, interface_t *itf) {
   // cells outside the interface band keep their previous normal, as in the reference
   if (h2d(*c, itf->vof, L_VOF, c->b.vof) || h2d(*c, itf->normal, L_NORMAL, c->b.normal)) return 1;
   launch_props(c->s, c->g, c->m, c->ph, c->b, false, false, true, nullptr);
-  launch_normal_curv(c->s, c->g, c->m, c->b, true, true);
+  launch_normal_curv(c->s, c->g, c->m, c->b, true, true, false);
   if (d2h(*c, itf->dvof, L_DVOF, c->b.dvof) || d2h(*c, itf->normal, L_NORMAL, c->b.normal) ||
       d2h(*c, itf->curv, L_CURV, c->b.curv))
     return 1;
@@ -791,7 +822,7 @@ int interface_compute_force(const domain_t *d, const fluid_t *f, interface_t *it
   if (h2d(*c, f->den[0], L_DEN, c->b.den0) || h2d(*c, itf->vof, L_VOF, c->b.vof) ||
       h2d(*c, itf->curv, L_CURV, c->b.curv))
     return 1;
-  launch_flux_force(c->s, c->g, c->m, c->ph, c->b, c->b.ux, c->b.uy, c->b.den0, false, true);
+  launch_flux_force(c->s, c->g, c->m, c->ph, c->b, c->b.ux, c->b.uy, c->b.den0, false, true, false);
   if (d2h(*c, itf->ifrcx, L_IFRCX, c->b.ifrcx) || d2h(*c, itf->ifrcy, L_IFRCY, c->b.ifrcy)) return 1;
   return sync(*c);
 }
@@ -809,7 +840,7 @@ int interface_update_vof(const domain_t *d, const size_t rkstep, const double dt
       h2d(*c, itf->normal, L_NORMAL, b.normal) || h2d(*c, itf->src[1], L_SRC, b.srcvof[1]))
     return 1;
   if (put_scalars(*c, dt, (int)rkstep, 0., 0.)) return 1;
-  launch_flux_force(c->s, c->g, c->m, c->ph, b, b.ux, b.uy, b.den0, true, false);
+  launch_flux_force(c->s, c->g, c->m, c->ph, b, b.ux, b.uy, b.den0, true, false, false);
   launch_vof_advance(c->s, c->g, c->m, c->ph, b, b.scalars, (int)rkstep, b.srcvof[0], b.srcvof[1], false, b.ux,
                      b.uy, nullptr);
   if (d2h(*c, itf->fluxx, L_FLUXX, b.fluxx) || d2h(*c, itf->fluxy, L_FLUXY, b.fluxy) ||
@@ -873,8 +904,8 @@ int fluid_compute_potential(const domain_t *d, const double dt_old, const double
       h2d(*c, f->den[1], L_DEN, b.den1))
     return 1;
   if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
-  launch_inv_face_density(c->s, c->g, b.den1, b.irhox, b.irhoy);
-  launch_poisson(c->s, c->g, c->m, c->ph, b, b.scalars, 0, b.ux, b.uy, b.psi0, b.psi1);
+  launch_face_factor(c->s, c->g, c->ph, b.den1, b.irhox, b.irhoy);
+  launch_poisson(c->s, c->g, b, b.scalars, 0, b.ux, b.uy, b.psi0, b.psi1);
   if (d2h(*c, f->psi[1], L_P, b.psi1)) return 1;
   return sync(*c);
 }
@@ -889,8 +920,8 @@ int fluid_correct_velocity(const domain_t *d, const double dt_old, const double 
       h2d(*c, f->psi[1], L_P, b.psi1) || h2d(*c, f->den[1], L_DEN, b.den1))
     return 1;
   if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
-  launch_inv_face_density(c->s, c->g, b.den1, b.irhox, b.irhoy);
-  launch_correct(c->s, c->g, c->m, c->ph, b, b.scalars, 0, b.ux, b.uy, b.psi1, b.psi0, false);
+  launch_face_factor(c->s, c->g, c->ph, b.den1, b.irhox, b.irhoy);
+  launch_correct(c->s, c->g, c->m, b, b.scalars, 0, b.ux, b.uy, b.psi1, b.psi0, false);
   if (d2h(*c, f->ux, L_UX, b.ux) || d2h(*c, f->uy, L_UY, b.uy)) return 1;
   return sync(*c);
 }

@@ -9,6 +9,13 @@
 // y is periodic and every kernel wraps J (J = 0 -> ny, J = ny + 1 -> 1, ...),
 // which replaces the reference's halo exchange (src/halo.c:18-76) without any
 // copy.  x ghost cells are stored and written by the producing kernel.
+//
+// Metrics.  The reference writes its stencils for general x metrics but
+// accepts uniform x grids only (src/domain.c:213-219); its Jacobians are
+// JDXF = HXXF * hy and JDXC = HXXC * hy (src/domain.c:114-144).  The kernels
+// use those identities to fold the metric factors of every stencil into one
+// coefficient per column (the half cells at the walls keep their own HXXF),
+// which changes the rounding of the reference's expressions, not their value.
 #pragma once
 
 #include <cstdint>
@@ -16,22 +23,14 @@
 
 namespace sbfs {
 
-// per-column coefficients, evaluated on the host with the reference's own
-// expressions (hence the reference's rounding); index = I (0..nx+2)
+// per-column coefficients, index = I (0..nx+2), built on the host
 struct Metrics {
-  const double *ihxxf;     // 1 / HXXF(I)
-  const double *ihxxc;     // 1 / HXXC(I)
-  const double *ijdxf;     // 1 / JDXF(I)
-  const double *ijdxc;     // 1 / JDXC(I)
-  const double *qf;        // JDXF(I) / HXXF(I)
-  const double *qc;        // JDXC(I) / HXXC(I)
-  const double *qf_hy;     // JDXF(I) / hy
-  const double *qc_hy;     // JDXC(I) / hy
-  const double *hqf;       // 0.5 * JDXF(I) / HXXF(I)
-  const double *hqc_hy;    // 0.5 * JDXC(I) / hy
-  const double *nu_ijdxf;  // (1 / Re) / JDXF(I)
-  const double *nu_ijdxc;  // (1 / Re) / JDXC(I)
-  const double *hxxf;      // HXXF(I)
+  const double *ihxxf;  // 1 / HXXF(I)          (faces)
+  const double *ihxxc;  // 1 / HXXC(I)          (centres)
+  const double *q4f;    // 0.25 / HXXF(I)       (ux advection in x)
+  const double *q4fy;   // 0.25 HXXC / (HXXF(I) hy) (ux advection in y)
+  const double *nuf;    // (1 / Re) / HXXF(I)   (ux diffusion in x)
+  const double *hxxf;   // HXXF(I)              (decide_dt)
 };
 
 struct Grid {
@@ -40,6 +39,7 @@ struct Grid {
   int p2;  // pitch of dvof (2 doubles per element)
   int p3;  // pitch of normal (3 doubles per element)
   double hy, ihy;
+  double dx, idx;  // uniform cell width HXXC and its inverse
 };
 
 // physical parameters of one case
@@ -47,26 +47,29 @@ struct Phys {
   double denr, visr, refden;
   double den_lo, den_hi, vis_lo, vis_hi;
   double grav;        // -1 / Fr / Fr
-  double force_coef;  // 2 / (1 + denr), times 1 / We applied separately
-  double tension;     // 1 / We
+  double force_coef;  // 2 / (1 + denr) / We
   double irefden;     // 1 / refden
+  double nu;          // 1 / Re
 };
 
 // per-step scalars written by the time-step kernel and read by all others:
-// [0] dt; for substage k: [1+5k] alpha_k dt, [2+5k] beta_k dt, [3+5k] gamma_k dt,
-// [4+5k] dt_old_k, [5+5k] dt_new_k; [16..21] Poisson/correction factors:
-// [16+2k] refden / dt_new_k / ny, [17+2k] -dt_old_k / dt_new_k / ny
-// [22+2k] dt_new_k / refden, [23+2k] -dt_old_k
-constexpr int kScalars = 32;
+// [0] dt; for substage k: alpha_k dt, beta_k dt, gamma_k dt, dt_old_k,
+// dt_new_k; the Poisson right-hand-side coefficients (already divided by
+// 2 ny for the unnormalised real DFT pair) and the correction coefficients
+constexpr int kScalars = 64;
 __host__ __device__ constexpr int sc_adt(int k) { return 1 + 5 * k; }
 __host__ __device__ constexpr int sc_bdt(int k) { return 2 + 5 * k; }
 __host__ __device__ constexpr int sc_gdt(int k) { return 3 + 5 * k; }
 __host__ __device__ constexpr int sc_dtold(int k) { return 4 + 5 * k; }
 __host__ __device__ constexpr int sc_dtnew(int k) { return 5 + 5 * k; }
-__host__ __device__ constexpr int sc_pdiv(int k) { return 16 + 2 * k; }
-__host__ __device__ constexpr int sc_padd(int k) { return 17 + 2 * k; }
-__host__ __device__ constexpr int sc_cnew(int k) { return 22 + 2 * k; }
-__host__ __device__ constexpr int sc_cold(int k) { return 23 + 2 * k; }
+// rhs = pdx dux + pdy duy + pax X + pay Y (see k_poisson_fwd)
+__host__ __device__ constexpr int sc_pdx(int k) { return 16 + 4 * k; }
+__host__ __device__ constexpr int sc_pdy(int k) { return 17 + 4 * k; }
+__host__ __device__ constexpr int sc_pax(int k) { return 18 + 4 * k; }
+__host__ __device__ constexpr int sc_pay(int k) { return 19 + 4 * k; }
+// correction: u -= cnew * ih * dpsi_new; u += cold * ih * e * dpsi_old
+__host__ __device__ constexpr int sc_cnew(int k) { return 28 + 2 * k; }
+__host__ __device__ constexpr int sc_cold(int k) { return 29 + 2 * k; }
 
 // THINC constants (reference src/interface/common.c:4-14)
 constexpr double kGaussPt = 0.2886751345948129;
@@ -79,14 +82,6 @@ __device__ __forceinline__ int wrap(int J, int ny) {
   r -= (r >= ny) ? ny : 0;
   return r;
 }
-
-// scalar field accessor: x offset ox = ax0 - 1 so that column = I + ox
-template <int OX>
-struct Fld {
-  double *d;
-  int pitch;
-  __device__ __forceinline__ double &at(int I, int row) const { return d[(size_t)row * pitch + (I + OX)]; }
-};
 
 // bit-level helpers: sign and threshold tests on the integer pattern of a
 // double keep these comparisons off the FP64 pipe
@@ -110,8 +105,43 @@ __device__ __forceinline__ double clip_pos(double v, double lo, double hi) {
   return v;
 }
 
-// vel < 0. as in the reference upwind choice: true for negative numbers,
-// false for +0 and -0
-__device__ __forceinline__ bool neg(double v) { return v < 0.; }
+// vel < 0. as in the reference upwind choice (false for -0.)
+__device__ __forceinline__ bool neg(double v) {
+  const long long b = dbits(v);
+  return b < 0 && (b << 1) != 0;
+}
+
+// 1 / x for finite normal x > 0 (or < 0): the hardware seed
+// rcp.approx.ftz.f64 refined by two Newton-Raphson steps
+// r <- r + r (1 - x r) (quadratic convergence: each step doubles the number
+// of correct bits); result within an ulp or so of the correctly rounded
+// reciprocal, four FP64 FMAs instead of a division.
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.);
+  return fma(r, e, r);
+}
+
+// 1 / sqrt(s) for finite normal s > 0: rsqrt.approx.ftz.f64 seed and two
+// Newton-Raphson steps y <- y + y (1/2 - (s/2) y^2)
+__device__ __forceinline__ double rsqrt_nr(double s) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(s));
+  const double h = 0.5 * s;
+  double e = fma(-h * y, y, 0.5);
+  y = fma(y, e, y);
+  e = fma(-h * y, y, 0.5);
+  return fma(y, e, y);
+}
+
+// 1 / max(sqrt(s), eps) with eps = DBL_EPSILON (the reference normalises a
+// gradient by 1 / fmax(|g|, DBL_EPSILON), curvature_tensor.c:43, 87)
+__device__ __forceinline__ double inv_norm(double s) {
+  constexpr double eps = 2.220446049250313080847e-16;
+  return lt_pos(s, eps * eps) ? 1. / eps : rsqrt_nr(s);
+}
 
 }  // namespace sbfs

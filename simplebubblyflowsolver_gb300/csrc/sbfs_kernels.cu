@@ -1,22 +1,25 @@
 // sm_103a kernels of the 2-D two-phase (VOF) time step.
 //
 // All arithmetic is FP64.  On GB300 the FP64 pipe (about 0.5 T fused
-// multiply-adds per second, measured) is the bound of this solver, not HBM,
-// so the kernels are written to minimise FP64 instructions:
-//   * every per-column metric factor of the reference's stencils (1/HXXF,
-//     JDXF/HXXF, 0.5 JDXF/HXXF, ...) is precomputed once with the reference's
-//     own expression (struct Metrics);
-//   * each reciprocal the reference forms with "1. / x" uses the correctly
-//     rounded reciprocal __drcp_rn (same value, cheaper than a division);
-//   * divisions by a face density are replaced by one reciprocal per face per
-//     substage, shared by the predictor, the Poisson right-hand side and the
-//     velocity correction (irhox / irhoy);
-//   * threshold tests (vofmin, upwind sign, clipping of the mixture rules)
-//     run on the integer pattern of the double;
-//   * cells where all inputs of a stencil are bitwise equal (single-phase
-//     bulk) take the exact short cut (zero gradient, zero force).
-// Index conventions follow sbfs_device.cuh; the reference file:line each
-// kernel follows is cited at the kernel.
+// multiply-adds per second, measured) bounds this solver, not HBM (a first
+// version of the momentum kernel ran its FP64 pipe at 86% of peak with DRAM
+// at 9%), so every kernel is written to spend as few FP64 instructions per
+// cell as the discretisation allows:
+//   * the reference's metric factors are folded into one coefficient per
+//     column or per grid (see sbfs_device.cuh), and constant factors such
+//     as the 0.5 of face averages are folded into those coefficients;
+//   * reciprocals and inverse square roots are Newton-Raphson refinements of
+//     the hardware seeds (rcp_nr, rsqrt_nr);
+//   * 1 / rho^{k+1} is formed once per face and substage, and stored as
+//     e = rho_ref / rho - 1, the factor the Poisson right-hand side and the
+//     velocity correction both need;
+//   * the THINC indicator 0.5 (1 + tanh(n . x + d)) with the intercept
+//     d = -ln(1/phi - 1) / 2 equals 1 / (1 + K exp(-2 n . x)), K = 1/phi - 1:
+//     one exponential per Gauss point and no logarithm;
+//   * threshold tests (vofmin, upwind sign, clipping) run on the integer
+//     pattern of the double; cells whose stencil inputs are bitwise equal
+//     (single-phase bulk) take the exact short cut.
+// The reference file:line each kernel follows is cited at the kernel.
 #include <cfloat>
 
 #include "sbfs_kernels.cuh"
@@ -56,16 +59,16 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph, co
   const double v = vof[ix(g, r, I)];
   if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.denr - 1., v, 1.), ph.den_lo, ph.den_hi);
   if (VIS) {
-    const double c = ph.visr - 1.;
+    // 1 + (visr - 1) 0.5 (a + b) = 1 + c2 (a + b), c2 = (visr - 1) / 2
+    const double c = ph.visr - 1., c2 = 0.5 * c;
     if (I >= 1) {
-      double phi;
-      if (I == 1) phi = vof[ix(g, r, 0)];
-      else if (I == g.nx + 1) phi = v;
-      else phi = half_sum(vof[ix(g, r, I - 1)], v);
-      visux[ix(g, r, I - 1)] = clip_pos(fma(c, phi, 1.), ph.vis_lo, ph.vis_hi);
+      double vis;
+      if (I == 1) vis = fma(c, vof[ix(g, r, 0)], 1.);
+      else if (I == g.nx + 1) vis = fma(c, v, 1.);
+      else vis = fma(c2, vof[ix(g, r, I - 1)] + v, 1.);
+      visux[ix(g, r, I - 1)] = clip_pos(vis, ph.vis_lo, ph.vis_hi);
     }
-    const double phy = half_sum(vof[ix(g, rm, I)], v);
-    visuy[ix(g, r, I)] = clip_pos(fma(c, phy, 1.), ph.vis_lo, ph.vis_hi);
+    visuy[ix(g, r, I)] = clip_pos(fma(c2, vof[ix(g, rm, I)] + v, 1.), ph.vis_lo, ph.vis_hi);
   }
   if (GRAD && I >= 1) {
     // corner at x face I between rows J-1 and J
@@ -73,10 +76,13 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph, co
     const double c = vof[ix(g, r, I - 1)], d = v;
     double2 out = make_double2(0., 0.);
     if (!(same(a, b) && same(b, c) && same(c, d))) {
+      // the reference's summation order, kept on purpose: in the THINC
+      // tails the four values differ by ~1e-16 and the reference's sum is
+      // rounding noise that the normalisation below (by max(|g|, eps))
+      // scales up to O(1); another order gives O(1) different corner normals
       const double gx = m.ihxxf[I] * (((-a + b) - c) + d);
       const double gy = g.ihy * (((-a - b) + c) + d);
-      const double nrm = sqrt(fma(gx, gx, gy * gy));
-      const double inv = __drcp_rn(lt_pos(nrm, DBL_EPSILON) ? DBL_EPSILON : nrm);
+      const double inv = inv_norm(fma(gx, gx, gy * gy));
       out = make_double2(gx * inv, gy * inv);
     }
     reinterpret_cast<double2 *>(dvof)[(size_t)r * (g.p2 / 2) + (I - 1)] = out;
@@ -84,12 +90,15 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph, co
 }
 
 // ---------------------------------------------------------------------------
-// cell normal + THINC intercept (interface cells) and curvature
+// cell normal + THINC parameter (interface cells) and curvature
 //   normal:    src/interface/curvature_tensor.c:51-97
 //   curvature: src/interface/curvature_tensor.c:100-135
+//     kappa = -[(nx_xp - nx_xm) / HXXC + (ny_yp - ny_ym) / hy]
+// STORE_K: the third component is K = 1/phi - 1 (used by the fused step);
+// otherwise the reference's intercept d = -ln(1/phi - 1) / 2.
 // thread (I, J): I = 1..nx
 // ---------------------------------------------------------------------------
-template <bool NORMAL, bool CURV>
+template <bool NORMAL, bool CURV, bool STORE_K>
 __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const double *__restrict__ vof,
                                                         const double *__restrict__ dvof, double *__restrict__ normal,
                                                         double *__restrict__ curv) {
@@ -106,46 +115,49 @@ __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const
                           dbits(d11.x) | dbits(d11.y);
     double k = -0.;
     if ((any << 1) != 0) {  // some corner normal is not +-0
-      const double nxm = half_sum(d00.x, d01.x), nxp = half_sum(d10.x, d11.x);
-      const double nym = half_sum(d00.y, d10.y), nyp = half_sum(d01.y, d11.y);
-      const double div = m.ijdxc[I] * (((-m.qf[I] * nxm + m.qf[I + 1] * nxp) - m.qc_hy[I] * nym) + m.qc_hy[I] * nyp);
-      k = -div;
+      const double ddx = (d10.x + d11.x) - (d00.x + d01.x);
+      const double ddy = (d01.y + d11.y) - (d00.y + d10.y);
+      k = -fma(0.5 * m.ihxxc[I], ddx, (0.5 * g.ihy) * ddy);
     }
     curv[ix(g, r, I)] = k;
   }
   if (NORMAL) {
     const double phi = vof[ix(g, r, I)];
     if (!single_phase(phi)) {
-      double mx = ((d00.x + d10.x) + d01.x) + d11.x;
-      double my = ((d00.y + d10.y) + d01.y) + d11.y;
-      mx *= m.ihxxc[I];
-      my *= g.ihy;
-      const double nrm = sqrt(fma(mx, mx, my * my));
-      const double inv = __drcp_rn(lt_pos(nrm, DBL_EPSILON) ? DBL_EPSILON : nrm);
+      const double mx = (((d00.x + d10.x) + d01.x) + d11.x) * m.ihxxc[I];
+      const double my = (((d00.y + d10.y) + d01.y) + d11.y) * g.ihy;
+      const double inv = inv_norm(fma(mx, mx, my * my));
       double *o = normal + (size_t)r * g.p3 + (size_t)(I - 1) * 3;
       o[0] = mx * inv;
       o[1] = my * inv;
-      o[2] = -0.5 * log(__drcp_rn(phi) - 1.);
+      o[2] = STORE_K ? rcp_nr(phi) - 1. : -0.5 * log(__drcp_rn(phi) - 1.);
     }
   }
 }
 
-// smoothed-indicator face average of a THINC cell: sum over the two Gauss
-// points of 0.5 * (1 + tanh(n . x + d)) with weight 0.5 each
-// (src/interface/update/main.c:18-35, fluxx.c:62-68)
-__device__ __forceinline__ double thinc_face(const double *n, double x0, double y0, double x1, double y1) {
-  const double i0 = 0.5 * (1. + tanh(fma(n[1], y0, n[0] * x0) + n[2]));
-  const double i1 = 0.5 * (1. + tanh(fma(n[1], y1, n[0] * x1) + n[2]));
-  return fma(0.5, i1, 0.5 * i0);
+// THINC flux factor of one face (src/interface/update/main.c:18-35,
+// fluxx.c:62-68): the mean of the indicator over the two Gauss points
+// t = +-g of the face, 0.5 sum 1 / (1 + K exp(-2 (n_a s + n_b t))), where s
+// is the face position along its normal (+-1/2) and n_a, n_b the normal
+// components along and across it.  With a = K exp(-2 n_a s) and
+// b = exp(-2 n_b g) the two terms are 1 / (1 + a b) and b / (b + a).
+__device__ __forceinline__ double thinc_face(double na, double nb, double K, double s) {
+  const double a = K * exp(-2. * na * s);
+  const double b = exp(-2. * kGaussPt * nb);
+  const double p = fma(a, b, 1.);
+  const double q = b + a;
+  return 0.5 * fma(b, p, q) * rcp_nr(p * q);
 }
 
 // ---------------------------------------------------------------------------
 // THINC vof fluxes and CSF surface-tension force
 //   fluxes: src/interface/update/fluxx.c:14-73, fluxy.c:14-73
 //   force:  src/interface/force.c:20-88
+// HAVE_K: normal[2] holds K = 1/phi - 1 (fused step) instead of the
+// reference's intercept d (then K = exp(-2 d)).
 // thread (I, J): I = 1..nx handles x face I (I >= 2) and y face (I, J - 1/2)
 // ---------------------------------------------------------------------------
-template <bool FLUX, bool FORCE>
+template <bool FLUX, bool FORCE, bool HAVE_K>
 __global__ void __launch_bounds__(BX *BY)
     k_flux_force(Grid g, Metrics m, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
                  const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
@@ -168,9 +180,9 @@ __global__ void __launch_bounds__(BX *BY)
       if (single_phase(phi)) {
         f = vel * phi;
       } else {
-        const double xq = n ? -0.5 : 0.5;
         const double *nv = normal + (size_t)r * g.p3 + (size_t)(iu - 1) * 3;
-        f = vel * thinc_face(nv, xq, -kGaussPt, xq, kGaussPt);
+        const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
+        f = vel * thinc_face(nv[0], nv[1], K, n ? -0.5 : 0.5);
       }
       fluxx[ix(g, r, I - 1)] = f;
     }
@@ -183,9 +195,9 @@ __global__ void __launch_bounds__(BX *BY)
       if (single_phase(phi)) {
         f = vel * phi;
       } else {
-        const double yq = n ? -0.5 : 0.5;
         const double *nv = normal + (size_t)ru * g.p3 + (size_t)(I - 1) * 3;
-        f = vel * thinc_face(nv, -kGaussPt, yq, kGaussPt, yq);
+        const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
+        f = vel * thinc_face(nv[1], nv[0], K, n ? -0.5 : 0.5);
       }
       fluxy[ix(g, r, I)] = f;
     }
@@ -200,22 +212,21 @@ __global__ void __launch_bounds__(BX *BY)
     }
   }
   if (FORCE) {
+    // f = 0.5 (rho_l + rho_r) 2 / (1 + denr) / We 0.5 (k_l + k_r) (phi_r - phi_l) / h
     if (I >= 2) {
       double f = 0.;
       if (!same(vxm, v0)) {
-        const double rho = half_sum(den0[ix(g, r, I - 1)], den0[ix(g, r, I)]);
-        const double kap = half_sum(curv[ix(g, r, I - 1)], curv[ix(g, r, I)]);
-        const double dl = m.ihxxf[I] * (v0 - vxm);
-        f = ((rho * ph.force_coef) * kap) * dl;
+        const double rho = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];
+        const double kap = curv[ix(g, r, I - 1)] + curv[ix(g, r, I)];
+        f = (rho * kap) * ((0.25 * ph.force_coef * m.ihxxf[I]) * (v0 - vxm));
       }
       ifrcx[ix(g, r, I - 2)] = f;
     }
     double f = 0.;
     if (!same(vym, v0)) {
-      const double rho = half_sum(den0[ix(g, rm, I)], den0[ix(g, r, I)]);
-      const double kap = half_sum(curv[ix(g, rm, I)], curv[ix(g, r, I)]);
-      const double dl = g.ihy * (v0 - vym);
-      f = ((rho * ph.force_coef) * kap) * dl;
+      const double rho = den0[ix(g, rm, I)] + den0[ix(g, r, I)];
+      const double kap = curv[ix(g, rm, I)] + curv[ix(g, r, I)];
+      f = (rho * kap) * ((0.25 * ph.force_coef * g.ihy) * (v0 - vym));
     }
     ifrcy[ix(g, r, I - 1)] = f;
   }
@@ -224,6 +235,7 @@ __global__ void __launch_bounds__(BX *BY)
 // ---------------------------------------------------------------------------
 // vof source (flux divergence), RK update and vof boundaries
 //   src/interface/update/main.c:54-136, src/interface/boundary.c:15-42
+//   src = (F_x(i) - F_x(i+1)) / HXXC + (F_y(j) - F_y(j+1)) / hy
 // FUSED additionally writes rho^{k+1} (src/fluid/density.c) and the mass
 // fluxes u + (rho_r - 1) flux into separate buffers
 // (src/interface/mass_flux.c:10-58).
@@ -241,7 +253,7 @@ __global__ void __launch_bounds__(BX *BY)
   const int r = J - 1, rp = wrap(J + 1, g.ny);
   const double fxm = fluxx[ix(g, r, I - 1)], fxp = fluxx[ix(g, r, I)];
   const double fym = fluxy[ix(g, r, I)], fyp = fluxy[ix(g, rp, I)];
-  const double s = m.ijdxc[I] * (((m.qf[I] * fxm - m.qf[I + 1] * fxp) + m.qc_hy[I] * fym) - m.qc_hy[I] * fyp);
+  const double s = fma(m.ihxxc[I], fxm - fxp, g.ihy * (fym - fyp));
   src_a[ix(g, r, I - 1)] = s;
   double v = vof[ix(g, r, I)];
   v = fma(sc[sc_adt(k)], s, v);
@@ -281,6 +293,8 @@ __global__ void k_mass_flux(Grid g, Phys ph, const double *__restrict__ ux, cons
 // ---------------------------------------------------------------------------
 // viscous stress tensor: txx, tyy at centres, txy at corners
 //   src/fluid/predict/txx.c:11-40, txy.c:13-50, tyy.c:10-38
+//   txx = 2 mu du/dx = (mu_l + mu_r) (u_r - u_l) / HXXC, likewise tyy;
+//   txy = 0.5 (mu_s + mu_n) du/dy + 0.5 (mu_w + mu_e) dv/dx
 // thread (I, J): I = 1..nx+1
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(BX *BY)
@@ -296,28 +310,27 @@ __global__ void __launch_bounds__(BX *BY)
   const double w0 = uy[ix(g, r, I)];
   const double vy0 = visuy[ix(g, r, I)];
   if (I <= g.nx) {
-    const double mu = half_sum(vx0, visux[ix(g, r, I)]);
-    const double l = m.ihxxc[I] * (ux[ix(g, r, I)] - u0);
-    const double t = __dmul_rn(mu, l);
-    txx[ix(g, r, I - 1)] = __dadd_rn(t, t);
-    const double muy = half_sum(vy0, visuy[ix(g, rp, I)]);
-    const double ly = g.ihy * (uy[ix(g, rp, I)] - w0);
-    const double ty = __dmul_rn(muy, ly);
-    tyy[ix(g, r, I - 1)] = __dadd_rn(ty, ty);
+    txx[ix(g, r, I - 1)] = (vx0 + visux[ix(g, r, I)]) * ((ux[ix(g, r, I)] - u0) * m.ihxxc[I]);
+    tyy[ix(g, r, I - 1)] = (vy0 + visuy[ix(g, rp, I)]) * ((uy[ix(g, rp, I)] - w0) * g.ihy);
   }
-  const double mux = half_sum(visux[ix(g, rm, I - 1)], vx0);
-  const double muy = half_sum(visuy[ix(g, r, I - 1)], vy0);
-  const double lxy = g.ihy * (u0 - ux[ix(g, rm, I - 1)]);
-  const double lyx = m.ihxxf[I] * (w0 - uy[ix(g, r, I - 1)]);
-  txy[ix(g, r, I - 1)] = fma(mux, lxy, muy * lyx);
+  const double sx = visux[ix(g, rm, I - 1)] + vx0;
+  const double sy = visuy[ix(g, r, I - 1)] + vy0;
+  const double lxy = (u0 - ux[ix(g, rm, I - 1)]) * (0.5 * g.ihy);
+  const double lyx = (w0 - uy[ix(g, r, I - 1)]) * (0.5 * m.ihxxf[I]);
+  txy[ix(g, r, I - 1)] = fma(sx, lxy, sy * lyx);
 }
 
 // ---------------------------------------------------------------------------
 // momentum right-hand sides and the RK predictor
 //   ux: src/fluid/predict/ux.c:29-273, uy: src/fluid/predict/uy.c:29-251,
 //   src/fluid/predict/main.c:9-80, walls: src/fluid/boundary/ux.c, uy.c
+// With JD = H hy the ux terms reduce to
+//   adv_x = 0.25 / HXXF(i) [(F_i + F_i+1)(u_i + u_i+1) - (F_i-1 + F_i)(u_i-1 + u_i)]
+//   adv_y = 0.25 HXXC / (HXXF(i) hy) [(G_j+1 sums)(u_j + u_j+1) - (G_j sums)(u_j-1 + u_j)]
+//   dif_x = nu / HXXF(i) (txx_i - txx_i-1),  dif_y = nu / hy (txy_j+1 - txy_j)
+// and the uy terms likewise with HXXC in place of HXXF.
 // thread (I, J): I = 1..nx handles the ux face I (I >= 2) and the uy face
-// (I, J - 1/2); also stores 1 / rho^{k+1} at both faces
+// (I, J - 1/2); also stores e = rho_ref / rho^{k+1} - 1 at both faces
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(BX *BY)
     k_predict(Grid g, Metrics m, Phys ph, const double *__restrict__ sc, int k, const double *__restrict__ ux,
@@ -327,85 +340,75 @@ __global__ void __launch_bounds__(BX *BY)
               const double *__restrict__ ifrcx, const double *__restrict__ ifrcy, const double *__restrict__ den0,
               const double *__restrict__ den1, double *__restrict__ sxa, const double *__restrict__ sxb,
               double *__restrict__ sxg, double *__restrict__ sya, const double *__restrict__ syb,
-              double *__restrict__ syg, double *__restrict__ irhox, double *__restrict__ irhoy) {
+              double *__restrict__ syg, double *__restrict__ ex, double *__restrict__ ey) {
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int r = J - 1, rm = wrap(J - 1, g.ny), rp = wrap(J + 1, g.ny);
   const double adt = sc[sc_adt(k)], bdt = sc[sc_bdt(k)], gdt = sc[sc_gdt(k)];
+  const double rref = ph.refden;
+  const double nuy = ph.nu * g.ihy;
   // ---- ux at face I
   if (I >= 2) {
-    const double fxm = mfx[ix(g, r, I - 2)], fx0 = mfx[ix(g, r, I - 1)], fxp = mfx[ix(g, r, I)];
-    const double um1 = ux[ix(g, r, I - 2)], u0 = ux[ix(g, r, I - 1)], up1 = ux[ix(g, r, I)];
-    double a;
-    {
-      const double mm = fma(m.hqf[I - 1], fxm, m.hqf[I] * fx0);
-      const double mp = fma(m.hqf[I], fx0, m.hqf[I + 1] * fxp);
-      const double um = half_sum(um1, u0), up = half_sum(u0, up1);
-      a = -(m.ijdxf[I] * fma(mp, up, -mm * um));
-    }
-    {
-      const double mm = fma(m.hqc_hy[I - 1], mfy[ix(g, r, I - 1)], m.hqc_hy[I] * mfy[ix(g, r, I)]);
-      const double mp = fma(m.hqc_hy[I - 1], mfy[ix(g, rp, I - 1)], m.hqc_hy[I] * mfy[ix(g, rp, I)]);
-      const double um = half_sum(ux[ix(g, rm, I - 1)], u0), up = half_sum(u0, ux[ix(g, rp, I - 1)]);
-      a -= m.ijdxf[I] * fma(mp, up, -mm * um);
-    }
-    a = fma(m.nu_ijdxf[I], fma(m.qc[I], txx[ix(g, r, I - 1)], -m.qc[I - 1] * txx[ix(g, r, I - 2)]), a);
-    a = fma(m.nu_ijdxf[I], m.qf_hy[I] * (txy[ix(g, rp, I - 1)] - txy[ix(g, r, I - 1)]), a);
-    const double gs = -(m.ihxxf[I] * (p[ix(g, r, I)] - p[ix(g, r, I - 1)]));
-    a += ifrcx[ix(g, r, I - 2)];
-    const double rho0 = half_sum(den0[ix(g, r, I - 1)], den0[ix(g, r, I)]);
-    a = fma(ph.grav, rho0, a);
-    const double irho = __drcp_rn(half_sum(den1[ix(g, r, I - 1)], den1[ix(g, r, I)]));
-    double u = fma(adt, a, rho0 * u0);
+    const double fx0 = mfx[ix(g, r, I - 1)];
+    const double u0 = ux[ix(g, r, I - 1)];
+    const double sxm = mfx[ix(g, r, I - 2)] + fx0, sxp = fx0 + mfx[ix(g, r, I)];
+    const double um = ux[ix(g, r, I - 2)] + u0, up = u0 + ux[ix(g, r, I)];
+    const double sym = mfy[ix(g, r, I - 1)] + mfy[ix(g, r, I)];
+    const double syp = mfy[ix(g, rp, I - 1)] + mfy[ix(g, rp, I)];
+    const double vm = ux[ix(g, rm, I - 1)] + u0, vp = u0 + ux[ix(g, rp, I - 1)];
+    double a = ifrcx[ix(g, r, I - 2)];
+    const double rho0 = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];  // 2 rho^k
+    a = fma(0.5 * ph.grav, rho0, a);
+    a = fma(m.nuf[I], txx[ix(g, r, I - 1)] - txx[ix(g, r, I - 2)], a);
+    a = fma(nuy, txy[ix(g, rp, I - 1)] - txy[ix(g, r, I - 1)], a);
+    a = fma(-m.q4f[I], fma(sxp, up, -sxm * um), a);
+    a = fma(-m.q4fy[I], fma(syp, vp, -sym * vm), a);
+    const double gs = (p[ix(g, r, I - 1)] - p[ix(g, r, I)]) * m.ihxxf[I];
+    const double irho = rcp_nr(half_sum(den1[ix(g, r, I - 1)], den1[ix(g, r, I)]));
+    double u = fma(adt, a, (0.5 * rho0) * u0);
     if (k != 0) u = fma(bdt, sxb[ix(g, r, I - 2)], u);
     u = fma(gdt, gs, u);
     ux_out[ix(g, r, I - 1)] = u * irho;
     sxa[ix(g, r, I - 2)] = a;
     if (sxg) sxg[ix(g, r, I - 2)] = gs;
-    irhox[ix(g, r, I - 1)] = irho;
+    ex[ix(g, r, I - 1)] = fma(rref, irho, -1.);
   }
   // ---- uy at face (I, J - 1/2)
   {
     const double w0 = uy[ix(g, r, I)];
-    double a;
-    {
-      const double mm = m.hqf[I] * (mfx[ix(g, rm, I - 1)] + mfx[ix(g, r, I - 1)]);
-      const double mp = m.hqf[I + 1] * (mfx[ix(g, rm, I)] + mfx[ix(g, r, I)]);
-      const double um = half_sum(uy[ix(g, r, I - 1)], w0), up = half_sum(w0, uy[ix(g, r, I + 1)]);
-      a = -(m.ijdxc[I] * fma(mp, up, -mm * um));
-    }
-    {
-      const double f0 = mfy[ix(g, r, I)];
-      const double mm = m.hqc_hy[I] * (mfy[ix(g, rm, I)] + f0);
-      const double mp = m.hqc_hy[I] * (f0 + mfy[ix(g, rp, I)]);
-      const double um = half_sum(uy[ix(g, rm, I)], w0), up = half_sum(w0, uy[ix(g, rp, I)]);
-      a -= m.ijdxc[I] * fma(mp, up, -mm * um);
-    }
-    a = fma(m.nu_ijdxc[I], fma(m.qf[I + 1], txy[ix(g, r, I)], -m.qf[I] * txy[ix(g, r, I - 1)]), a);
-    a = fma(m.nu_ijdxc[I], m.qc_hy[I] * (tyy[ix(g, r, I - 1)] - tyy[ix(g, rm, I - 1)]), a);
-    const double gs = -(g.ihy * (p[ix(g, r, I)] - p[ix(g, rm, I)]));
-    a += ifrcy[ix(g, r, I - 1)];
+    const double sxm = mfx[ix(g, rm, I - 1)] + mfx[ix(g, r, I - 1)];
+    const double sxp = mfx[ix(g, rm, I)] + mfx[ix(g, r, I)];
+    const double um = uy[ix(g, r, I - 1)] + w0, up = w0 + uy[ix(g, r, I + 1)];
+    const double f0 = mfy[ix(g, r, I)];
+    const double sym = mfy[ix(g, rm, I)] + f0, syp = f0 + mfy[ix(g, rp, I)];
+    const double vm = uy[ix(g, rm, I)] + w0, vp = w0 + uy[ix(g, rp, I)];
+    double a = ifrcy[ix(g, r, I - 1)];
+    a = fma(ph.nu * m.ihxxc[I], txy[ix(g, r, I)] - txy[ix(g, r, I - 1)], a);
+    a = fma(nuy, tyy[ix(g, r, I - 1)] - tyy[ix(g, rm, I - 1)], a);
+    a = fma(-0.25 * m.ihxxc[I], fma(sxp, up, -sxm * um), a);
+    a = fma(-0.25 * g.ihy, fma(syp, vp, -sym * vm), a);
+    const double gs = (p[ix(g, rm, I)] - p[ix(g, r, I)]) * g.ihy;
     const double rho0 = half_sum(den0[ix(g, rm, I)], den0[ix(g, r, I)]);
-    const double irho = __drcp_rn(half_sum(den1[ix(g, rm, I)], den1[ix(g, r, I)]));
+    const double irho = rcp_nr(half_sum(den1[ix(g, rm, I)], den1[ix(g, r, I)]));
     double u = fma(adt, a, rho0 * w0);
     if (k != 0) u = fma(bdt, syb[ix(g, r, I - 1)], u);
     u = fma(gdt, gs, u);
     uy_out[ix(g, r, I)] = u * irho;
     sya[ix(g, r, I - 1)] = a;
     if (syg) syg[ix(g, r, I - 1)] = gs;
-    irhoy[ix(g, r, I)] = irho;
+    ey[ix(g, r, I)] = fma(rref, irho, -1.);
   }
-  // walls: impermeable, no-slip; wall-face densities for the Poisson operator
+  // walls: impermeable, no-slip; wall-face factors for the Poisson operator
   if (I == 1) {
     ux_out[ix(g, r, 0)] = 0.;
     uy_out[ix(g, r, 0)] = 0.;
-    irhox[ix(g, r, 0)] = __drcp_rn(half_sum(den1[ix(g, r, 0)], den1[ix(g, r, 1)]));
+    ex[ix(g, r, 0)] = fma(rref, rcp_nr(half_sum(den1[ix(g, r, 0)], den1[ix(g, r, 1)])), -1.);
   }
   if (I == g.nx) {
     ux_out[ix(g, r, g.nx)] = 0.;
     uy_out[ix(g, r, g.nx + 1)] = 0.;
-    irhox[ix(g, r, g.nx)] = __drcp_rn(half_sum(den1[ix(g, r, g.nx)], den1[ix(g, r, g.nx + 1)]));
+    ex[ix(g, r, g.nx)] = fma(rref, rcp_nr(half_sum(den1[ix(g, r, g.nx)], den1[ix(g, r, g.nx + 1)])), -1.);
   }
 }
 
@@ -418,36 +421,67 @@ __global__ void __launch_bounds__(BX *BY)
 // along the periodic y direction and one (non-periodic, Neumann-ended)
 // tridiagonal system along x is solved per y wavenumber.
 //   1. k_poisson_fwd: right-hand side of src/fluid/compute_potential.c:
-//      285-363 for a tile of W columns, packed two reals per complex, a
-//      radix-2 Stockham FFT of length ny/2 in shared memory and the
-//      real-to-complex split; spectrum [I][m], m = 0..ny/2
-//   2. k_poisson_tdm: Thomas sweeps along x with precomputed pivots; the
-//      singular m = 0 mode is pinned to zero mean
+//      285-363 for a tile of W columns,
+//        rhs = rho_ref/dt_new div u* - dt_old/dt_new div((rho_ref/rho - 1) grad psi_old)
+//      with div and the face differences in the JD = H hy form, packed two
+//      reals per complex, a mixed radix-4/2 Stockham FFT of length ny/2 in
+//      shared memory and the real-to-complex split; spectrum [I][m]
+//   2. k_poisson_tdm: tridiagonal solves along x (warp-parallel scan)
 //   3. k_poisson_inv: inverse of step 1, psi and its Neumann ghosts
+// The 1 / ny of the inverse DFT and the 1/2 of the real split are folded
+// into the right-hand-side coefficients.
 // ---------------------------------------------------------------------------
 
-// radix-2 Stockham FFT of W rows of length M in shared memory; tw[e] =
-// exp(-2 pi i e / (2M)), so W_M^e = tw[2e].  Returns the buffer holding the
-// result (x or y).
+// twiddle W_M^e, e in [0, M), from tw[m] = exp(-2 pi i m / 2M), m = 0..M
+__device__ __forceinline__ double2 twiddle(const double2 *__restrict__ tw, int M, int e, bool inverse) {
+  const int idx = 2 * e;
+  double2 w = idx <= M ? tw[idx] : make_double2(-tw[idx - M].x, -tw[idx - M].y);
+  if (inverse) w.y = -w.y;
+  return w;
+}
+
+// Stockham FFT (radix 4, one radix-2 stage first when log2 M is odd) of W
+// rows of length M in shared memory.  Returns the buffer holding the result.
 template <int W>
 __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__restrict__ tw, bool inverse) {
-  const int half = M >> 1;
-  for (int Ns = 1; Ns < M; Ns <<= 1) {
+  int Ns = 1;
+  if ((__ffs(M) - 1) & 1) {  // log2 M odd
+    const int half = M >> 1;
     for (int t = threadIdx.x; t < W * half; t += blockDim.x) {
       const int c = t / half, j = t - c * half;
+      const double2 v0 = x[c * M + j], v1 = x[c * M + j + half];
+      y[c * M + 2 * j] = cadd(v0, v1);
+      y[c * M + 2 * j + 1] = csub(v0, v1);
+    }
+    __syncthreads();
+    double2 *tmp = x;
+    x = y;
+    y = tmp;
+    Ns = 2;
+  }
+  const int q4 = M >> 2;
+  for (; Ns < M; Ns <<= 2) {
+    const int step = M / (4 * Ns);
+    for (int t = threadIdx.x; t < W * q4; t += blockDim.x) {
+      const int c = t / q4, j = t - c * q4;
       const double2 *xr = x + c * M;
       double2 *yr = y + c * M;
       const int kk = j & (Ns - 1);
-      const double2 v0 = xr[j];
-      double2 v1 = xr[j + half];
+      double2 v0 = xr[j], v1 = xr[j + q4], v2 = xr[j + 2 * q4], v3 = xr[j + 3 * q4];
       if (Ns > 1) {
-        double2 w = tw[kk * (M / Ns)];
-        if (inverse) w.y = -w.y;
-        v1 = cmul(v1, w);
+        const int e = kk * step;
+        v1 = cmul(v1, twiddle(tw, M, e, inverse));
+        v2 = cmul(v2, twiddle(tw, M, 2 * e, inverse));
+        v3 = cmul(v3, twiddle(tw, M, 3 * e, inverse));
       }
-      const int d = ((j - kk) << 1) + kk;
-      yr[d] = cadd(v0, v1);
-      yr[d + Ns] = csub(v0, v1);
+      const double2 a0 = cadd(v0, v2), a1 = csub(v0, v2), a2 = cadd(v1, v3), a3 = csub(v1, v3);
+      // -i a3 (forward) or +i a3 (inverse)
+      const double2 r3 = inverse ? make_double2(-a3.y, a3.x) : make_double2(a3.y, -a3.x);
+      const int d = ((j - kk) << 2) + kk;
+      yr[d] = cadd(a0, a2);
+      yr[d + Ns] = cadd(a1, r3);
+      yr[d + 2 * Ns] = csub(a0, a2);
+      yr[d + 3 * Ns] = csub(a1, r3);
     }
     __syncthreads();
     double2 *tmp = x;
@@ -459,38 +493,34 @@ __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__res
 
 template <int W>
 __global__ void __launch_bounds__(256)
-    k_poisson_fwd(Grid g, Metrics m, Phys ph, const double *__restrict__ sc, int k, const double *__restrict__ ux,
-                  const double *__restrict__ uy, const double *__restrict__ psi, const double *__restrict__ irhox,
-                  const double *__restrict__ irhoy, const double2 *__restrict__ tw, double2 *__restrict__ spec) {
+    k_poisson_fwd(Grid g, const double *__restrict__ sc, int k, const double *__restrict__ ux,
+                  const double *__restrict__ uy, const double *__restrict__ psi, const double *__restrict__ ex,
+                  const double *__restrict__ ey, const double2 *__restrict__ tw, double2 *__restrict__ spec) {
   extern __shared__ double2 smem[];
   const int ny = g.ny, M = ny >> 1;
   double2 *A = smem, *B = smem + W * M;
   double *Ad = reinterpret_cast<double *>(A);
   const int I0 = blockIdx.x * W + 1;
-  const double pdiv = sc[sc_pdiv(k)], padd = sc[sc_padd(k)];
-  const double rref = ph.refden;
+  const double pdx = sc[sc_pdx(k)], pdy = sc[sc_pdy(k)], pax = sc[sc_pax(k)], pay = sc[sc_pay(k)];
   for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
     const int c = t % W, r = t / W;
     const int I = I0 + c;
     double val = 0.;
     if (I <= g.nx) {
       const int rm = r == 0 ? ny - 1 : r - 1, rp = r == ny - 1 ? 0 : r + 1;
-      const double div = m.ijdxc[I] * (((-m.qf[I] * ux[ix(g, r, I - 1)] + m.qf[I + 1] * ux[ix(g, r, I)]) -
-                                        m.qc_hy[I] * uy[ix(g, r, I)]) +
-                                       m.qc_hy[I] * uy[ix(g, rp, I)]);
       const double ps = psi[ix(g, r, I)];
-      const double gxm = fma(rref, irhox[ix(g, r, I - 1)], -1.) * (ps - psi[ix(g, r, I - 1)]) * m.ihxxf[I];
-      const double gxp = fma(rref, irhox[ix(g, r, I)], -1.) * (psi[ix(g, r, I + 1)] - ps) * m.ihxxf[I + 1];
-      const double gym = fma(rref, irhoy[ix(g, r, I)], -1.) * (ps - psi[ix(g, rm, I)]) * g.ihy;
-      const double gyp = fma(rref, irhoy[ix(g, rp, I)], -1.) * (psi[ix(g, rp, I)] - ps) * g.ihy;
-      const double add = m.ijdxc[I] * (((-m.qf[I] * gxm + m.qf[I + 1] * gxp) - m.qc_hy[I] * gym) + m.qc_hy[I] * gyp);
-      val = fma(pdiv, div, padd * add);
+      // (e dpsi) differences across the cell; the wall faces have dpsi = 0
+      const double X = fma(ex[ix(g, r, I)], psi[ix(g, r, I + 1)] - ps, -ex[ix(g, r, I - 1)] * (ps - psi[ix(g, r, I - 1)]));
+      const double Y = fma(ey[ix(g, rp, I)], psi[ix(g, rp, I)] - ps, -ey[ix(g, r, I)] * (ps - psi[ix(g, rm, I)]));
+      const double dux = ux[ix(g, r, I)] - ux[ix(g, r, I - 1)];
+      const double duy = uy[ix(g, rp, I)] - uy[ix(g, r, I)];
+      val = fma(pdx, dux, fma(pdy, duy, fma(pax, X, pay * Y)));
     }
     Ad[c * ny + r] = val;
   }
   __syncthreads();
   double2 *Z = fft_rows<W>(A, B, M, tw, false);
-  // real-to-complex split: X_m = E_m + exp(-2 pi i m / ny) O_m
+  // real-to-complex split, times 2: X_m = (z_m + conj z_{M-m}) + w^m (-i)(z_m - conj z_{M-m})
   const int M1 = M + 1;
   for (int t = threadIdx.x; t < W * M1; t += blockDim.x) {
     const int c = t / M1, mm = t - c * M1;
@@ -498,10 +528,8 @@ __global__ void __launch_bounds__(256)
     if (I > g.nx) continue;
     const double2 zm = Z[c * M + (mm == M ? 0 : mm)];
     const double2 zr = Z[c * M + (mm == 0 ? 0 : M - mm)];
-    const double2 zc = make_double2(zr.x, -zr.y);
-    const double2 E = make_double2(0.5 * (zm.x + zc.x), 0.5 * (zm.y + zc.y));
-    const double2 dd = csub(zm, zc);
-    const double2 O = make_double2(0.5 * dd.y, -0.5 * dd.x);
+    const double2 E = make_double2(zm.x + zr.x, zm.y - zr.y);
+    const double2 O = make_double2(zm.y + zr.y, zr.x - zm.x);  // -i (zm - conj zr)
     spec[(size_t)(I - 1) * M1 + mm] = cadd(E, cmul(tw[mm], O));
   }
 }
@@ -520,10 +548,10 @@ __global__ void __launch_bounds__(256)
     if (I <= g.nx) {
       const double2 xm = spec[(size_t)(I - 1) * M1 + mm];
       const double2 xr = spec[(size_t)(I - 1) * M1 + (M - mm)];
-      const double2 xc = make_double2(xr.x, -xr.y);
-      const double2 E = cadd(xm, xc);
+      const double2 E = make_double2(xm.x + xr.x, xm.y - xr.y);
+      const double2 D = make_double2(xm.x - xr.x, xm.y + xr.y);
       const double2 w = make_double2(tw[mm].x, -tw[mm].y);
-      const double2 O = cmul(csub(xm, xc), w);
+      const double2 O = cmul(D, w);
       z = make_double2(E.x - O.y, E.y + O.x);
     }
     A[c * M + mm] = z;
@@ -542,60 +570,100 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Thomas sweeps along x for MB consecutive y wavenumbers held in shared
-// memory as [I][mode] complex; fac[I][m] = (1 / pivot_I, off / pivot_I)
+// Tridiagonal solves along x, one per real system (y wavenumber m, real or
+// imaginary part), one warp per system.  The pivots of the constant operator
+// are precomputed, so the Thomas forward sweep is the first-order linear
+// recurrence y_i = w_i r_i - v_i y_{i-1} and the back substitution is
+// x_i = y_i - v_i x_{i+1}.  Lane l owns the L consecutive rows l*L..l*L+L-1:
+// it runs both recurrences on its rows from a zero carry, the lanes combine
+// their chunk maps (T, B): y -> T + B y with a shuffle scan, and each row is
+// fixed up with the precomputed cumulative products P_i (forward) and Q_i
+// (backward) of the recurrence coefficients inside its chunk.  Per row: 5
+// FP64 operations instead of the 3 of a sequential sweep, but 32-way
+// parallel per system.  fac[(m*L + k)*32 + l] = (w, v, P, Q) for row l*L+k.
+// The singular m = 0 mode (Neumann in x, constant null space) has its last
+// pivot pinned (w = v = 0) and is shifted to zero mean.
+// Shared memory: per system a planar array with an odd lane stride S.
 __global__ void __launch_bounds__(256)
-    k_poisson_tdm(Grid g, int MB, const double2 *__restrict__ fac, double2 *__restrict__ spec) {
-  extern __shared__ double2 s[];
-  __shared__ double red[256];
+    k_poisson_tdm(Grid g, int MB, int L, int S, const double4_32a *__restrict__ fac, double2 *__restrict__ spec) {
+  extern __shared__ double2 smem_d2[];
+  double *sm = reinterpret_cast<double *>(smem_d2);
   const int nx = g.nx, M1 = g.ny / 2 + 1;
   const int m0 = blockIdx.x * MB;
   const int nm = min(MB, M1 - m0);
-  for (int t = threadIdx.x; t < nx * nm; t += blockDim.x) {
+  const int sys_len = 32 * S;
+  // ---- load: spec[i][m0 + q] -> planar (q, re) and (q, im) arrays
+  for (int t = threadIdx.x; t < 32 * L * nm; t += blockDim.x) {
     const int i = t / nm, q = t - i * nm;
-    s[i * MB + q] = spec[(size_t)i * M1 + m0 + q];
+    const int at = (i / L) * S + (i % L);
+    double2 v = make_double2(0., 0.);
+    if (i < nx) v = spec[(size_t)i * M1 + m0 + q];
+    sm[(2 * q) * sys_len + at] = v.x;
+    sm[(2 * q + 1) * sys_len + at] = v.y;
   }
   __syncthreads();
-  if (threadIdx.x < 2 * nm) {
-    const int q = threadIdx.x >> 1, comp = threadIdx.x & 1;
-    double *sd = reinterpret_cast<double *>(s) + 2 * q + comp;
-    const double2 *f = fac + m0 + q;
-    double y = 0.;
-#pragma unroll 8
-    for (int i = 0; i < nx; ++i) {
-      const double2 wv = f[(size_t)i * M1];
-      y = fma(-wv.y, y, wv.x * sd[2 * MB * i]);
-      sd[2 * MB * i] = y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < 2 * nm) {
+    const int q = warp >> 1;
+    const int m = m0 + q;
+    double *x = sm + warp * sys_len + lane * S;
+    const double4_32a *f = fac + (size_t)m * L * 32 + lane;
+    // forward, local from a zero carry
+    double t = 0.;
+    for (int k = 0; k < L; ++k) {
+      const double4_32a c = f[(size_t)k * 32];
+      t = fma(-c.y, t, c.x * x[k]);
+      x[k] = t;
     }
-    double x = y;
-#pragma unroll 8
-    for (int i = nx - 2; i >= 0; --i) {
-      const double2 wv = f[(size_t)i * M1];
-      x = fma(-wv.y, x, sd[2 * MB * i]);
-      sd[2 * MB * i] = x;
+    double T = t, B = f[(size_t)(L - 1) * 32].z;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double Tp = __shfl_up_sync(0xffffffffu, T, d), Bp = __shfl_up_sync(0xffffffffu, B, d);
+      if (lane >= d) {
+        T = fma(B, Tp, T);
+        B *= Bp;
+      }
     }
-  }
-  __syncthreads();
-  if (m0 == 0) {
-    // gauge of the singular mode: zero mean over x
+    double carry = __shfl_up_sync(0xffffffffu, T, 1);
+    if (lane == 0) carry = 0.;
+    // fix up the forward solution, then the backward sweep from a zero carry
+    double u = 0.;
+    for (int k = L - 1; k >= 0; --k) {
+      const double4_32a c = f[(size_t)k * 32];
+      const double y = fma(c.z, carry, x[k]);
+      u = fma(-c.y, u, y);
+      x[k] = u;
+    }
+    double Sx = u, C = f[0].w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double Sp = __shfl_down_sync(0xffffffffu, Sx, d), Cp = __shfl_down_sync(0xffffffffu, C, d);
+      if (lane + d < 32) {
+        Sx = fma(C, Sp, Sx);
+        C *= Cp;
+      }
+    }
+    double next = __shfl_down_sync(0xffffffffu, Sx, 1);
+    if (lane == 31) next = 0.;
     double acc = 0.;
-    for (int i = threadIdx.x; i < nx; i += blockDim.x) acc += s[i * MB].x;
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
+    for (int k = 0; k < L; ++k) {
+      const double v = fma(f[(size_t)k * 32].w, next, x[k]);
+      x[k] = v;
+      acc += (lane * L + k < nx) ? v : 0.;
     }
-    const double mean = red[0] / nx;
-    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
-      s[i * MB].x -= mean;
-      s[i * MB].y = 0.;
+    if (m == 0) {
+      // gauge of the singular mode: zero mean over x (imaginary part is 0)
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+      const double mean = (warp & 1) ? 0. : acc / nx;
+      for (int k = 0; k < L; ++k) x[k] = (warp & 1) ? 0. : x[k] - mean;
     }
-    __syncthreads();
   }
+  __syncthreads();
   for (int t = threadIdx.x; t < nx * nm; t += blockDim.x) {
     const int i = t / nm, q = t - i * nm;
-    spec[(size_t)i * M1 + m0 + q] = s[i * MB + q];
+    const int at = (i / L) * S + (i % L);
+    spec[(size_t)i * M1 + m0 + q] = make_double2(sm[(2 * q) * sys_len + at], sm[(2 * q + 1) * sys_len + at]);
   }
 }
 
@@ -603,13 +671,15 @@ __global__ void __launch_bounds__(256)
 // velocity correction (+ pressure update)
 //   src/fluid/correct_velocity/ux.c:18-66, uy.c:17-64
 //   src/fluid/update_pressure.c:7-53
+//   u -= dt_new / rho_ref dpsi_new / h;  u += -dt_old (1/rho - 1/rho_ref) dpsi_old / h
+//   with 1/rho - 1/rho_ref = e / rho_ref
 // thread (I, J): I = 1..nx
 // ---------------------------------------------------------------------------
 template <bool PRES>
 __global__ void __launch_bounds__(BX *BY)
-    k_correct(Grid g, Metrics m, Phys ph, const double *__restrict__ sc, int k, double *__restrict__ ux,
+    k_correct(Grid g, Metrics m, const double *__restrict__ sc, int k, double *__restrict__ ux,
               double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ psio,
-              const double *__restrict__ irhox, const double *__restrict__ irhoy, double *__restrict__ p) {
+              const double *__restrict__ ex, const double *__restrict__ ey, double *__restrict__ p) {
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -620,13 +690,13 @@ __global__ void __launch_bounds__(BX *BY)
     const double ih = m.ihxxf[I];
     double u = ux[ix(g, r, I - 1)];
     u = fma(-(cnew * ih), pn0 - psin[ix(g, r, I - 1)], u);
-    u = fma(cold * (irhox[ix(g, r, I - 1)] - ph.irefden) * ih, po0 - psio[ix(g, r, I - 1)], u);
+    u = fma((cold * ih) * ex[ix(g, r, I - 1)], po0 - psio[ix(g, r, I - 1)], u);
     ux[ix(g, r, I - 1)] = u;
   }
   {
     double u = uy[ix(g, r, I)];
     u = fma(-(cnew * g.ihy), pn0 - psin[ix(g, rm, I)], u);
-    u = fma(cold * (irhoy[ix(g, r, I)] - ph.irefden) * g.ihy, po0 - psio[ix(g, rm, I)], u);
+    u = fma((cold * g.ihy) * ey[ix(g, r, I)], po0 - psio[ix(g, rm, I)], u);
     uy[ix(g, r, I)] = u;
   }
   if (I == 1) {
@@ -663,7 +733,8 @@ __global__ void k_pressure(Grid g, const double *__restrict__ psin, double *__re
 // fixed h because both roundings are monotone; so the kernel reduces max |u|
 // per x column (ux) and over the domain (uy) on the integer patterns of the
 // non-negative doubles, and one block finishes with nx + 1 divisions.  A
-// non-finite velocity sets bit 0 of the status word.
+// non-finite velocity sets bit 0 of the status word.  The finishing block
+// also writes every per-substage scalar of the step.
 // ---------------------------------------------------------------------------
 constexpr unsigned long long kAbsMask = 0x7fffffffffffffffULL;
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
@@ -671,8 +742,7 @@ constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
 __global__ void __launch_bounds__(BX *BY)
     k_decide_dt(Grid g, Metrics m, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
                 unsigned long long *__restrict__ acc, double *__restrict__ sc, int *__restrict__ status,
-                double dt_fixed, double coef_adv, double r_a0, double r_a1, double r_a2, double r_b0, double r_b1,
-                double r_b2) {
+                double dt_fixed, double coef_adv) {
   __shared__ unsigned long long colmax[BY][BX];
   __shared__ unsigned long long ymax[BY * BX];
   __shared__ bool last;
@@ -740,22 +810,26 @@ __global__ void __launch_bounds__(BX *BY)
     dt *= coef_adv;
     dt = fmin(dt, dt_fixed);
     if (bad[0] || by >= kInfBits) atomicOr(status, 1);
-    const double al[3] = {r_a0, r_a1, r_a2}, be[3] = {r_b0, r_b1, r_b2};
+    // per-substage scalars; RK3 coefficients of src/runge_kutta.c:8-15
+    const double al[3] = {32. / 60., 25. / 60., 45. / 60.};
+    const double be[3] = {0. / 60., -17. / 60., -25. / 60.};
     sc[0] = dt;
     for (int k = 0; k < 3; ++k) {
-      const double gk = al[k] + be[k];
       const int ko = (k + 2) % 3;
-      const double go = al[ko] + be[ko];
-      const double dtold = go * dt, dtnew = gk * dt;
+      const double dtold = (al[ko] + be[ko]) * dt, dtnew = (al[k] + be[k]) * dt;
       sc[sc_adt(k)] = al[k] * dt;
       sc[sc_bdt(k)] = be[k] * dt;
-      sc[sc_gdt(k)] = gk * dt;
+      sc[sc_gdt(k)] = (al[k] + be[k]) * dt;
       sc[sc_dtold(k)] = dtold;
       sc[sc_dtnew(k)] = dtnew;
-      sc[sc_pdiv(k)] = ph.refden / dtnew / g.ny;
-      sc[sc_padd(k)] = -(dtold / dtnew) / g.ny;
-      sc[sc_cnew(k)] = dtnew / ph.refden;
-      sc[sc_cold(k)] = -dtold;
+      const double cdiv = ph.refden / dtnew * (0.5 / g.ny);
+      const double cadd = -(dtold / dtnew) * (0.5 / g.ny);
+      sc[sc_pdx(k)] = cdiv * g.idx;
+      sc[sc_pdy(k)] = cdiv * g.ihy;
+      sc[sc_pax(k)] = cadd * (g.idx * g.idx);
+      sc[sc_pay(k)] = cadd * (g.ihy * g.ihy);
+      sc[sc_cnew(k)] = dtnew * ph.irefden;
+      sc[sc_cold(k)] = -dtold * ph.irefden;
     }
   }
   __syncthreads();
@@ -763,16 +837,16 @@ __global__ void __launch_bounds__(BX *BY)
   for (int i = tid; i <= g.nx + 3; i += BX * BY) acc[i] = 0ULL;
 }
 
-// 1 / rho at ux faces (I = 1..nx+1) and uy faces (I = 1..nx) from a density
-// field, as k_predict stores them (fine-grained entry points); I = 1..nx+1
-__global__ void k_inv_face_density(Grid g, const double *__restrict__ den, double *__restrict__ irhox,
-                                   double *__restrict__ irhoy) {
+// e = rho_ref / rho - 1 at ux faces (I = 1..nx+1) and uy faces (I = 1..nx)
+// from a density field, as k_predict stores it (fine-grained entry points)
+__global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, double *__restrict__ ex,
+                              double *__restrict__ ey) {
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int r = J - 1, rm = wrap(J - 1, g.ny);
-  irhox[ix(g, r, I - 1)] = __drcp_rn(half_sum(den[ix(g, r, I - 1)], den[ix(g, r, I)]));
-  if (I <= g.nx) irhoy[ix(g, r, I)] = __drcp_rn(half_sum(den[ix(g, rm, I)], den[ix(g, r, I)]));
+  ex[ix(g, r, I - 1)] = fma(ph.refden, rcp_nr(half_sum(den[ix(g, r, I - 1)], den[ix(g, r, I)])), -1.);
+  if (I <= g.nx) ey[ix(g, r, I)] = fma(ph.refden, rcp_nr(half_sum(den[ix(g, rm, I)], den[ix(g, r, I)])), -1.);
 }
 
 // ---- boundary kernels of the fine-grained entry points (one thread per row)
@@ -801,9 +875,69 @@ __global__ void k_bc_vof(Grid g, double *vof) {
   vof[ix(g, J - 1, g.nx + 1)] = 0.;
 }
 
+// test hook: the Newton-Raphson reciprocal and inverse square root on n inputs
+__global__ void k_nr_check(const double *__restrict__ x, double *__restrict__ rcp, double *__restrict__ rsq, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  rcp[i] = rcp_nr(x[i]);
+  rsq[i] = rsqrt_nr(x[i]);
+}
+
 constexpr int kFftCols = 4;
 
+// FP64 fused multiply-add throughput: 8 independent chains per thread, every
+// thread writes only its own output element
+__global__ void k_fp64_peak(double *out, int iters, double seed) {
+  const double m = 0.999999, c = 1e-7;
+  double a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = seed + 1e-3 * j + 1e-9 * threadIdx.x;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fma(a[j], m, c);
+  }
+  double s = 0.;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
+
+cudaError_t measure_fp64_peak(double *gflops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 8192;
+  double *out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(double) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int w = 0; w < 3; ++w) k_fp64_peak<<<blocks, threads>>>(out, iters, 0.1);
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(e0);
+    k_fp64_peak<<<blocks, threads>>>(out, iters, 0.1);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = ms < best ? ms : best;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *gflops = 2.0 * 8.0 * blocks * threads * (double)iters / (best * 1e-3) / 1e9;
+  return e;
+}
+
+cudaError_t nr_check(const double *x, double *rcp, double *rsq, int n) {
+  k_nr_check<<<(n + 255) / 256, 256>>>(x, rcp, rsq, n);
+  return cudaDeviceSynchronize();
+}
 
 // ===========================================================================
 // launch helpers
@@ -811,12 +945,13 @@ constexpr int kFftCols = 4;
 
 int poisson_fft_cols(int) { return kFftCols; }
 size_t poisson_fft_smem(int ny) { return sizeof(double2) * 2 * kFftCols * (size_t)(ny / 2); }
+int tdm_chunk(int nx) { return (nx + 31) / 32; }
+int tdm_stride(int nx) { return tdm_chunk(nx) | 1; }
 int poisson_tdm_modes(int nx) {
-  int mb = 8;
-  while (mb > 1 && sizeof(double2) * (size_t)nx * mb > 200 * 1024) mb >>= 1;
-  return mb;
+  const size_t per_mode = 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double);
+  return per_mode * 4 <= 200 * 1024 ? 4 : (per_mode * 2 <= 200 * 1024 ? 2 : 1);
 }
-size_t poisson_tdm_smem(int nx) { return sizeof(double2) * (size_t)nx * poisson_tdm_modes(nx); }
+size_t poisson_tdm_smem(int nx) { return 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double) * poisson_tdm_modes(nx); }
 
 cudaError_t configure_kernels() {
   cudaError_t e;
@@ -844,25 +979,34 @@ void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &p
     k_props<false, false, true><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
 }
 
-void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv) {
+void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv,
+                        bool store_k) {
   const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
-  if (normal && curv) k_normal_curv<true, true><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
-  else if (normal) k_normal_curv<true, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
-  else if (curv) k_normal_curv<false, true><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+  if (normal && curv && store_k)
+    k_normal_curv<true, true, true><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+  else if (normal && curv)
+    k_normal_curv<true, true, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+  else if (normal)
+    k_normal_curv<true, false, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+  else if (curv)
+    k_normal_curv<false, true, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
 }
 
 void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                       const double *ux, const double *uy, const double *den0, bool flux, bool force) {
+                       const double *ux, const double *uy, const double *den0, bool flux, bool force, bool have_k) {
   const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
-  if (flux && force)
-    k_flux_force<true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx, b.fluxy,
-                                               b.ifrcx, b.ifrcy);
+  if (flux && force && have_k)
+    k_flux_force<true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+                                                     b.fluxy, b.ifrcx, b.ifrcy);
+  else if (flux && force)
+    k_flux_force<true, true, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+                                                      b.fluxy, b.ifrcx, b.ifrcy);
   else if (flux)
-    k_flux_force<true, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx, b.fluxy,
-                                                b.ifrcx, b.ifrcy);
+    k_flux_force<true, false, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+                                                       b.fluxy, b.ifrcx, b.ifrcy);
   else if (force)
-    k_flux_force<false, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx, b.fluxy,
-                                                b.ifrcx, b.ifrcy);
+    k_flux_force<false, true, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+                                                       b.fluxy, b.ifrcx, b.ifrcy);
 }
 
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
@@ -898,17 +1042,18 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                                                         b.irhoy);
 }
 
-void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                        const double *sc, int k, const double *ux, const double *uy, const double *psi_old) {
+void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
+                        const double *uy, const double *psi_old) {
   const int nb = (g.nx + kFftCols - 1) / kFftCols;
-  k_poisson_fwd<kFftCols><<<nb, 256, poisson_fft_smem(g.ny), s>>>(g, m, ph, sc, k, ux, uy, psi_old, b.irhox,
-                                                                  b.irhoy, b.twiddle, b.spec);
+  k_poisson_fwd<kFftCols><<<nb, 256, poisson_fft_smem(g.ny), s>>>(g, sc, k, ux, uy, psi_old, b.irhox, b.irhoy,
+                                                                  b.twiddle, b.spec);
 }
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
   const int mb = poisson_tdm_modes(g.nx);
   const int M1 = g.ny / 2 + 1;
-  k_poisson_tdm<<<(M1 + mb - 1) / mb, 256, poisson_tdm_smem(g.nx), s>>>(g, mb, b.tdm_fac, b.spec);
+  k_poisson_tdm<<<(M1 + mb - 1) / mb, 64 * mb, poisson_tdm_smem(g.nx), s>>>(
+      g, mb, tdm_chunk(g.nx), tdm_stride(g.nx), reinterpret_cast<const double4_32a *>(b.tdm_fac), b.spec);
 }
 
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
@@ -916,20 +1061,20 @@ void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *ps
   k_poisson_inv<kFftCols><<<nb, 256, poisson_fft_smem(g.ny), s>>>(g, b.twiddle, b.spec, psi_new);
 }
 
-void launch_poisson(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
-                    int k, const double *ux, const double *uy, const double *psi_old, double *psi_new) {
-  launch_poisson_fwd(s, g, m, ph, b, sc, k, ux, uy, psi_old);
+void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
+                    const double *uy, const double *psi_old, double *psi_new) {
+  launch_poisson_fwd(s, g, b, sc, k, ux, uy, psi_old);
   launch_poisson_tdm(s, g, b);
   launch_poisson_inv(s, g, b, psi_new);
 }
 
-void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
-                    int k, double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure) {
+void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
+                    double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure) {
   const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
   if (pressure)
-    k_correct<true><<<gr, bl, 0, s>>>(g, m, ph, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
+    k_correct<true><<<gr, bl, 0, s>>>(g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
   else
-    k_correct<false><<<gr, bl, 0, s>>>(g, m, ph, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
+    k_correct<false><<<gr, bl, 0, s>>>(g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
 }
 
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new) {
@@ -938,19 +1083,15 @@ void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double 
 
 void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                       const double *ux, const double *uy, double dt_fixed, double coef_adv) {
-  // RK3 coefficients (reference src/runge_kutta.c:8-15)
-  const double a0 = 32. / 60., b0 = 0. / 60.;
-  const double a1 = 25. / 60., b1 = -17. / 60.;
-  const double a2 = 45. / 60., b2 = -25. / 60.;
   int gy = (g.ny + BY - 1) / BY;
   const int gx = (g.nx + BX) / BX;
   while (gy > 1 && gx * gy > 4 * 152) gy = (gy + 1) / 2;
   k_decide_dt<<<dim3(gx, gy), dim3(BX, BY), 0, s>>>(g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
-                                                    coef_adv, a0, a1, a2, b0, b1, b2);
+                                                    coef_adv);
 }
 
-void launch_inv_face_density(cudaStream_t s, const Grid &g, const double *den, double *irhox, double *irhoy) {
-  k_inv_face_density<<<grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s>>>(g, den, irhox, irhoy);
+void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey) {
+  k_face_factor<<<grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s>>>(g, ph, den, ex, ey);
 }
 
 void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux) { k_bc_ux<<<(g.ny + 127) / 128, 128, 0, s>>>(g, ux); }

@@ -19,10 +19,10 @@ struct Bufs {
   double *fluxx, *fluxy, *mfluxx, *mfluxy;
   // RK sources
   double *srcux[3], *srcuy[3], *srcvof[2];
-  // inverse face densities 1 / rho^{k+1} at ux and uy faces
+  // face factors e = rho_ref / rho^{k+1} - 1 at ux and uy faces
   double *irhox, *irhoy;
   // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
-  double2 *spec, *tdm_fac;
+  double2 *spec, *tdm_fac;  // tdm_fac: (w, v, P, Q) per row, see k_poisson_tdm
   double2 *twiddle;  // exp(-2 pi i m / ny), m = 0..ny/2
   // decide_dt accumulators and per-step scalars
   unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
@@ -33,9 +33,12 @@ struct Bufs {
 // ---- launch helpers (defined in sbfs_kernels.cu), all on stream `s`
 void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                   bool den, bool vis, bool grad, double *den_out);
-void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv);
+// store_k: normal[2] = 1/phi - 1 (fused step) instead of the intercept
+void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv,
+                        bool store_k);
+// have_k: normal[2] holds 1/phi - 1 instead of the intercept
 void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                       const double *ux, const double *uy, const double *den0, bool flux, bool force);
+                       const double *ux, const double *uy, const double *den0, bool flux, bool force, bool have_k);
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                         const double *sc, int k, double *src_a, const double *src_b, bool fused,
                         const double *ux, const double *uy, double *den1);
@@ -47,20 +50,19 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                     const double *mfx, const double *mfy, const double *den0, const double *den1,
                     double *srcux_a, const double *srcux_b, double *srcux_g,
                     double *srcuy_a, const double *srcuy_b, double *srcuy_g);
-void launch_poisson(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                    const double *sc, int k, const double *ux, const double *uy, const double *psi_old,
-                    double *psi_new);
-void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                        const double *sc, int k, const double *ux, const double *uy, const double *psi_old);
+void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
+                    const double *uy, const double *psi_old, double *psi_new);
+void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
+                        const double *uy, const double *psi_old);
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b);
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new);
-void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                    const double *sc, int k, double *ux, double *uy, const double *psi_new,
-                    const double *psi_old, bool pressure);
+void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
+                    double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure);
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new);
 void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                       const double *ux, const double *uy, double dt_fixed, double coef_adv);
-void launch_inv_face_density(cudaStream_t s, const Grid &g, const double *den, double *irhox, double *irhoy);
+// e = rho_ref / rho - 1 at the faces from a density field (as k_predict stores it)
+void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey);
 // boundary kernels of the fine-grained entry points
 void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux);
 void launch_bc_uy(cudaStream_t s, const Grid &g, double *uy);
@@ -70,8 +72,13 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
 // smem budget checks (host side)
 int poisson_fft_cols(int ny);
 int poisson_tdm_modes(int nx);
+int tdm_chunk(int nx);
 size_t poisson_fft_smem(int ny);
 size_t poisson_tdm_smem(int nx);
 cudaError_t configure_kernels();
+// Newton-Raphson reciprocal / inverse square root of n device inputs (tests)
+cudaError_t nr_check(const double *x, double *rcp, double *rsq, int n);
+// FP64 FMA throughput of this GPU, GFLOP/s (2 flops per FMA)
+cudaError_t measure_fp64_peak(double *gflops);
 
 }  // namespace sbfs
