@@ -131,6 +131,33 @@ const char *sbfs_kernel_name(int cls);
 int sbfs_profile_steps(const domain_t *domain, fluid_t *fluid, interface_t *interface, int nsteps,
                        float *ms_per_class, int *launches_per_class);
 
+/* ---- decide_dt without allocation (no counterpart in the reference).
+ * For callers that may not allocate GPU memory -- programs that hand out
+ * device memory only from their own pre-sized pool, or that must not call
+ * cudaMalloc/cudaFree while running because those calls synchronise the GPU
+ * and take unbounded time.  The velocities are already on the GPU; the
+ * kernel's scratch (per-column maxima and a block counter) lives in a fixed
+ * array inside the library (SBFS_NOALLOC_MAX_NX + 8 words, 64 KB, one copy on
+ * every GPU that loads the library, kept until the process exits), so the
+ * call allocates nothing.
+ *   ux, uy  device arrays of ny rows with `pitch` doubles per row; row j
+ *           holds UX(1..nx+1, j+1) and UY(0..nx+1, j+1) from column 0
+ *   hxxf    device array HXXF(1..nx+1)
+ *   scalars device array of SBFS_STEP_SCALARS doubles; [0] receives dt
+ *   status  device int; bit 0 is set when a velocity is not finite
+ *   stream  the cudaStream_t to run on (NULL: the legacy default stream)
+ * The result is ready when the stream reaches it.  The first call on each
+ * GPU resolves the address of that GPU's scratch array (make it before any
+ * stream capture).  Every call shares the one array: calls that overlap on
+ * the GPU race and give wrong results.  nx > SBFS_NOALLOC_MAX_NX is rejected.
+ * Message of the last failure: sbfs_noalloc_last_error(). */
+#define SBFS_NOALLOC_MAX_NX 8192
+#define SBFS_STEP_SCALARS 64
+int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, const double *ux, const double *uy, int pitch,
+                           const double *hxxf, double Re, double denr, double visr, double We, double coef_adv,
+                           double coef_dif, double coef_int, double *scalars, int *status, void *stream);
+const char *sbfs_noalloc_last_error(void);
+
 /* device status bits: 1 = non-finite velocity seen by decide_dt */
 int sbfs_device_status(int *status);
 
