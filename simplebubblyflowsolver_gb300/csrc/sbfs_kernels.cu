@@ -610,6 +610,7 @@ __global__ void __launch_bounds__(256)
     const double4_32a *f = fac + (size_t)m * L * 32 + lane;
     // forward, local from a zero carry
     double t = 0.;
+#pragma unroll 8
     for (int k = 0; k < L; ++k) {
       const double4_32a c = f[(size_t)k * 32];
       t = fma(-c.y, t, c.x * x[k]);
@@ -628,6 +629,7 @@ __global__ void __launch_bounds__(256)
     if (lane == 0) carry = 0.;
     // fix up the forward solution, then the backward sweep from a zero carry
     double u = 0.;
+#pragma unroll 8
     for (int k = L - 1; k >= 0; --k) {
       const double4_32a c = f[(size_t)k * 32];
       const double y = fma(c.z, carry, x[k]);
@@ -646,6 +648,7 @@ __global__ void __launch_bounds__(256)
     double next = __shfl_down_sync(0xffffffffu, Sx, 1);
     if (lane == 31) next = 0.;
     double acc = 0.;
+#pragma unroll 8
     for (int k = 0; k < L; ++k) {
       const double v = fma(f[(size_t)k * 32].w, next, x[k]);
       x[k] = v;
