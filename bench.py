@@ -49,8 +49,9 @@ HBM_FALLBACK_GBS = 6800.0
 # writes counted once per cell (8 bytes per double); see the design doc
 ALG_DOUBLES_PER_CELL = {
     "k_props": 1 + 4,          # vof -> visux, visuy, dvof(2)
-    "k_normal_curv": 3 + 4,    # vof, dvof(2) -> curv, normal(3)
-    "k_flux_force": 8 + 4,     # ux, uy, vof, den, curv, normal(3) -> fluxx, fluxy, ifrcx, ifrcy
+    "k_curv_list": 3 + 1,      # vof, dvof(2) -> curv (+ list of interface cells)
+    "k_interface_cells": 0,    # listed cells only (a few percent of the domain)
+    "k_flux_force": 5 + 4,     # ux, uy, vof, den, curv -> fluxx, fluxy, ifrcx, ifrcy
     "k_vof_advance": 6 + 5,    # fluxx, fluxy, vof, src_b, ux, uy -> src_a, vof, den1, mflux(2)
     "k_stress": 4 + 3,         # ux, uy, visux, visuy -> txx, txy, tyy
     "k_predict": 14 + 6,       # ux, uy, mflux(2), t(3), p, ifrc(2), den(2), src_b(2) -> u*(2), src_a(2), 1/rho(2)

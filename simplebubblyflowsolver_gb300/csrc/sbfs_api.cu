@@ -346,6 +346,10 @@ int make_ctx(const domain_t *d) {
   b.twiddle = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, (size_t)c->nx + 8)) return 1;
   b.dt_acc = reinterpret_cast<unsigned long long *>(tmp);
+  if (dalloc(*c, &tmp, ((size_t)c->nx * c->ny + 2) / 2 + 1)) return 1;
+  b.ilist = reinterpret_cast<int *>(tmp);
+  if (dalloc(*c, &tmp, 1)) return 1;
+  b.icount = reinterpret_cast<int *>(tmp);
   if (dalloc(*c, &tmp, kScalars + 2)) return 1;
   b.scalars = tmp;
   b.status = reinterpret_cast<int *>(tmp + kScalars);
@@ -445,10 +449,10 @@ struct Prof {
 } g_prof;
 
 enum KernelClass {
-  KC_PROPS, KC_NORMAL_CURV, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_STRESS, KC_PREDICT,
+  KC_PROPS, KC_CURV_LIST, KC_INTERFACE, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_STRESS, KC_PREDICT,
   KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_COUNT
 };
-const char *kKernelNames[KC_COUNT] = {"k_props", "k_normal_curv", "k_flux_force", "k_vof_advance", "k_stress",
+const char *kKernelNames[KC_COUNT] = {"k_props", "k_curv_list", "k_interface_cells", "k_flux_force", "k_vof_advance", "k_stress",
                                       "k_predict", "k_poisson_fwd", "k_poisson_tdm", "k_poisson_inv", "k_correct",
                                       "k_decide_dt"};
 
@@ -476,8 +480,9 @@ void enqueue_substage(Ctx &c, int k) {
   double *sva = c.SV[c.isrc], *svb = c.SV[c.isrc ^ 1];
   const double *sc = b.scalars;
   timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
-  timed(c, KC_NORMAL_CURV, [&] { launch_normal_curv(c.s, c.g, c.m, b, true, true, true); });
-  timed(c, KC_FLUX_FORCE, [&] { launch_flux_force(c.s, c.g, c.m, c.ph, b, ux, uy, den0, true, true, true); });
+  timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
+  timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
+  timed(c, KC_FLUX_FORCE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 2); });
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
   timed(c, KC_PREDICT, [&] {
@@ -493,7 +498,7 @@ void enqueue_substage(Ctx &c, int k) {
   c.iden ^= 1;
 }
 
-constexpr int kKernelsPerStep = 1 + 3 * 10;
+constexpr int kKernelsPerStep = 1 + 3 * 11;
 
 void enqueue_step(Ctx &c) {
   timed(c, KC_DECIDE_DT,

@@ -157,7 +157,7 @@ __device__ __forceinline__ double thinc_face(double na, double nb, double K, dou
 // reference's intercept d (then K = exp(-2 d)).
 // thread (I, J): I = 1..nx handles x face I (I >= 2) and y face (I, J - 1/2)
 // ---------------------------------------------------------------------------
-template <bool FLUX, bool FORCE, bool HAVE_K>
+template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY = false>
 __global__ void __launch_bounds__(BX *BY)
     k_flux_force(Grid g, Metrics m, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
                  const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
@@ -176,30 +176,26 @@ __global__ void __launch_bounds__(BX *BY)
       const bool n = neg(vel);
       const int iu = n ? I : I - 1;
       const double phi = n ? v0 : vxm;
-      double f;
       if (single_phase(phi)) {
-        f = vel * phi;
-      } else {
+        fluxx[ix(g, r, I - 1)] = vel * phi;
+      } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)r * g.p3 + (size_t)(iu - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
-        f = vel * thinc_face(nv[0], nv[1], K, n ? -0.5 : 0.5);
+        fluxx[ix(g, r, I - 1)] = vel * thinc_face(nv[0], nv[1], K, n ? -0.5 : 0.5);
       }
-      fluxx[ix(g, r, I - 1)] = f;
     }
     {
       const double vel = uy[ix(g, r, I)];
       const bool n = neg(vel);
       const int ru = n ? r : rm;
       const double phi = n ? v0 : vym;
-      double f;
       if (single_phase(phi)) {
-        f = vel * phi;
-      } else {
+        fluxy[ix(g, r, I)] = vel * phi;
+      } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)ru * g.p3 + (size_t)(I - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
-        f = vel * thinc_face(nv[1], nv[0], K, n ? -0.5 : 0.5);
+        fluxy[ix(g, r, I)] = vel * thinc_face(nv[1], nv[0], K, n ? -0.5 : 0.5);
       }
-      fluxy[ix(g, r, I)] = f;
     }
     // impermeable walls / dummy ghost faces
     if (I == 1) {
@@ -229,6 +225,86 @@ __global__ void __launch_bounds__(BX *BY)
       f = (rho * kap) * ((0.25 * ph.force_coef * g.ihy) * (v0 - vym));
     }
     ifrcy[ix(g, r, I - 1)] = f;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interface compaction of the fused step.  THINC work (normal, intercept,
+// two exponentials per face) exists only in interface cells, a few percent
+// of the domain scattered along the bubbles; done in place it makes whole
+// warps wait on a few lanes.  So:
+//   k_curv_list       curvature of every cell (curvature_tensor.c:100-135)
+//                     and a list of the interface cells (warp-aggregated)
+//   k_interface_cells one thread per listed cell: normal and K = 1/phi - 1
+//                     (curvature_tensor.c:51-97), then the THINC flux of each
+//                     face the cell is upwind of (update/fluxx.c, fluxy.c)
+//   k_flux_force<.., BULK_ONLY>  every other face (upwind cell single-phase:
+//                     flux = vel phi) and the CSF force
+// Each face is written by exactly one of them: the upwind choice and the
+// vofmin test are the same integer tests in both.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const double *__restrict__ vof,
+                                                      const double *__restrict__ dvof, double *__restrict__ curv,
+                                                      int *__restrict__ list, int *__restrict__ count) {
+  const int I = blockIdx.x * BX + threadIdx.x + 1;
+  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const bool in = I <= g.nx && J <= g.ny;
+  bool itf = false;
+  if (in) {
+    const int r = J - 1, rp = wrap(J + 1, g.ny);
+    const double2 *dv = reinterpret_cast<const double2 *>(dvof);
+    const size_t q = g.p2 / 2;
+    const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
+    const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
+    const long long any = dbits(d00.x) | dbits(d00.y) | dbits(d10.x) | dbits(d10.y) | dbits(d01.x) | dbits(d01.y) |
+                          dbits(d11.x) | dbits(d11.y);
+    double k = -0.;
+    if ((any << 1) != 0) {
+      const double ddx = (d10.x + d11.x) - (d00.x + d01.x);
+      const double ddy = (d01.y + d11.y) - (d00.y + d10.y);
+      k = -fma(0.5 * m.ihxxc[I], ddx, (0.5 * g.ihy) * ddy);
+    }
+    curv[ix(g, r, I)] = k;
+    itf = !single_phase(vof[ix(g, r, I)]);
+  }
+  // warp-aggregated append (a warp is 32 consecutive cells of one row)
+  const unsigned mask = __ballot_sync(0xffffffffu, itf);
+  if (mask) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (itf) list[base + __popc(mask & ((1u << lane) - 1u))] = (J - 1) * g.nx + (I - 1);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_interface_cells(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
+                      const double *__restrict__ vof, const double *__restrict__ dvof, const int *__restrict__ list,
+                      const int *__restrict__ count, double *__restrict__ fluxx, double *__restrict__ fluxy) {
+  const int n = *count;
+  const double2 *dv = reinterpret_cast<const double2 *>(dvof);
+  const size_t q = g.p2 / 2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int id = list[t];
+    const int r = id / g.nx, I = id - r * g.nx + 1;
+    const int J = r + 1, rp = wrap(J + 1, g.ny);
+    const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
+    const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
+    const double mx = (((d00.x + d10.x) + d01.x) + d11.x) * m.ihxxc[I];
+    const double my = (((d00.y + d10.y) + d01.y) + d11.y) * g.ihy;
+    const double inv = inv_norm(fma(mx, mx, my * my));
+    const double n0 = mx * inv, n1 = my * inv;
+    const double K = rcp_nr(vof[ix(g, r, I)]) - 1.;
+    // x faces I (left) and I + 1 (right); the wall faces belong to k_flux_force
+    const double ul = ux[ix(g, r, I - 1)], ur = ux[ix(g, r, I)];
+    if (I >= 2 && neg(ul)) fluxx[ix(g, r, I - 1)] = ul * thinc_face(n0, n1, K, -0.5);
+    if (I < g.nx && !neg(ur)) fluxx[ix(g, r, I)] = ur * thinc_face(n0, n1, K, 0.5);
+    // y faces J - 1/2 (bottom, stored in row J) and J + 1/2 (row J + 1)
+    const double vb = uy[ix(g, r, I)], vt = uy[ix(g, rp, I)];
+    if (neg(vb)) fluxy[ix(g, r, I)] = vb * thinc_face(n1, n0, K, -0.5);
+    if (!neg(vt)) fluxy[ix(g, rp, I)] = vt * thinc_face(n1, n0, K, 0.5);
   }
 }
 
@@ -1010,6 +1086,20 @@ void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
   else if (force)
     k_flux_force<false, true, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                        b.fluxy, b.ifrcx, b.ifrcy);
+}
+
+void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                            const double *ux, const double *uy, const double *den0, int stage) {
+  const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
+  if (stage == 0) {
+    cudaMemsetAsync(b.icount, 0, sizeof(int), s);
+    k_curv_list<<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.curv, b.ilist, b.icount);
+  } else if (stage == 1) {
+    k_interface_cells<<<4 * 152, 256, 0, s>>>(g, m, ux, uy, b.vof, b.dvof, b.ilist, b.icount, b.fluxx, b.fluxy);
+  } else {
+    k_flux_force<true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+                                                           b.fluxy, b.ifrcx, b.ifrcy);
+  }
 }
 
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,

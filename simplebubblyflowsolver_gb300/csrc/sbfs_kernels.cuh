@@ -28,6 +28,8 @@ struct Bufs {
   unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
   double *scalars;             // kScalars doubles
   int *status;                 // device error word
+  // interface cells of the current substage (linear index (J-1)*nx + I-1) and their count
+  int *ilist, *icount;
 };
 
 // ---- launch helpers (defined in sbfs_kernels.cu), all on stream `s`
@@ -39,6 +41,10 @@ void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const B
 // have_k: normal[2] holds 1/phi - 1 instead of the intercept
 void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                        const double *ux, const double *uy, const double *den0, bool flux, bool force, bool have_k);
+// fused interface stage: 0 = curvature + interface-cell list, 1 = dense THINC
+// fluxes of the listed cells, 2 = bulk fluxes and the CSF force
+void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                            const double *ux, const double *uy, const double *den0, int stage);
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                         const double *sc, int k, double *src_a, const double *src_b, bool fused,
                         const double *ux, const double *uy, double *den1);
