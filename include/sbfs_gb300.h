@@ -131,6 +131,30 @@ const char *sbfs_kernel_name(int cls);
 int sbfs_profile_steps(const domain_t *domain, fluid_t *fluid, interface_t *interface, int nsteps,
                        float *ms_per_class, int *launches_per_class);
 
+/* ---- monitoring on the GPU (reference src/logging/ and src/statistics.c);
+ * they read the device state (uploading the host state first unless the
+ * device-resident mode holds it) */
+typedef struct {
+  double divmax;           /* max |div u|                 logging/divergence.c:41-64 */
+  double vof_min, vof_max; /* extrema of vof              logging/interface.c:34-45 */
+  double vof_integral;     /* sum vof J                   logging/interface.c:36-41 */
+  double volume;           /* sum J */
+  double interface_area;   /* sum |d vof| over faces      logging/interface.c:47-62 */
+  double momentum[2];      /* sum rho u J                 logging/momentum.c:40-56 */
+  double energy[2];        /* sum rho u^2 J / 2           logging/energy.c:42-58 */
+  double umax[2];          /* max |ux|, max |uy|          logging/extrema.c:25-38 */
+  double wall_stress[2];   /* nu sum txy at x = 0, lx     logging/stress.c:29-35 */
+} sbfs_diagnostics_t;
+int sbfs_diagnostics(const domain_t *domain, fluid_t *fluid, interface_t *interface, sbfs_diagnostics_t *out);
+/* running sums ux1, uy1, vof1 and their count (statistics.c:99-166) */
+int sbfs_statistics_collect(const domain_t *domain, fluid_t *fluid, interface_t *interface);
+int sbfs_statistics_reset(void);
+/* host copies: ux1 (ny, nx+1), uy1 and vof1 (ny, nx+2), the reference's layout */
+int sbfs_statistics_fetch(double *ux1, double *uy1, double *vof1, size_t *num);
+/* writes num, ux1, uy1, vof1 and the domain into dirname as the reference's
+ * statistics output does (statistics.c:174-216) */
+int sbfs_statistics_output(const char dirname[], const domain_t *domain);
+
 /* ---- decide_dt without allocation (no counterpart in the reference).
  * For callers that may not allocate GPU memory -- programs that hand out
  * device memory only from their own pre-sized pool, or that must not call

@@ -46,6 +46,7 @@ class Oracle(ReferenceAPI):
         lib.orc_get_threads.restype = C.c_int
         lib.orc_max_divergence.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
         lib.orc_vof_stats.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double * 4)]
+        lib.orc_diagnostics.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double * 16)]
 
     def set_dt_coefs(self, adv, dif, itf):
         self.lib.orc_set_dt_coefs(adv, dif, itf)
@@ -61,10 +62,23 @@ class Oracle(ReferenceAPI):
         self.lib.orc_max_divergence(C.addressof(st.domain), C.addressof(st.fluid), C.byref(out))
         return out.value
 
+    def diagnostics(self, st) -> dict:
+        out = (C.c_double * 16)()
+        self.lib.orc_diagnostics(*self._ptrs(st), C.byref(out))
+        return diag_dict(list(out))
+
     def vof_stats(self, st):
         out = (C.c_double * 4)()
         self.lib.orc_vof_stats(C.addressof(st.domain), C.addressof(st.interface), C.byref(out))
         return tuple(out)
+
+
+DIAG_NAMES = ["divmax", "vof_min", "vof_max", "vof_integral", "volume", "interface_area", "momentum_x",
+              "momentum_y", "energy_x", "energy_y", "umax", "vmax", "wall_stress_xm", "wall_stress_xp"]
+
+
+def diag_dict(vals) -> dict:
+    return dict(zip(DIAG_NAMES, vals))
 
 
 def ref_available() -> bool:

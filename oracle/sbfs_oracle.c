@@ -952,3 +952,59 @@ int orc_vof_stats(const domain_t *dom, const interface_t *itf, double out[4]) {
   out[0] = lo; out[1] = hi; out[2] = s0; out[3] = s1;
   return 0;
 }
+
+/* all logging quantities of src/logging/{divergence,interface,momentum,energy,extrema,stress}.c
+ * in the order of sbfs_diagnostics:
+ * divmax, vof min, max, sum vof J, sum J, interface area, momentum x, y,
+ * energy x, y, max |ux|, max |uy|, wall stress at x = 0, lx */
+int orc_diagnostics(const domain_t *dom, const fluid_t *fl, const interface_t *itf, double out[16]) {
+  const int nx = (int)dom->mysizes[0], ny = (int)dom->mysizes[1];
+  const double hy = dom->hy;
+  double st[4];
+  for (int k = 0; k < 16; k++) out[k] = 0.;
+  orc_max_divergence(dom, fl, &out[0]);
+  orc_vof_stats(dom, itf, st);
+  out[1] = st[0]; out[2] = st[1]; out[3] = st[2]; out[4] = st[3];
+  fview vof = view_of(dom, &itf->vof, 1);
+  fview den = view_of(dom, &fl->den[1], 1);
+  fview ux = view_of(dom, &fl->ux, 1);
+  fview uy = view_of(dom, &fl->uy, 1);
+  fview txy = view_of(dom, &fl->txy, 1);
+  /* interface area (src/logging/interface.c:47-62) */
+  double area = 0.;
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx + 1; i++) area += fabs(F(vof, i, j) - F(vof, i - 1, j)) * (JDXF(i) / HXXF(i));
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) area += fabs(F(vof, i, j) - F(vof, i, j - 1)) * (JDXC(i) / hy);
+  out[5] = area;
+  /* momentum, energy, extrema (momentum.c:40-56, energy.c:42-58, extrema.c:25-38) */
+  double mx = 0., my = 0., ex = 0., ey = 0., umax = 0., vmax = 0.;
+  for (int j = 1; j <= ny; j++) {
+    for (int i = 2; i <= nx; i++) {
+      const double ds = JDXF(i);
+      const double r = 0.5 * F(den, i - 1, j) + 0.5 * F(den, i, j);
+      const double u = F(ux, i, j);
+      mx += r * u * ds;
+      ex += 0.5 * r * pow(u, 2.) * ds;
+      umax = fmax(umax, fabs(u));
+    }
+  }
+  for (int j = 1; j <= ny; j++) {
+    for (int i = 1; i <= nx; i++) {
+      const double ds = JDXC(i);
+      const double r = 0.5 * F(den, i, j - 1) + 0.5 * F(den, i, j);
+      const double v = F(uy, i, j);
+      my += r * v * ds;
+      ey += 0.5 * r * pow(v, 2.) * ds;
+      vmax = fmax(vmax, fabs(v));
+    }
+  }
+  out[6] = mx; out[7] = my; out[8] = ex; out[9] = ey; out[10] = umax; out[11] = vmax;
+  /* wall shear stress (stress.c:29-35) */
+  const double nu = 1. / fl->Re;
+  for (int j = 1; j <= ny; j++) {
+    out[12] += nu * JDXF(1) / HXXF(1) * F(txy, 1, j);
+    out[13] += nu * JDXF(nx + 1) / HXXF(nx + 1) * F(txy, nx + 1, j);
+  }
+  return 0;
+}

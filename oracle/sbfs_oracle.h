@@ -49,6 +49,9 @@ int orc_interface_update_boundaries_vof(const domain_t *domain, array_t *vof);
 int orc_max_divergence(const domain_t *domain, const fluid_t *fluid, double *divmax);
 int orc_vof_stats(const domain_t *domain, const interface_t *interface, double out[4]);
 
+/* every quantity of the reference's log files, see sbfs_diagnostics_t */
+int orc_diagnostics(const domain_t *domain, const fluid_t *fluid, const interface_t *interface, double out[16]);
+
 /* number of OpenMP threads the oracle uses (0 = library default) */
 void orc_set_threads(int nthreads);
 int orc_get_threads(void);

@@ -44,6 +44,9 @@ class GpuLibrary(ReferenceAPI):
         lib.sbfs_device_status.argtypes = [C.POINTER(C.c_int)]
         lib.sbfs_set_device.argtypes = [C.c_int]
         lib.sbfs_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+        lib.sbfs_diagnostics.argtypes = [C.c_void_p] * 4
+        lib.sbfs_statistics_collect.argtypes = [C.c_void_p] * 3
+        lib.sbfs_statistics_fetch.argtypes = [C.POINTER(C.c_double)] * 3 + [C.POINTER(C.c_size_t)]
         lib.sbfs_check_newton_raphson.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int]
         lib.sbfs_pin_host_state.argtypes = [C.c_void_p, C.c_void_p]
         lib.sbfs_unpin_host_state.argtypes = [C.c_void_p, C.c_void_p]
@@ -97,6 +100,31 @@ class GpuLibrary(ReferenceAPI):
         self._ext("sbfs_check_newton_raphson", x.ctypes.data_as(dp), r.ctypes.data_as(dp), q.ctypes.data_as(dp),
                   x.size)
         return r, q
+
+    def diagnostics(self, st: SolverState) -> dict:
+        """the reference's logging quantities reduced on the GPU"""
+        out = (C.c_double * 14)()
+        self._ext("sbfs_diagnostics", *self._ptrs(st), C.byref(out))
+        names = ["divmax", "vof_min", "vof_max", "vof_integral", "volume", "interface_area", "momentum_x",
+                 "momentum_y", "energy_x", "energy_y", "umax", "vmax", "wall_stress_xm", "wall_stress_xp"]
+        return dict(zip(names, list(out)))
+
+    def statistics_collect(self, st: SolverState):
+        self._ext("sbfs_statistics_collect", *self._ptrs(st))
+
+    def statistics_reset(self):
+        self._ext("sbfs_statistics_reset")
+
+    def statistics_fetch(self, nx: int, ny: int):
+        import numpy as np
+        ux1 = np.zeros((ny, nx + 1))
+        uy1 = np.zeros((ny, nx + 2))
+        vof1 = np.zeros((ny, nx + 2))
+        num = C.c_size_t(0)
+        dp = C.POINTER(C.c_double)
+        self._ext("sbfs_statistics_fetch", ux1.ctypes.data_as(dp), uy1.ctypes.data_as(dp),
+                  vof1.ctypes.data_as(dp), C.byref(num))
+        return ux1, uy1, vof1, num.value
 
     def measure_fp64_peak(self) -> float:
         out = C.c_double(0.0)

@@ -83,6 +83,10 @@ struct Ctx {
   bool resident = false;  // device holds the current state
   std::map<int, cudaGraphExec_t> graphs;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  // diagnostics partials / result and statistics sums (allocated on first use)
+  double *diag_part = nullptr, *diag_out = nullptr;
+  double *st_ux1 = nullptr, *st_uy1 = nullptr, *st_vof1 = nullptr;
+  size_t st_num = 0;
 
   ~Ctx() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -630,6 +634,87 @@ int sbfs_invalidate_device(void) {
 }
 
 int sbfs_kernels_per_step(void) { return kKernelsPerStep; }
+
+// the state the device holds, uploaded first when the host is the truth
+static Ctx *diag_ctx(const domain_t *d, fluid_t *f, interface_t *itf) {
+  Ctx *c = prepare_step(d, f, itf);
+  if (!c) return nullptr;
+  if (!c->resident) {
+    if (upload_state(*c, f, itf)) return nullptr;
+    // the wall-stress log reads the caller's txy, as the reference's does
+    if (h2d(*c, f->txy, L_TXY, c->b.txy)) return nullptr;
+  }
+  return c;
+}
+
+// logging quantities of the reference (src/logging/), reduced on the GPU
+int sbfs_diagnostics(const domain_t *d, fluid_t *f, interface_t *itf, sbfs_diagnostics_t *out) {
+  Ctx *c = diag_ctx(d, f, itf);
+  if (!c) return 1;
+  if (!c->diag_part) {
+    if (dalloc(*c, &c->diag_part, (size_t)diag_partial_blocks(c->g) * 16) || dalloc(*c, &c->diag_out, 16)) return 1;
+  }
+  launch_diagnostics(c->s, c->g, c->m, c->U[c->iu], c->V[c->iu], c->b.vof, c->DEN[c->iden], c->b.txy, c->ph.nu,
+                     c->diag_part, c->diag_out);
+  double h[16];
+  CK(cudaMemcpyAsync(h, c->diag_out, sizeof(h), cudaMemcpyDeviceToHost, c->s));
+  if (sync(*c)) return 1;
+  out->divmax = h[0];
+  out->vof_min = h[1];
+  out->vof_max = h[2];
+  out->vof_integral = h[3];
+  out->volume = h[4];
+  out->interface_area = h[5];
+  out->momentum[0] = h[6];
+  out->momentum[1] = h[7];
+  out->energy[0] = h[8];
+  out->energy[1] = h[9];
+  out->umax[0] = h[10];
+  out->umax[1] = h[11];
+  out->wall_stress[0] = h[12];
+  out->wall_stress[1] = h[13];
+  return 0;
+}
+
+// running sums of src/statistics.c:99-166 kept on the GPU
+int sbfs_statistics_collect(const domain_t *d, fluid_t *f, interface_t *itf) {
+  Ctx *c = diag_ctx(d, f, itf);
+  if (!c) return 1;
+  if (!c->st_ux1) {
+    const size_t n1 = (size_t)c->g.p1 * c->g.ny;
+    if (dalloc(*c, &c->st_ux1, n1) || dalloc(*c, &c->st_uy1, n1) || dalloc(*c, &c->st_vof1, n1)) return 1;
+    c->st_num = 0;
+  }
+  launch_stats_collect(c->s, c->g, c->U[c->iu], c->V[c->iu], c->b.vof, c->st_ux1, c->st_uy1, c->st_vof1);
+  c->st_num += 1;
+  return sync(*c);
+}
+
+int sbfs_statistics_reset(void) {
+  Ctx *c = g_ctx.get();
+  if (!c || !c->st_ux1) return 0;
+  const size_t bytes = sizeof(double) * (size_t)c->g.p1 * c->g.ny;
+  CK(cudaMemsetAsync(c->st_ux1, 0, bytes, c->s));
+  CK(cudaMemsetAsync(c->st_uy1, 0, bytes, c->s));
+  CK(cudaMemsetAsync(c->st_vof1, 0, bytes, c->s));
+  c->st_num = 0;
+  return sync(*c);
+}
+
+// sums in the reference's statistics layout: ux1 (ny, nx+1), uy1 and vof1 (ny, nx+2)
+int sbfs_statistics_fetch(double *ux1, double *uy1, double *vof1, size_t *num) {
+  Ctx *c = g_ctx.get();
+  *num = (c && c->st_ux1) ? c->st_num : 0;
+  if (!*num) return 0;
+  const size_t p = sizeof(double) * c->g.p1;
+  CK(cudaMemcpy2DAsync(ux1, sizeof(double) * (c->nx + 1), c->st_ux1, p, sizeof(double) * (c->nx + 1), c->ny,
+                       cudaMemcpyDeviceToHost, c->s));
+  CK(cudaMemcpy2DAsync(uy1, sizeof(double) * (c->nx + 2), c->st_uy1, p, sizeof(double) * (c->nx + 2), c->ny,
+                       cudaMemcpyDeviceToHost, c->s));
+  CK(cudaMemcpy2DAsync(vof1, sizeof(double) * (c->nx + 2), c->st_vof1, p, sizeof(double) * (c->nx + 2), c->ny,
+                       cudaMemcpyDeviceToHost, c->s));
+  return sync(*c);
+}
 
 int sbfs_measure_fp64_peak(double *gflops) {
   CK(measure_fp64_peak(gflops));

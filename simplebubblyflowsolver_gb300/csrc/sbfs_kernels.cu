@@ -928,6 +928,109 @@ __global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, d
   if (I <= g.nx) ey[ix(g, r, I)] = fma(ph.refden, rcp_nr(half_sum(den[ix(g, rm, I)], den[ix(g, r, I)])), -1.);
 }
 
+// ---------------------------------------------------------------------------
+// diagnostics of the reference's log files (src/logging/), reduced on the device:
+//   [0] max |div u|                     src/logging/divergence.c:41-64
+//   [1] min vof, [2] max vof, [3] sum vof J, [4] sum J, [5] interface area
+//                                       src/logging/interface.c:34-65
+//   [6..7] momentum x, y                src/logging/momentum.c:40-56
+//   [8..9] kinetic energy x, y          src/logging/energy.c:42-58
+//   [10..11] max |ux|, max |uy|         src/logging/extrema.c:25-38
+//   [12..13] wall shear stress x = 0, lx  src/logging/stress.c:29-35
+// Per-block partials in a fixed order, then one block: deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kDiag = 16;
+
+__device__ __forceinline__ void block_reduce(double (*sm)[BX * BY], int tid, const double *v) {
+  for (int q = 0; q < kDiag; ++q) sm[q][tid] = v[q];
+  __syncthreads();
+  for (int w = BX * BY / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+      for (int q = 0; q < kDiag; ++q) {
+        const double a = sm[q][tid], b = sm[q][tid + w];
+        // 0 and 2 and 10..11 are maxima, 1 is a minimum, the rest sums
+        sm[q][tid] = (q == 0 || q == 2 || q == 10 || q == 11) ? fmax(a, b) : (q == 1 ? fmin(a, b) : a + b);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(BX *BY)
+    k_diag_partial(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
+                   const double *__restrict__ vof, const double *__restrict__ den, const double *__restrict__ txy,
+                   double nu, double *__restrict__ part) {
+  __shared__ double sm[kDiag][BX * BY];
+  const int I = blockIdx.x * BX + threadIdx.x + 1;
+  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  double v[kDiag];
+  for (int q = 0; q < kDiag; ++q) v[q] = 0.;
+  v[1] = 1.;  // the reference starts min at 1 and max at 0
+  if (I <= g.nx && J <= g.ny) {
+    const int r = J - 1, rm = wrap(J - 1, g.ny), rp = wrap(J + 1, g.ny);
+    const double jdxc = g.dx * g.hy;
+    const double div = (ux[ix(g, r, I)] - ux[ix(g, r, I - 1)]) * g.idx + (uy[ix(g, rp, I)] - uy[ix(g, r, I)]) * g.ihy;
+    v[0] = fabs(div);
+    const double phi = vof[ix(g, r, I)];
+    v[1] = phi;
+    v[2] = phi;
+    v[3] = phi * jdxc;
+    v[4] = jdxc;
+    v[5] = fabs(phi - vof[ix(g, r, I - 1)]) * g.hy + fabs(phi - vof[ix(g, rm, I)]) * g.dx;
+    if (I == g.nx) v[5] += fabs(vof[ix(g, r, g.nx + 1)] - phi) * g.hy;
+    if (I >= 2) {
+      const double u = ux[ix(g, r, I - 1)];
+      const double jdxf = m.hxxf[I] * g.hy;
+      const double rho = 0.5 * den[ix(g, r, I - 1)] + 0.5 * den[ix(g, r, I)];
+      v[6] = rho * u * jdxf;
+      v[8] = 0.5 * rho * u * u * jdxf;
+      v[10] = fabs(u);
+    }
+    const double w = uy[ix(g, r, I)];
+    const double rhoy = 0.5 * den[ix(g, rm, I)] + 0.5 * den[ix(g, r, I)];
+    v[7] = rhoy * w * jdxc;
+    v[9] = 0.5 * rhoy * w * w * jdxc;
+    v[11] = fabs(w);
+    // JDXF / HXXF = hy at the wall faces
+    if (I == 1) v[12] = nu * g.hy * txy[ix(g, r, 0)];
+    if (I == g.nx) v[13] = nu * g.hy * txy[ix(g, r, g.nx)];
+  }
+  block_reduce(sm, tid, v);
+  if (tid < kDiag) part[(size_t)(blockIdx.y * gridDim.x + blockIdx.x) * kDiag + tid] = sm[tid][0];
+}
+
+__global__ void __launch_bounds__(BX *BY) k_diag_final(const double *__restrict__ part, int nblocks,
+                                                       double *__restrict__ out) {
+  __shared__ double sm[kDiag][BX * BY];
+  const int tid = threadIdx.x;
+  double v[kDiag];
+  for (int q = 0; q < kDiag; ++q) v[q] = 0.;
+  v[1] = 1.;
+  for (int b = tid; b < nblocks; b += BX * BY) {
+    for (int q = 0; q < kDiag; ++q) {
+      const double x = part[(size_t)b * kDiag + q];
+      v[q] = (q == 0 || q == 2 || q == 10 || q == 11) ? fmax(v[q], x) : (q == 1 ? fmin(v[q], x) : v[q] + x);
+    }
+  }
+  block_reduce(sm, tid, v);
+  if (tid < kDiag) out[tid] = sm[tid][0];
+}
+
+// running sums of the statistics (src/statistics.c:99-151): ux1 += ux over
+// I = 1..nx+1, uy1 += uy and vof1 += vof over I = 0..nx+1
+__global__ void k_stats_collect(Grid g, const double *__restrict__ ux, const double *__restrict__ uy,
+                                const double *__restrict__ vof, double *__restrict__ ux1, double *__restrict__ uy1,
+                                double *__restrict__ vof1) {
+  const int I = blockIdx.x * BX + threadIdx.x;
+  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  if (I > g.nx + 1 || J > g.ny) return;
+  const int r = J - 1;
+  if (I >= 1) ux1[ix(g, r, I - 1)] += ux[ix(g, r, I - 1)];
+  uy1[ix(g, r, I)] += uy[ix(g, r, I)];
+  vof1[ix(g, r, I)] += vof[ix(g, r, I)];
+}
+
 // ---- boundary kernels of the fine-grained entry points (one thread per row)
 __global__ void k_bc_ux(Grid g, double *ux) {
   const int J = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -1185,6 +1288,24 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
 
 void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey) {
   k_face_factor<<<grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s>>>(g, ph, den, ex, ey);
+}
+
+int diag_partial_blocks(const Grid &g) {
+  const dim3 gr = grid2d(g.nx, g.ny);
+  return (int)(gr.x * gr.y);
+}
+
+void launch_diagnostics(cudaStream_t s, const Grid &g, const Metrics &m, const double *ux, const double *uy,
+                        const double *vof, const double *den, const double *txy, double nu, double *part,
+                        double *out) {
+  const dim3 gr = grid2d(g.nx, g.ny);
+  k_diag_partial<<<gr, dim3(BX, BY), 0, s>>>(g, m, ux, uy, vof, den, txy, nu, part);
+  k_diag_final<<<1, BX * BY, 0, s>>>(part, (int)(gr.x * gr.y), out);
+}
+
+void launch_stats_collect(cudaStream_t s, const Grid &g, const double *ux, const double *uy, const double *vof,
+                          double *ux1, double *uy1, double *vof1) {
+  k_stats_collect<<<grid2d(g.nx + 2, g.ny), dim3(BX, BY), 0, s>>>(g, ux, uy, vof, ux1, uy1, vof1);
 }
 
 void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux) { k_bc_ux<<<(g.ny + 127) / 128, 128, 0, s>>>(g, ux); }

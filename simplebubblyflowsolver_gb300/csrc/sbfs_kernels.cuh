@@ -69,6 +69,13 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
                       const double *ux, const double *uy, double dt_fixed, double coef_adv);
 // e = rho_ref / rho - 1 at the faces from a density field (as k_predict stores it)
 void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey);
+// logging diagnostics (16 doubles, see k_diag_partial) and statistics sums
+int diag_partial_blocks(const Grid &g);
+void launch_diagnostics(cudaStream_t s, const Grid &g, const Metrics &m, const double *ux, const double *uy,
+                        const double *vof, const double *den, const double *txy, double nu, double *part,
+                        double *out);
+void launch_stats_collect(cudaStream_t s, const Grid &g, const double *ux, const double *uy, const double *vof,
+                          double *ux1, double *uy1, double *vof1);
 // boundary kernels of the fine-grained entry points
 void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux);
 void launch_bc_uy(cudaStream_t s, const Grid &g, double *uy);

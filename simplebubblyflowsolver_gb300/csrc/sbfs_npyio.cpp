@@ -357,6 +357,19 @@ int interface_save(const char dir[], const domain_t *d, const interface_t *itf) 
   return dump_array(d, dir, "vof", &itf->vof);
 }
 
+int sbfs_statistics_output(const char dir[], const domain_t *d) {
+  const size_t nx = d->glsizes[0], ny = d->glsizes[1];
+  std::vector<double> ux1(ny * (nx + 1)), uy1(ny * (nx + 2)), vof1(ny * (nx + 2));
+  size_t num = 0;
+  if (sbfs_statistics_fetch(ux1.data(), uy1.data(), vof1.data(), &num)) return io_fail("%s", sbfs_last_error());
+  if (num == 0) return 0;  // nothing collected: nothing to save, as the reference
+  if (npy_write(dir, "num", "<u8", {}, sizeof(size_t), &num)) return 1;
+  if (domain_save(dir, d)) return 1;
+  if (npy_write(dir, "ux1", "<f8", {ny, nx + 1}, 8, ux1.data())) return 1;
+  if (npy_write(dir, "uy1", "<f8", {ny, nx + 2}, 8, uy1.data())) return 1;
+  return npy_write(dir, "vof1", "<f8", {ny, nx + 2}, 8, vof1.data());
+}
+
 int sbfs_free_state(domain_t *d, fluid_t *f, interface_t *itf) {
   if (f) {
     array_t *fa[] = {&f->ux, &f->uy, &f->p, &f->psi[0], &f->psi[1], &f->den[0], &f->den[1], &f->visux, &f->visuy,
