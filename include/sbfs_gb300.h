@@ -182,6 +182,33 @@ int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, const double *u
                            double coef_dif, double coef_int, double *scalars, int *status, void *stream);
 const char *sbfs_noalloc_last_error(void);
 
+/* ---- learned curvature closure (no reference counterpart) ----
+ * A 16 -> 64 -> 64 -> 1 ReLU perceptron mapping the 3x3 vof stencil of an
+ * interface cell and the cell normal to kappa * dx, evaluated with BF16
+ * tensor-core products (FP32 accumulate).  Feature row (16 bf16): the nine
+ * stencil values (y rows bottom to top, x fastest), the unit cell normal
+ * (x, y), five zeros.  Parameters: one FP32 vector of sbfs_mlp_nparams()
+ * values [W1 (64 x 16, row-major), b1 (64), W2 (64 x 64), b2 (64), w3 (64),
+ * b3].  X, Y, idx and out below are device pointers. */
+int sbfs_mlp_nparams(void);
+int sbfs_mlp_set_params(const float *host_params, int n); /* also resets Adam */
+int sbfs_mlp_get_params(float *host_params, int n);
+/* gradient (host, n params) and loss of the mean-square error over rows
+ * idx[0..n) of X (bf16 [rows][16]) against Y */
+int sbfs_mlp_gradient(const void *X, const float *Y, const int *idx, int n, float *grad_out, double *loss);
+/* Adam steps over consecutive batches of the row permutation idx[0..n) */
+int sbfs_mlp_train_epoch(const void *X, const float *Y, const int *idx, int n, int batch, float lr,
+                         double *mean_loss);
+int sbfs_mlp_predict(const void *X, int n, float *out);
+/* 0: kappa = -div n (the reference, default); 1: the learned closure in
+ * interface cells whose stencil is in range (centre vof in [0.01, 0.99], a
+ * prediction |kappa dx| in [0.015, 0.55]), plain kappa elsewhere.  Square
+ * cells.  Applies to integrate() and the timed runs. */
+int sbfs_set_curvature_model(int model);
+/* interface cells that took the learned curvature since the last call */
+int sbfs_mlp_take_usage(long long *used);
+const char *sbfs_mlp_last_error(void);
+
 /* device status bits: 1 = non-finite velocity seen by decide_dt */
 int sbfs_device_status(int *status);
 

@@ -159,6 +159,71 @@ class GpuLibrary(ReferenceAPI):
     def release(self):
         self._ext("sbfs_release")
 
+    # ---- learned curvature closure (device pointers are plain ints)
+    def _mlp(self, fn, *args):
+        rc = getattr(self.lib, fn)(*args)
+        if rc != 0:
+            raise SolverError(f"{fn} failed: {self.lib.sbfs_mlp_last_error().decode()}")
+
+    def _mlp_types(self):
+        L = self.lib
+        if getattr(L, "_mlp_typed", False):
+            return
+        vp, fp, dp = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double)
+        L.sbfs_mlp_last_error.restype = C.c_char_p
+        L.sbfs_mlp_set_params.argtypes = [fp, C.c_int]
+        L.sbfs_mlp_get_params.argtypes = [fp, C.c_int]
+        L.sbfs_mlp_gradient.argtypes = [vp, vp, vp, C.c_int, fp, dp]
+        L.sbfs_mlp_train_epoch.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, dp]
+        L.sbfs_mlp_predict.argtypes = [vp, C.c_int, vp]
+        L.sbfs_mlp_take_usage.argtypes = [C.POINTER(C.c_longlong)]
+        L.sbfs_set_curvature_model.argtypes = [C.c_int]
+        L._mlp_typed = True
+
+    def mlp_set_params(self, params):
+        import numpy as np
+        self._mlp_types()
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._mlp("sbfs_mlp_set_params", p.ctypes.data_as(C.POINTER(C.c_float)), p.size)
+
+    def mlp_get_params(self):
+        import numpy as np
+        self._mlp_types()
+        p = np.empty(self.lib.sbfs_mlp_nparams(), dtype=np.float32)
+        self._mlp("sbfs_mlp_get_params", p.ctypes.data_as(C.POINTER(C.c_float)), p.size)
+        return p
+
+    def mlp_gradient(self, X_ptr: int, Y_ptr: int, idx_ptr: int, n: int):
+        """(gradient (float32, host), loss) of the mean-square error over n rows"""
+        import numpy as np
+        self._mlp_types()
+        g = np.empty(self.lib.sbfs_mlp_nparams(), dtype=np.float32)
+        loss = C.c_double(0.0)
+        self._mlp("sbfs_mlp_gradient", X_ptr, Y_ptr, idx_ptr, n, g.ctypes.data_as(C.POINTER(C.c_float)),
+                  C.byref(loss))
+        return g, loss.value
+
+    def mlp_train_epoch(self, X_ptr: int, Y_ptr: int, idx_ptr: int, n: int, batch: int, lr: float) -> float:
+        self._mlp_types()
+        loss = C.c_double(0.0)
+        self._mlp("sbfs_mlp_train_epoch", X_ptr, Y_ptr, idx_ptr, n, batch, lr, C.byref(loss))
+        return loss.value
+
+    def mlp_predict(self, X_ptr: int, n: int, out_ptr: int):
+        self._mlp_types()
+        self._mlp("sbfs_mlp_predict", X_ptr, n, out_ptr)
+
+    def mlp_take_usage(self) -> int:
+        self._mlp_types()
+        u = C.c_longlong(0)
+        self._mlp("sbfs_mlp_take_usage", C.byref(u))
+        return u.value
+
+    def set_curvature_model(self, model: int):
+        """0: the reference's kappa = -div n; 1: the learned closure"""
+        self._mlp_types()
+        self._ext("sbfs_set_curvature_model", model)
+
 
 def load_library(path: str | None = None, build_if_missing: bool = False) -> GpuLibrary:
     """Load libsbfs_gb300.so (built in-tree by :func:`build_library`)."""

@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsbfs_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["sbfs_kernels.cu", "sbfs_api.cu", "sbfs_noalloc.cu"]
+CUDA_SOURCES = ["sbfs_kernels.cu", "sbfs_api.cu", "sbfs_noalloc.cu", "sbfs_mlp.cu"]
 CXX_SOURCES = ["sbfs_npyio.cpp"]
 
 

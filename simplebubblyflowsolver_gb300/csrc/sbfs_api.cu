@@ -82,6 +82,9 @@ struct Ctx {
   int iu = 0, ipsi = 0, iden = 0, isrc = 0;
   bool resident = false;  // device holds the current state
   std::map<int, cudaGraphExec_t> graphs;
+  // kernel arguments the graphs were captured with (physics, fixed dt, dt
+  // safety factor); graphs are dropped when any of them changes
+  std::vector<double> graph_sig;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   // diagnostics partials / result and statistics sums (allocated on first use)
   double *diag_part = nullptr, *diag_out = nullptr;
@@ -454,11 +457,15 @@ struct Prof {
 
 enum KernelClass {
   KC_PROPS, KC_CURV_LIST, KC_INTERFACE, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_STRESS, KC_PREDICT,
-  KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_COUNT
+  KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_MLP_CURV, KC_COUNT
 };
 const char *kKernelNames[KC_COUNT] = {"k_props", "k_curv_list", "k_interface_cells", "k_flux_force", "k_vof_advance", "k_stress",
                                       "k_predict", "k_poisson_fwd", "k_poisson_tdm", "k_poisson_inv", "k_correct",
-                                      "k_decide_dt"};
+                                      "k_decide_dt", "k_mlp_curv"};
+
+// curvature model of the fused step: 0 = the reference's kappa = -div n,
+// 1 = the learned closure in interface cells (plain kappa outside its range)
+int g_curv_model = 0;
 
 template <class F>
 void timed(Ctx &c, int cls, F &&launch) {
@@ -485,8 +492,10 @@ void enqueue_substage(Ctx &c, int k) {
   const double *sc = b.scalars;
   timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
+  if (g_curv_model) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
   timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
-  timed(c, KC_FLUX_FORCE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 2); });
+  timed(c, KC_FLUX_FORCE,
+        [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, g_curv_model ? 3 : 2); });
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
   timed(c, KC_PREDICT, [&] {
@@ -510,13 +519,25 @@ void enqueue_step(Ctx &c) {
   for (int k = 0; k < 3; ++k) enqueue_substage(c, k);
 }
 
-int role_key(const Ctx &c) { return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3); }
+int role_key(const Ctx &c) { return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4); }
 
 int launch_step(Ctx &c) {
   if (!g_use_graphs || g_prof.on) {
     enqueue_step(c);
     CK(cudaGetLastError());
     return 0;
+  }
+  {
+    const Phys &p = c.ph;
+    const std::vector<double> sig = {p.denr, p.visr,   p.refden,   p.den_lo,   p.den_hi,   p.vis_lo,
+                                     p.vis_hi, p.grav, p.force_coef, p.irefden, p.nu,      c.dt_fixed,
+                                     g_coef[0], g_coef[1], g_coef[2]};
+    if (sig.size() != c.graph_sig.size() ||
+        memcmp(sig.data(), c.graph_sig.data(), sizeof(double) * sig.size()) != 0) {
+      for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
+      c.graphs.clear();
+      c.graph_sig = sig;
+    }
   }
   const int key = role_key(c);
   auto it = c.graphs.find(key);
@@ -633,7 +654,14 @@ int sbfs_invalidate_device(void) {
   return 0;
 }
 
-int sbfs_kernels_per_step(void) { return kKernelsPerStep; }
+int sbfs_kernels_per_step(void) { return kKernelsPerStep + (g_curv_model ? 3 : 0); }
+
+int sbfs_set_curvature_model(int model) {
+  if (model != 0 && model != 1) return fail("bad curvature model %d", model);
+  if (model == 1 && !mlp_ready()) return fail("learned curvature selected before its parameters were set");
+  g_curv_model = model;
+  return 0;
+}
 
 // the state the device holds, uploaded first when the host is the truth
 static Ctx *diag_ctx(const domain_t *d, fluid_t *f, interface_t *itf) {

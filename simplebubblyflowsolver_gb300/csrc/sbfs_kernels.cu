@@ -157,7 +157,16 @@ __device__ __forceinline__ double thinc_face(double na, double nb, double K, dou
 // reference's intercept d (then K = exp(-2 d)).
 // thread (I, J): I = 1..nx handles x face I (I >= 2) and y face (I, J - 1/2)
 // ---------------------------------------------------------------------------
-template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY = false>
+// ITF_KAPPA (learned curvature mode): the face curvature comes from the
+// interface side alone when only one of the two cells is an interface cell
+// (the -div n of a single-phase cell next to the interface is not a
+// curvature of anything); otherwise the mean, as in the reference.
+__device__ __forceinline__ double face_kappa_sum(double pl, double pr, double kl, double kr) {
+  const bool il = !single_phase(pl), ir = !single_phase(pr);
+  return il == ir ? kl + kr : (il ? 2. * kl : 2. * kr);
+}
+
+template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY = false, bool ITF_KAPPA = false>
 __global__ void __launch_bounds__(BX *BY)
     k_flux_force(Grid g, Metrics m, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
                  const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
@@ -213,7 +222,8 @@ __global__ void __launch_bounds__(BX *BY)
       double f = 0.;
       if (!same(vxm, v0)) {
         const double rho = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];
-        const double kap = curv[ix(g, r, I - 1)] + curv[ix(g, r, I)];
+        const double kap = ITF_KAPPA ? face_kappa_sum(vxm, v0, curv[ix(g, r, I - 1)], curv[ix(g, r, I)])
+                                     : curv[ix(g, r, I - 1)] + curv[ix(g, r, I)];
         f = (rho * kap) * ((0.25 * ph.force_coef * m.ihxxf[I]) * (v0 - vxm));
       }
       ifrcx[ix(g, r, I - 2)] = f;
@@ -221,7 +231,8 @@ __global__ void __launch_bounds__(BX *BY)
     double f = 0.;
     if (!same(vym, v0)) {
       const double rho = den0[ix(g, rm, I)] + den0[ix(g, r, I)];
-      const double kap = curv[ix(g, rm, I)] + curv[ix(g, r, I)];
+      const double kap = ITF_KAPPA ? face_kappa_sum(vym, v0, curv[ix(g, rm, I)], curv[ix(g, r, I)])
+                                   : curv[ix(g, rm, I)] + curv[ix(g, r, I)];
       f = (rho * kap) * ((0.25 * ph.force_coef * g.ihy) * (v0 - vym));
     }
     ifrcy[ix(g, r, I - 1)] = f;
@@ -1199,9 +1210,12 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
     k_curv_list<<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.curv, b.ilist, b.icount);
   } else if (stage == 1) {
     k_interface_cells<<<4 * 152, 256, 0, s>>>(g, m, ux, uy, b.vof, b.dvof, b.ilist, b.icount, b.fluxx, b.fluxy);
-  } else {
+  } else if (stage == 2) {
     k_flux_force<true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                            b.fluxy, b.ifrcx, b.ifrcy);
+  } else {
+    k_flux_force<true, true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv,
+                                                                 b.fluxx, b.fluxy, b.ifrcx, b.ifrcy);
   }
 }
 

@@ -42,7 +42,8 @@ void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const B
 void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                        const double *ux, const double *uy, const double *den0, bool flux, bool force, bool have_k);
 // fused interface stage: 0 = curvature + interface-cell list, 1 = dense THINC
-// fluxes of the listed cells, 2 = bulk fluxes and the CSF force
+// fluxes of the listed cells, 2 = bulk fluxes and the CSF force, 3 = as 2
+// with the face curvature taken from the interface side (learned curvature)
 void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                             const double *ux, const double *uy, const double *den0, int stage);
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
@@ -93,5 +94,9 @@ cudaError_t configure_kernels();
 cudaError_t nr_check(const double *x, double *rcp, double *rsq, int n);
 // FP64 FMA throughput of this GPU, GFLOP/s (2 flops per FMA)
 cudaError_t measure_fp64_peak(double *gflops);
+// learned curvature closure (sbfs_mlp.cu): parameters present, and the
+// in-step kernel overwriting curv in the listed interface cells
+bool mlp_ready();
+void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b);
 
 }  // namespace sbfs

@@ -31,13 +31,13 @@ def _chord_integral(u0, u1, r):
 
 def disc_cell_fraction(x0, x1, y0, y1, xc, yc, r):
     """Exact area of disc((xc, yc), r) inside [x0,x1]x[y0,y1], divided by the
-    cell area.  Arguments broadcast (numpy arrays of cell edges)."""
-    x0, x1, y0, y1 = np.broadcast_arrays(*(np.asarray(a, dtype=np.float64) for a in (x0, x1, y0, y1)))
+    cell area.  All arguments broadcast elementwise (numpy arrays)."""
+    x0, x1, y0, y1, xc, yc, r = np.broadcast_arrays(
+        *(np.asarray(a, dtype=np.float64) for a in (x0, x1, y0, y1, xc, yc, r)))
     shape = x0.shape
-    x0, x1, y0, y1 = (a.ravel() for a in (x0, x1, y0, y1))
-    n = x0.size
+    x0, x1, y0, y1, xc, yc, r = (a.ravel() for a in (x0, x1, y0, y1, xc, yc, r))
     # candidate breakpoints in x, relative to the centre
-    bps = [x0 - xc, x1 - xc, np.full(n, -r), np.full(n, r)]
+    bps = [x0 - xc, x1 - xc, -r, r]
     for yy in (y0, y1):
         dy = yy - yc
         inside = np.abs(dy) < r
@@ -49,20 +49,20 @@ def disc_cell_fraction(x0, x1, y0, y1, xc, yc, r):
     hi = (x1 - xc)[:, None]
     B = np.clip(B, lo, hi)
     B.sort(axis=1)
-    area = np.zeros(n)
     ylo = (y0 - yc)[:, None]
     yhi = (y1 - yc)[:, None]
+    rr = r[:, None]
     a, b = B[:, :-1], B[:, 1:]
     m = 0.5 * (a + b)
-    s = np.sqrt(np.maximum(r * r - m * m, 0.0))
+    s = np.sqrt(np.maximum(rr * rr - m * m, 0.0))
     top_is_chord = s < yhi          # top boundary is the circle on this piece
     bot_is_chord = -s > ylo
     width = b - a
-    chord = _chord_integral(a, b, r)
+    chord = _chord_integral(a, b, rr)
     top = np.where(top_is_chord, chord, yhi * width)
     bot = np.where(bot_is_chord, -chord, ylo * width)
     piece = top - bot
-    valid = (np.abs(m) < r) & (np.minimum(yhi, s) > np.maximum(ylo, -s)) & (width > 0)
+    valid = (np.abs(m) < rr) & (np.minimum(yhi, s) > np.maximum(ylo, -s)) & (width > 0)
     area = np.where(valid, piece, 0.0).sum(axis=1)
     cell = (x1 - x0) * (y1 - y0)
     return np.clip(area / cell, 0.0, 1.0).reshape(shape)

@@ -1,0 +1,497 @@
+"""Learned curvature closure: training data, a CPU reference network, and
+the GPU training / evaluation driver.
+
+The closure replaces the curvature of the reference's CSF model (kappa =
+-div n, src/interface/curvature_tensor.c:100-135) in interface cells by a small
+multilayer perceptron evaluated with BF16 tensor-core MMA (FP32 accumulate):
+
+    features (16, 11 used) -> 64 -> ReLU -> 64 -> ReLU -> 1 = kappa * dx
+
+The features are the 3x3 VOF stencil around the cell (row-major, y rows,
+x fastest) and the cell normal the solver itself forms from the stencil
+(the sum of the four unit corner gradients, normalised; curvature_tensor.c:
+16-97), so the network sees exactly what the solver has.  Square cells are
+assumed (dx = dy).  vof = 1 marks the inside of a bubble or drop; a circle of
+radius R (in cells) then has kappa dx = +1/R.
+
+Training set (defaults), each part with the 8 rotations / reflections of
+every stencil and half of it inverted (1 - vof, label -1/R):
+  * 2e5 circles, R ~ U[2, 50] cells, centre offset ~ U[0, 1)^2 cells, one
+    interface cell per circle at a random angle, exact cell-area VOF
+    (ic.disc_cell_fraction);
+  * as many stencils of circles translated by the solver itself
+    (advected_circle_stencils): THINC (beta = 1) fluxes turn the sharp
+    exact-area profile into a diffuse one within a few cells of travel, and
+    a network that has only seen the sharp profile fails on it;
+  * up to as many stencils of static drops held by their exact curvature
+    (relaxed_drop_stencils): the states a good closure meets in the step.
+Training: Adam, batch 1024, cosine learning rate 2e-3 -> 2e-5, 40 epochs,
+on the GPU (k_mlp_grad / k_mlp_adam of sbfs_mlp.cu).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import ic
+
+NFEAT = 16   # 11 used, padded for the k = 16 MMA
+NHID = 64
+NPARAM = NHID * NFEAT + NHID + NHID * NHID + NHID + NHID + 1  # W1, b1, W2, b2, w3, b3
+
+
+def stencil_normal(st: np.ndarray) -> np.ndarray:
+    """cell normal of the centre cell of 3x3 stencils st[..., 3, 3] (y, x):
+    unit corner gradients (curvature_tensor.c:16-49) summed over the four
+    corners and normalised (curvature_tensor.c:51-97), dx = dy."""
+    eps = np.finfo(np.float64).eps
+    out = np.zeros(st.shape[:-2] + (2,))
+    for cy in (0, 1):          # corner rows between stencil rows cy and cy+1
+        for cx in (0, 1):
+            a = st[..., cy, cx]
+            b = st[..., cy, cx + 1]
+            c = st[..., cy + 1, cx]
+            d = st[..., cy + 1, cx + 1]
+            gx = ((-a + b) - c) + d
+            gy = ((-a - b) + c) + d
+            inv = 1.0 / np.maximum(np.sqrt(gx * gx + gy * gy), eps)
+            out[..., 0] += gx * inv
+            out[..., 1] += gy * inv
+    inv = 1.0 / np.maximum(np.hypot(out[..., 0], out[..., 1]), eps)
+    return out * inv[..., None]
+
+
+def features(st: np.ndarray) -> np.ndarray:
+    """(n, 16) float32 feature rows from (n, 3, 3) stencils"""
+    n = st.shape[0]
+    f = np.zeros((n, NFEAT), dtype=np.float32)
+    f[:, :9] = st.reshape(n, 9)
+    f[:, 9:11] = stencil_normal(st)
+    return f
+
+
+def symmetries(st: np.ndarray) -> np.ndarray:
+    """the 8 rotations / reflections of (n, 3, 3) stencils -> (8 n, 3, 3)"""
+    out = []
+    for flip in (False, True):
+        s = st[:, :, ::-1] if flip else st
+        for k in range(4):
+            out.append(np.rot90(s, k, axes=(1, 2)))
+    return np.concatenate(out, axis=0)
+
+
+def circle_stencils(n: int, rmin=2.0, rmax=50.0, seed=0, invert_fraction=0.5):
+    """(stencils (n, 3, 3), labels kappa dx (n,), radii (n,)) for n circles"""
+    rng = np.random.default_rng(seed)
+    R = rng.uniform(rmin, rmax, n)
+    c = rng.uniform(0.0, 1.0, (n, 2))
+    th = rng.uniform(0.0, 2.0 * math.pi, n)
+    px = c[:, 0] + R * np.cos(th)
+    py = c[:, 1] + R * np.sin(th)
+    ci = np.floor(px)
+    cj = np.floor(py)
+    st = np.zeros((n, 3, 3))
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            x0 = ci + dx
+            y0 = cj + dy
+            st[:, dy + 1, dx + 1] = ic.disc_cell_fraction(x0, x0 + 1.0, y0, y0 + 1.0, c[:, 0], c[:, 1], R)
+    lab = 1.0 / R
+    inv = rng.uniform(0.0, 1.0, n) < invert_fraction
+    st[inv] = 1.0 - st[inv]
+    lab = np.where(inv, -lab, lab)
+    # keep stencils whose centre is a genuine interface cell
+    keep = (st[:, 1, 1] > 1e-8) & (st[:, 1, 1] < 1 - 1e-8)
+    return st[keep], lab[keep], R[keep]
+
+
+def dataset(ncircles=200000, seed=0):
+    """(features (8 m, 16) float32, labels (8 m,) float32) with symmetries"""
+    st, lab, _ = circle_stencils(ncircles, seed=seed)
+    st8 = symmetries(st)
+    lab8 = np.tile(lab, 8)
+    return features(st8), lab8.astype(np.float32)
+
+
+def advected_circle_stencils(backend, n=512, nfields=1, steps=160, sample_every=20, rmin=2.0, rmax=50.0,
+                             seed=0, courant=(0.05, 0.2, 0.4), log=None):
+    """(stencils, labels, radii) of circles as the solver itself carries them.
+
+    The vof that the time step produces is not the exact cell area of the
+    initial condition: THINC fluxes (beta = 1) turn a sharp profile into a
+    diffuse one within a few cells of travel.  To train on what the closure
+    will see, circles (log-uniform R, so every R contributes about equally
+    many interface cells) are placed without overlap in an n x n box and
+    translated by a uniform vertical velocity (no surface tension, no gravity,
+    matched densities: a translated circle keeps its curvature 1/R exactly),
+    and the interface stencils are sampled every `sample_every` steps,
+    including step 0.  `backend` is anything with the reference's integrate
+    (the GPU library or the oracle).  Stencils are labelled by the circle
+    whose travelled centre is nearest; half of them are inverted.
+    """
+    from .binding import state_from_fields
+    rng = np.random.default_rng(seed)
+    out_st, out_lab, out_R = [], [], []
+    gpu = hasattr(backend, "set_sync_mode")
+    for fi in range(nfields):
+        # non-overlapping discs, clear of the walls (boundary layers)
+        discs = []
+        tries = 0
+        while tries < 20000:
+            tries += 1
+            R = math.exp(rng.uniform(math.log(rmin), math.log(rmax)))
+            x = rng.uniform(R + 24, n - R - 24)
+            y = rng.uniform(0, n)
+            ok = True
+            for (x2, y2, R2) in discs:
+                dy = abs(y - y2)
+                dy = min(dy, n - dy)
+                if math.hypot(x - x2, dy) < R + R2 + 8:
+                    ok = False
+                    break
+            if ok:
+                discs.append((x, y, R))
+        V = 1.0 if rng.uniform() < 0.5 else -1.0
+        cfl = courant[fi % len(courant)]
+        wl = ic.Workload("advected_circles", n, n, 1.0, 1.0, [(x / n, y / n, R / n) for x, y, R in discs],
+                         Re=1e6, We=1e30, Fr=math.inf, denr=1.0, visr=1.0, coef_dt_adv=cfl)
+        f = wl.fields()
+        f["uy"][...] = V
+        import os
+        for k, v in wl.env().items():
+            os.environ[k] = v
+        backend.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+        st = state_from_fields(f, Re=wl.Re, We=wl.We, Fr=wl.Fr, denr=wl.denr, visr=wl.visr)
+        backend.apply_initial_boundaries(st)
+        if gpu:
+            from . import SYNC_NONE
+            backend.set_sync_mode(SYNC_NONE)
+        t = 0.0
+        try:
+            for s in range(steps + 1):
+                if s % sample_every == 0:
+                    if gpu and s > 0:
+                        backend.sync_to_host(st)
+                    stn, rr, cc = interface_stencils(st.interior_rows("vof"))
+                    keep = (stn[:, 1, 1] >= 0.01) & (stn[:, 1, 1] <= 0.99)
+                    stn, rr, cc = stn[keep], rr[keep], cc[keep]
+                    X = cc + 0.5
+                    Y = rr + 0.5
+                    dmin = np.full(X.size, np.inf)
+                    lab = np.zeros(X.size)
+                    for (x, y, R) in discs:
+                        yc = (y + V * t * n) % n
+                        dy = np.abs(Y - yc)
+                        dy = np.minimum(dy, n - dy)
+                        d = np.abs(np.hypot(X - x, dy) - R)
+                        closer = d < dmin
+                        dmin = np.where(closer, d, dmin)
+                        lab = np.where(closer, R, lab)
+                    good = dmin < 3.0
+                    out_st.append(stn[good])
+                    out_R.append(lab[good])
+                if s < steps:
+                    t += backend.integrate(st)
+        finally:
+            if gpu:
+                from . import SYNC_STATE
+                backend.set_sync_mode(SYNC_STATE)
+        if log:
+            log(f"field {fi}: {len(discs)} circles, courant {cfl}, travelled {abs(V) * t * n:.1f} cells")
+    st = np.concatenate(out_st)
+    R = np.concatenate(out_R)
+    lab = 1.0 / R
+    inv = rng.uniform(0.0, 1.0, st.shape[0]) < 0.5
+    st[inv] = 1.0 - st[inv]
+    lab = np.where(inv, -lab, lab)
+    return st, lab, R
+
+
+def relaxed_drop_stencils(lib, radii, steps=400, sample_every=50, seed=0):
+    """(stencils, labels, radii) of static drops (density ratio 1e-3, the
+    static-drop physics) held by their exact curvature: the closure is set to
+    a constant network output kappa dx = 1/R, so the interface relaxes the
+    way it does under an ideal curvature model and stays a circle of radius
+    R to within the parasitic motion.  These are the stencils a good closure
+    meets inside the time step.  Needs the GPU library."""
+    from . import SYNC_NONE, SYNC_STATE
+    from .binding import state_from_fields
+    import os
+    rng = np.random.default_rng(seed)
+    out_st, out_R = [], []
+    for R in radii:
+        n = 64
+        while R > 0.3 * n:
+            n *= 2
+        n = max(n, 64)
+        off = rng.uniform(-0.5, 0.5, 2) / n
+        wl = ic.Workload("relaxed_drop", n, n, 1.0, 1.0, [(0.5 + off[0], 0.5 + off[1], R / n)], Re=math.sqrt(12000.0),
+                         We=1.0, Fr=math.inf, denr=1e-3, visr=1e-3)
+        for k, v in wl.env().items():
+            os.environ[k] = v
+        lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+        const = np.zeros(NPARAM, dtype=np.float32)
+        const[-1] = 1.0 / R
+        lib.mlp_set_params(const)
+        lib.set_curvature_model(1)
+        st = state_from_fields(wl.fields(), Re=wl.Re, We=wl.We, Fr=wl.Fr, denr=wl.denr, visr=wl.visr)
+        lib.apply_initial_boundaries(st)
+        lib.set_sync_mode(SYNC_NONE)
+        try:
+            for s in range(1, steps + 1):
+                lib.integrate(st)
+                if s % sample_every == 0:
+                    lib.sync_to_host(st)
+                    stn, rr, cc = interface_stencils(st.interior_rows("vof"))
+                    # interface cells of the drop itself (not debris): within
+                    # 2 cells of the initial circle
+                    d = np.hypot(cc + 0.5 - (0.5 + off[0]) * n, rr + 0.5 - (0.5 + off[1]) * n)
+                    keep = (stn[:, 1, 1] >= 0.01) & (stn[:, 1, 1] <= 0.99) & (np.abs(d - R) < 2.0)
+                    out_st.append(stn[keep])
+                    out_R.append(np.full(int(keep.sum()), R))
+        finally:
+            lib.set_sync_mode(SYNC_STATE)
+            lib.set_curvature_model(0)
+    st = np.concatenate(out_st)
+    R = np.concatenate(out_R)
+    lab = 1.0 / R
+    inv = rng.uniform(0.0, 1.0, st.shape[0]) < 0.5
+    st[inv] = 1.0 - st[inv]
+    lab = np.where(inv, -lab, lab)
+    return st, lab, R
+
+
+# ---------------------------------------------------------------- parameters
+def init_params(seed=0) -> np.ndarray:
+    """He-initialised flat FP32 parameter vector [W1 (64x16), b1, W2 (64x64),
+    b2, w3 (64), b3]"""
+    rng = np.random.default_rng(seed)
+    W1 = rng.standard_normal((NHID, NFEAT)) * math.sqrt(2.0 / 11)
+    W1[:, 11:] = 0.0
+    W2 = rng.standard_normal((NHID, NHID)) * math.sqrt(2.0 / NHID)
+    w3 = rng.standard_normal(NHID) * math.sqrt(1.0 / NHID)
+    return np.concatenate([W1.ravel(), np.zeros(NHID), W2.ravel(), np.zeros(NHID), w3, [0.0]]).astype(np.float32)
+
+
+def unpack(p):
+    i = 0
+    W1 = p[i:i + NHID * NFEAT].reshape(NHID, NFEAT); i += NHID * NFEAT
+    b1 = p[i:i + NHID]; i += NHID
+    W2 = p[i:i + NHID * NHID].reshape(NHID, NHID); i += NHID * NHID
+    b2 = p[i:i + NHID]; i += NHID
+    w3 = p[i:i + NHID]; i += NHID
+    b3 = p[i]
+    return W1, b1, W2, b2, w3, b3
+
+
+def bf16(x: np.ndarray) -> np.ndarray:
+    """round to the nearest bfloat16 (ties to even), returned as float64"""
+    a = np.ascontiguousarray(x, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def reference_forward_backward(p, X, y, quantise=True):
+    """FP64 CPU network with the GPU's precision steps (BF16 weights,
+    activations and gradients fed to the matrix products when `quantise`):
+    returns (predictions, mean-square loss, gradient of the loss)"""
+    W1, b1, W2, b2, w3, b3 = (np.asarray(a, dtype=np.float64) for a in unpack(p))
+    q = bf16 if quantise else (lambda a: np.asarray(a, dtype=np.float64))
+    Xq = q(X)
+    z1 = Xq @ q(W1).T + b1
+    h1 = np.maximum(z1, 0.0)
+    z2 = q(h1) @ q(W2).T + b2
+    h2 = np.maximum(z2, 0.0)
+    out = h2 @ w3 + b3
+    n = X.shape[0]
+    r = out - y
+    loss = float(np.mean(r * r))
+    dout = 2.0 * r / n
+    gw3 = h2.T @ dout
+    gb3 = dout.sum()
+    dz2 = np.outer(dout, w3) * (z2 > 0)
+    gW2 = q(dz2).T @ q(h1)
+    gb2 = dz2.sum(0)
+    dz1 = (q(dz2) @ q(W2)) * (z1 > 0)
+    gW1 = q(dz1).T @ Xq
+    gb1 = dz1.sum(0)
+    g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gw3, [gb3]])
+    return out, loss, g
+
+
+# ------------------------------------------------------------- GPU training
+class GpuCurvatureModel:
+    """Training and evaluation of the closure with the library's BF16 MMA
+    kernels.  Device buffers are torch tensors (memory only; every
+    computation is a kernel of libsbfs_gb300)."""
+
+    def __init__(self, lib, X: np.ndarray, Y: np.ndarray, device="cuda:0"):
+        import torch
+        self.torch = torch
+        self.lib = lib
+        self.device = device
+        self.X = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).to(device).to(torch.bfloat16)
+        self.Y = torch.from_numpy(np.ascontiguousarray(Y, dtype=np.float32)).to(device)
+        self.n = X.shape[0]
+        self._params = None
+
+    def set_params(self, p):
+        self.lib.mlp_set_params(p)
+        self._params = np.array(p, dtype=np.float32)
+
+    def params(self) -> np.ndarray:
+        """the parameters of this model (the library holds one parameter set
+        at a time; fetched after training)"""
+        return self._params.copy()
+
+    def gradient(self, rows: np.ndarray):
+        self.lib.mlp_set_params(self._params)
+        idx = self.torch.from_numpy(np.ascontiguousarray(rows, dtype=np.int32)).to(self.device)
+        return self.lib.mlp_gradient(self.X.data_ptr(), self.Y.data_ptr(), idx.data_ptr(), idx.numel())
+
+    def train(self, epochs=30, batch=1024, lr=2e-3, lr_min=2e-5, seed=0, log=None):
+        """Adam with a cosine learning-rate decay, one shuffle per epoch;
+        returns the mean training loss of each epoch"""
+        torch = self.torch
+        gen = torch.Generator(device="cpu").manual_seed(seed)
+        self.lib.mlp_set_params(self._params)  # this model's start point, fresh Adam moments
+        hist = []
+        for e in range(epochs):
+            perm = torch.randperm(self.n, generator=gen).to(torch.int32).to(self.device)
+            rate = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * e / max(epochs - 1, 1)))
+            loss = self.lib.mlp_train_epoch(self.X.data_ptr(), self.Y.data_ptr(), perm.data_ptr(), self.n,
+                                            batch, rate)
+            hist.append(loss)
+            if log:
+                log(f"epoch {e:3d} lr {rate:.2e} loss {loss:.3e}")
+        self._params = self.lib.mlp_get_params()
+        return hist
+
+    def predict(self, X: np.ndarray) -> np.ndarray:
+        torch = self.torch
+        Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).to(self.device).to(torch.bfloat16)
+        out = torch.empty(X.shape[0], dtype=torch.float32, device=self.device)
+        self.lib.mlp_set_params(self._params)
+        self.lib.mlp_predict(Xd.data_ptr(), X.shape[0], out.data_ptr())
+        return out.cpu().numpy()
+
+
+def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfields=2, seed=0, log=None):
+    """(features, labels) with the 8 symmetries: the exact-area circles and,
+    run on `lib`, up to as many stencils of circles carried by the solver
+    (`advected`) and of drops relaxed under their exact curvature (`relaxed`)"""
+    st, lab, _ = circle_stencils(ncircles, seed=seed)
+    parts_st, parts_lab = [st], [lab]
+    rng = np.random.default_rng(seed + 2)
+    if advected:
+        sa, la, _ = advected_circle_stencils(lib, n=n, nfields=nfields, steps=160, sample_every=40, seed=seed + 1,
+                                             log=log)
+        pick = rng.choice(sa.shape[0], min(sa.shape[0], st.shape[0]), replace=False)
+        parts_st.append(sa[pick])
+        parts_lab.append(la[pick])
+    if relaxed:
+        radii = np.exp(rng.uniform(math.log(2.0), math.log(50.0), 48))
+        sr, lr, _ = relaxed_drop_stencils(lib, radii, seed=seed + 3)
+        pick = rng.choice(sr.shape[0], min(sr.shape[0], st.shape[0]), replace=False)
+        parts_st.append(sr[pick])
+        parts_lab.append(lr[pick])
+        if log:
+            log(f"relaxed drops: {sr.shape[0]} stencils")
+    st = np.concatenate(parts_st)
+    lab = np.concatenate(parts_lab)
+    return features(symmetries(st)), np.tile(lab, 8).astype(np.float32)
+
+
+def train_default(lib, ncircles=200000, epochs=40, seed=0, advected=True, relaxed=True, log=None):
+    """train the closure on the default data set on the GPU; returns
+    (model, parameters, loss history)"""
+    X, Y = training_set(lib, ncircles, advected=advected, relaxed=relaxed, seed=seed, log=log)
+    m = GpuCurvatureModel(lib, X, Y)
+    m.set_params(init_params(seed))
+    hist = m.train(epochs=epochs, seed=seed, log=log)
+    return m, m.params(), hist
+
+
+# ------------------------------------------------------------- evaluation
+def plain_curvature(st: np.ndarray) -> np.ndarray:
+    """kappa dx of the reference's CSF curvature -div n on (n, 3, 3) stencils
+    (curvature_tensor.c:100-135 with the unit corner normals of :16-49), dx = dy"""
+    eps = np.finfo(np.float64).eps
+    nrm = {}
+    for cy in (0, 1):
+        for cx in (0, 1):
+            a, b = st[..., cy, cx], st[..., cy, cx + 1]
+            c, d = st[..., cy + 1, cx], st[..., cy + 1, cx + 1]
+            gx = ((-a + b) - c) + d
+            gy = ((-a - b) + c) + d
+            inv = 1.0 / np.maximum(np.sqrt(gx * gx + gy * gy), eps)
+            nrm[cy, cx] = (gx * inv, gy * inv)
+    ddx = (nrm[0, 1][0] + nrm[1, 1][0]) - (nrm[0, 0][0] + nrm[1, 0][0])
+    ddy = (nrm[1, 0][1] + nrm[1, 1][1]) - (nrm[0, 0][1] + nrm[0, 1][1])
+    return -(0.5 * ddx + 0.5 * ddy)
+
+
+def interface_stencils(vof_rows: np.ndarray, vofmin=1e-8):
+    """(stencils (m, 3, 3), (row, column) of each) of the interface cells of a
+    vof field given as device-order rows (ny, nx + 2) with x ghost columns;
+    y periodic"""
+    ny, w = vof_rows.shape
+    nx = w - 2
+    inner = vof_rows[:, 1:nx + 1]
+    rr, cc = np.nonzero((inner > vofmin) & (inner < 1 - vofmin))
+    st = np.empty((rr.size, 3, 3))
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            st[:, dy + 1, dx + 1] = vof_rows[(rr + dy) % ny, cc + 1 + dx]
+    return st, rr, cc
+
+
+def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_every=0):
+    """Run the static drop (r = 0.25 in the unit box, density ratio 1e-3,
+    La = 12000) for `steps` steps with curvature model 0 (-div n) or 1 (the
+    learned closure with `params`) and measure the parasitic currents and
+    the Laplace pressure jump (exact: kappa / We = 4)."""
+    import os
+
+    from . import SYNC_NONE, SYNC_STATE
+    from .binding import state_from_fields
+    wl = ic.static_drop(n, steps)
+    for k, v in wl.env().items():
+        os.environ[k] = v
+    lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    if params is not None:
+        lib.mlp_set_params(params)
+    lib.set_curvature_model(model)
+    try:
+        st = state_from_fields(wl.fields(), Re=wl.Re, We=wl.We, Fr=wl.Fr, denr=wl.denr, visr=wl.visr)
+        lib.apply_initial_boundaries(st)
+        lib.mlp_take_usage() if model else None
+        lib.set_sync_mode(SYNC_NONE)
+        t = 0.0
+        hist = []
+        for s in range(steps):
+            t += lib.integrate(st)
+            if record_every and (s + 1) % record_every == 0:
+                dg = lib.diagnostics(st)
+                hist.append((s + 1, t, max(dg["umax"], dg["vmax"])))
+        lib.sync_to_host(st)
+        used = lib.mlp_take_usage() if model else 0
+    finally:
+        lib.set_sync_mode(SYNC_STATE)
+        lib.set_curvature_model(0)
+    ux, uy = st.interior_rows("ux"), st.interior_rows("uy")
+    p, vof = st.interior_rows("p")[:, 1:-1], st.interior_rows("vof")[:, 1:-1]
+    xc = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(xc, xc)
+    d = np.hypot(X - 0.5, Y - 0.5)
+    p_in = p[(vof > 1 - 1e-6) & (d < 0.15)].mean()
+    p_out = p[(vof < 1e-6) & (d > 0.35)].mean()
+    exact = 1.0 / (wl.We * 0.25)
+    umax = max(float(np.abs(ux).max()), float(np.abs(uy).max()))
+    st_i, _, _ = interface_stencils(st.interior_rows("vof"))
+    return {"n": n, "steps": steps, "time": t, "umax": umax, "capillary_number": umax * wl.We / wl.Re,
+            "dp": float(p_in - p_out), "dp_rel_err": float(abs(p_in - p_out - exact) / exact),
+            "learned_cells_per_step": used / (3.0 * steps) if model else 0.0,
+            "interface_cells": int(st_i.shape[0]), "umax_history": hist}

@@ -129,3 +129,25 @@ def test_matches_reference_fixtures(libs):
             err = np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
             print(name, s, f"{err:.2e}", "tol", tol)
             assert err <= tol, (name, s, err, tol)
+
+
+def test_graphs_follow_physics_changes(libs):
+    """captured step graphs hold the physics and dt factors as kernel
+    arguments: a second case on the same grid with other physics must not
+    replay the first case's graphs"""
+    import dataclasses
+    gpu, orc = libs
+    a = ic.single_bubble(128, 64)
+    b = dataclasses.replace(a, Re=a.Re * 0.5, We=a.We * 2.0, denr=0.05, visr=0.2, coef_dt_adv=0.2)
+    st_a = prepare(libs, a)
+    sg = clone(st_a)
+    for _ in range(2):
+        gpu.integrate(sg)
+    st_b = prepare(libs, b)
+    sg, so = clone(st_b), clone(st_b)
+    for _ in range(3):
+        dg = gpu.integrate(sg)
+        do = orc.integrate(so)
+        assert abs(dg - do) <= 1e-12 * do
+    errs = compare_state(sg, so)
+    assert max(errs.values()) <= 1e-10, errs
