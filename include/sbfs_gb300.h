@@ -182,6 +182,26 @@ int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, const double *u
                            double coef_dif, double coef_int, double *scalars, int *status, void *stream);
 const char *sbfs_noalloc_last_error(void);
 
+/* ---- batches of independent cases (no reference counterpart) ----
+ * integrate() for n cases at once, each described by the reference's own
+ * structs (any mix of grids and physics; every case steps with its own dt,
+ * returned in dts[i]).  Cases on the same grid form a group whose fields hold
+ * the cases side by side; each kernel of the step runs all cases of a group
+ * in one launch, and groups run on separate streams.  The sync mode applies
+ * as for integrate(); in SBFS_SYNC_NONE the cases stay on the device between
+ * calls as long as the same fluid/interface pointers are passed in the same
+ * order.  Learned curvature is not applied to batches. */
+int sbfs_integrate_batch(int n, const domain_t *const *domains, fluid_t *const *fluids,
+                         interface_t *const *interfaces, double *dts);
+/* advance the device-resident batch nsteps steps; *ms from CUDA events */
+int sbfs_run_batch_steps_timed(int nsteps, float *ms);
+/* copy the device-resident batch back into the callers' structs */
+int sbfs_batch_sync_to_host(int n, const domain_t *const *domains, fluid_t *const *fluids,
+                            interface_t *const *interfaces);
+/* number of grid groups and cases per group of the current batch */
+int sbfs_batch_groups(int *ngroups, int *cases_per_group);
+int sbfs_batch_release(void);
+
 /* ---- learned curvature closure (no reference counterpart) ----
  * A 16 -> 64 -> 64 -> 1 ReLU perceptron mapping the 3x3 vof stencil of an
  * interface cell and the cell normal to kappa * dx, evaluated with BF16

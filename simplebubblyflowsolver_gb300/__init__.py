@@ -159,6 +159,47 @@ class GpuLibrary(ReferenceAPI):
     def release(self):
         self._ext("sbfs_release")
 
+    # ---- batches of independent cases
+    def _batch_args(self, states):
+        n = len(states)
+        vp = C.c_void_p * n
+        d = vp(*[C.addressof(st.domain) for st in states])
+        f = vp(*[C.addressof(st.fluid) for st in states])
+        i = vp(*[C.addressof(st.interface) for st in states])
+        return n, d, f, i
+
+    def integrate_batch(self, states):
+        """one step of every case (each with its own dt); returns the dts"""
+        import numpy as np
+        n, d, f, i = self._batch_args(states)
+        dts = np.zeros(n)
+        self.lib.sbfs_integrate_batch.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                  C.POINTER(C.c_double)]
+        self._ext("sbfs_integrate_batch", n, d, f, i, dts.ctypes.data_as(C.POINTER(C.c_double)))
+        # the library swapped psi pointers inside the structs (SYNC_STATE/ALL)
+        return dts
+
+    def run_batch_steps_timed(self, nsteps: int) -> float:
+        ms = C.c_float(0.0)
+        self.lib.sbfs_run_batch_steps_timed.argtypes = [C.c_int, C.POINTER(C.c_float)]
+        self._ext("sbfs_run_batch_steps_timed", nsteps, C.byref(ms))
+        return ms.value
+
+    def batch_sync_to_host(self, states):
+        n, d, f, i = self._batch_args(states)
+        self.lib.sbfs_batch_sync_to_host.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        self._ext("sbfs_batch_sync_to_host", n, d, f, i)
+
+    def batch_groups(self):
+        ng = C.c_int(0)
+        cases = (C.c_int * 64)()
+        self.lib.sbfs_batch_groups.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        self._ext("sbfs_batch_groups", C.byref(ng), cases)
+        return list(cases[:ng.value])
+
+    def batch_release(self):
+        self._ext("sbfs_batch_release")
+
     # ---- learned curvature closure (device pointers are plain ints)
     def _mlp(self, fn, *args):
         rc = getattr(self.lib, fn)(*args)

@@ -63,6 +63,10 @@ const Layout L_CURV{1, 1, 1, 1, 1}, L_FLUXX{0, 1, 1, 1, 1}, L_FLUXY{1, 1, 1, 1, 
 
 struct Ctx {
   int nx = 0, ny = 0;
+  int nc = 1;     // cases on this grid (batches); every field holds nc case slabs
+  int kcase = 0;  // case slab that h2d / d2h address
+  Phys *phys_dev = nullptr;  // per-case physics (batches)
+  std::vector<Phys> phys_host;
   double lx = 0., ly = 0.;
   Grid g{};
   Metrics m{};
@@ -120,11 +124,17 @@ bool layout_ok(const array_t &a, const Layout &l) {
 
 int pitch_of(const Ctx &c, const Layout &l) { return l.nc == 1 ? c.g.p1 : (l.nc == 2 ? c.g.p2 : c.g.p3); }
 
+// start of case slab c.kcase of a device field
+size_t case_off(const Ctx &c, const Layout &l) {
+  return (size_t)c.kcase * (l.nc == 1 ? c.g.cs1 : (l.nc == 2 ? c.g.cs2 : c.g.cs3));
+}
+
 // host array (reference layout, rows J = 1 - ay0 .. ny + ay1) -> device rows J = 1..ny
 int h2d(Ctx &c, const array_t &a, const Layout &l, double *dev) {
   if (!layout_ok(a, l)) return fail("array layout does not match the reference's (nadds/size)");
   const size_t row = (size_t)(c.nx + l.ax0 + l.ax1) * l.nc;
   const double *src = static_cast<const double *>(a.data) + (size_t)l.ay0 * row;
+  dev += case_off(c, l);
   CK(cudaMemcpy2DAsync(dev, sizeof(double) * pitch_of(c, l), src, sizeof(double) * row, sizeof(double) * row, c.ny,
                        cudaMemcpyHostToDevice, c.s));
   return 0;
@@ -136,6 +146,7 @@ int d2h(Ctx &c, array_t &a, const Layout &l, const double *dev) {
   const size_t row = (size_t)(c.nx + l.ax0 + l.ax1) * l.nc;
   const size_t pitch = sizeof(double) * pitch_of(c, l);
   double *dst = static_cast<double *>(a.data);
+  dev += case_off(c, l);
   CK(cudaMemcpy2DAsync(dst + (size_t)l.ay0 * row, sizeof(double) * row, dev, pitch, sizeof(double) * row, c.ny,
                        cudaMemcpyDeviceToHost, c.s));
   for (int J = 1 - l.ay0; J <= c.ny + l.ay1; ++J) {
@@ -184,22 +195,27 @@ int check_domain(const domain_t *d) {
 }
 
 // per-column coefficients (see Metrics)
-int upload_metrics(Ctx &c, const domain_t *d, double Re) {
+// (batches: one block of 6 columns per case, Re[k] per case; the kernels
+// offset only nuf, the one column that depends on the case)
+int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   const int nx = c.nx, n = nx + 3;
   const double hy = d->hy;
-  const double nu = 1. / Re;
   const double dx = d->hxxc[0];
-  std::vector<double> h(6 * (size_t)n, 0.);
-  auto A = [&](int k, int I) -> double & { return h[(size_t)k * n + I]; };
-  for (int I = 1; I <= nx + 1; ++I) {
-    const double hf = d->hxxf[I - 1];
-    A(0, I) = 1. / hf;
-    A(2, I) = 0.25 / hf;
-    A(3, I) = 0.25 * dx / (hf * hy);
-    A(4, I) = nu / hf;
-    A(5, I) = hf;
+  std::vector<double> h(6 * (size_t)n * c.nc, 0.);
+  for (int k = 0; k < c.nc; ++k) {
+    const double nu = 1. / Re[k];
+    auto A = [&](int q, int I) -> double & { return h[((size_t)k * 6 + q) * n + I]; };
+    for (int I = 1; I <= nx + 1; ++I) {
+      const double hf = d->hxxf[I - 1];
+      A(0, I) = 1. / hf;
+      A(2, I) = 0.25 / hf;
+      A(3, I) = 0.25 * dx / (hf * hy);
+      A(4, I) = nu / hf;
+      A(5, I) = hf;
+    }
+    for (int I = 1; I <= nx; ++I) A(1, I) = 1. / d->hxxc[I - 1];
   }
-  for (int I = 1; I <= nx; ++I) A(1, I) = 1. / d->hxxc[I - 1];
+  c.g.cm = c.nc > 1 ? 6 * n : 0;
   if (!c.met) {
     if (dalloc(c, &c.met, h.size())) return 1;
   }
@@ -212,12 +228,12 @@ int upload_metrics(Ctx &c, const domain_t *d, double Re) {
   c.m.q4fy = b + 3 * n;
   c.m.nuf = b + 4 * n;
   c.m.hxxf = b + 5 * n;
-  c.Re = Re;
+  c.Re = Re[0];
   return 0;
 }
 
-void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
-  Phys &p = c.ph;
+Phys phys_of(const fluid_t *f, const interface_t *itf) {
+  Phys p{};
   p.denr = f->denr;
   p.visr = f->visr;
   p.refden = f->refden;
@@ -229,7 +245,10 @@ void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
   p.force_coef = itf ? 2. / (1. + f->denr) / itf->We : 0.;
   p.irefden = 1. / f->refden;
   p.nu = 1. / f->Re;
+  return p;
 }
+
+void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) { c.ph = phys_of(f, itf); }
 
 double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
   double hxmin = 1.79769313486231570e+308;
@@ -309,9 +328,9 @@ int upload_poisson(Ctx &c, const domain_t *d) {
   return 0;
 }
 
-int make_ctx(const domain_t *d) {
-  g_ctx.reset();
-  auto c = std::make_unique<Ctx>();
+// device context for nc cases on the grid of d
+int build_ctx(Ctx *c, const domain_t *d, int nc) {
+  c->nc = nc;
   c->nx = (int)d->mysizes[0];
   c->ny = (int)d->mysizes[1];
   c->lx = d->lengths[0];
@@ -334,33 +353,48 @@ int make_ctx(const domain_t *d) {
   g.dx = d->hxxc[0];
   g.idx = 1. / d->hxxc[0];
   const size_t n1 = (size_t)g.p1 * g.ny, n2 = (size_t)g.p2 * g.ny, n3 = (size_t)g.p3 * g.ny;
+  const int M1 = g.ny / 2 + 1;
+  g.nc = nc;
+  g.cs1 = n1;
+  g.cs2 = n2;
+  g.cs3 = n3;
+  g.css = (size_t)c->nx * M1;
+  g.cm = 0;
+  g.phys = nullptr;
   Bufs &b = c->b;
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
                      &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.irhox, &b.irhoy};
   for (double **p : scal)
-    if (dalloc(*c, p, n1)) return 1;
-  if (dalloc(*c, &b.dvof, n2)) return 1;
-  if (dalloc(*c, &b.normal, n3)) return 1;
-  const int M1 = g.ny / 2 + 1;
+    if (dalloc(*c, p, n1 * nc)) return 1;
+  if (dalloc(*c, &b.dvof, n2 * nc)) return 1;
+  if (dalloc(*c, &b.normal, n3 * nc)) return 1;
   double *tmp = nullptr;
-  if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1)) return 1;
+  if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1 * nc)) return 1;
   b.spec = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, 4 * (size_t)32 * tdm_chunk(c->nx) * M1)) return 1;
   b.tdm_fac = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, 2 * (size_t)M1)) return 1;
   b.twiddle = reinterpret_cast<double2 *>(tmp);
-  if (dalloc(*c, &tmp, (size_t)c->nx + 8)) return 1;
+  if (dalloc(*c, &tmp, ((size_t)c->nx + 8) * nc)) return 1;
   b.dt_acc = reinterpret_cast<unsigned long long *>(tmp);
-  if (dalloc(*c, &tmp, ((size_t)c->nx * c->ny + 2) / 2 + 1)) return 1;
+  if (dalloc(*c, &tmp, ((size_t)c->nx * c->ny * nc + 2) / 2 + 1)) return 1;
   b.ilist = reinterpret_cast<int *>(tmp);
-  if (dalloc(*c, &tmp, 1)) return 1;
+  if (dalloc(*c, &tmp, (size_t)nc / 2 + 1)) return 1;
   b.icount = reinterpret_cast<int *>(tmp);
-  if (dalloc(*c, &tmp, kScalars + 2)) return 1;
+  // scalars of every case, then one status word per case
+  if (dalloc(*c, &tmp, (size_t)kScalars * nc + nc / 2 + 2)) return 1;
   b.scalars = tmp;
-  b.status = reinterpret_cast<int *>(tmp + kScalars);
-  CK(cudaMallocHost(&c->small_host, sizeof(double) * (kScalars + 2)));
+  b.status = reinterpret_cast<int *>(tmp + (size_t)kScalars * nc);
+  CK(cudaMallocHost(&c->small_host, sizeof(double) * ((size_t)kScalars * nc + nc / 2 + 2)));
+  if (nc > 1) {
+    void *q = nullptr;
+    CK(cudaMalloc(&q, sizeof(Phys) * nc));
+    c->allocs.push_back(q);
+    c->phys_dev = static_cast<Phys *>(q);
+    g.phys = c->phys_dev;
+  }
   if (upload_poisson(*c, d)) return 1;
   c->U[0] = b.ux;
   c->U[1] = b.ux_star;
@@ -376,6 +410,13 @@ int make_ctx(const domain_t *d) {
   c->SY[1] = b.srcuy[1];
   c->SV[0] = b.srcvof[0];
   c->SV[1] = b.srcvof[1];
+  return 0;
+}
+
+int make_ctx(const domain_t *d) {
+  g_ctx.reset();
+  auto c = std::make_unique<Ctx>();
+  if (build_ctx(c.get(), d, 1)) return 1;
   g_ctx = std::move(c);
   return 0;
 }
@@ -393,7 +434,7 @@ Ctx *get_ctx(const domain_t *d, const fluid_t *f, const interface_t *itf) {
   }
   const double Re = f ? f->Re : (std::isnan(c->Re) ? 1. : c->Re);
   if (!c->met || !(c->Re == Re)) {
-    if (upload_metrics(*c, d, Re)) return nullptr;
+    if (upload_metrics(*c, d, &Re)) return nullptr;
   }
   if (f) set_phys(*c, f, itf);
   return c;
@@ -492,10 +533,11 @@ void enqueue_substage(Ctx &c, int k) {
   const double *sc = b.scalars;
   timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
-  if (g_curv_model) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
+  const bool learned = g_curv_model && c.nc == 1;
+  if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
   timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
   timed(c, KC_FLUX_FORCE,
-        [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, g_curv_model ? 3 : 2); });
+        [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
   timed(c, KC_PREDICT, [&] {
@@ -532,11 +574,16 @@ int launch_step(Ctx &c) {
     const std::vector<double> sig = {p.denr, p.visr,   p.refden,   p.den_lo,   p.den_hi,   p.vis_lo,
                                      p.vis_hi, p.grav, p.force_coef, p.irefden, p.nu,      c.dt_fixed,
                                      g_coef[0], g_coef[1], g_coef[2]};
-    if (sig.size() != c.graph_sig.size() ||
-        memcmp(sig.data(), c.graph_sig.data(), sizeof(double) * sig.size()) != 0) {
+    std::vector<double> all(sig);
+    for (const Phys &q : c.phys_host) {
+      const double *w = reinterpret_cast<const double *>(&q);
+      all.insert(all.end(), w, w + sizeof(Phys) / sizeof(double));
+    }
+    if (all.size() != c.graph_sig.size() ||
+        memcmp(all.data(), c.graph_sig.data(), sizeof(double) * all.size()) != 0) {
       for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
       c.graphs.clear();
-      c.graph_sig = sig;
+      c.graph_sig = all;
     }
   }
   const int key = role_key(c);
@@ -568,10 +615,13 @@ int launch_step(Ctx &c) {
   return 0;
 }
 
+int upload_fields(Ctx &c, const fluid_t *f, const interface_t *itf) {
+  return h2d(c, f->ux, L_UX, c.U[c.iu]) || h2d(c, f->uy, L_UY, c.V[c.iu]) || h2d(c, f->p, L_P, c.b.p) ||
+         h2d(c, f->psi[0], L_P, c.PSI[c.ipsi]) || h2d(c, itf->vof, L_VOF, c.b.vof);
+}
+
 int upload_state(Ctx &c, const fluid_t *f, const interface_t *itf) {
-  if (h2d(c, f->ux, L_UX, c.U[c.iu]) || h2d(c, f->uy, L_UY, c.V[c.iu]) || h2d(c, f->p, L_P, c.b.p) ||
-      h2d(c, f->psi[0], L_P, c.PSI[c.ipsi]) || h2d(c, itf->vof, L_VOF, c.b.vof))
-    return 1;
+  if (upload_fields(c, f, itf)) return 1;
   // rho^k of the current vof (src/fluid/density.c)
   launch_props(c.s, c.g, c.m, c.ph, c.b, true, false, false, c.DEN[c.iden]);
   c.resident = true;
@@ -606,6 +656,160 @@ int read_dt_status(Ctx &c, double *dt, int *status) {
   if (sync(c)) return 1;
   if (dt) *dt = c.small_host[0];
   if (status) memcpy(status, c.small_host + kScalars, sizeof(int));
+  return 0;
+}
+
+// ---- batches of independent cases (sbfs_integrate_batch)
+// Cases are grouped by grid; each group is one context whose fields hold its
+// cases as consecutive slabs, and every kernel of the step runs all cases of
+// the group in one launch (the case is blockIdx.z).  Groups run on their own
+// streams.
+struct Batch {
+  std::vector<std::unique_ptr<Ctx>> groups;
+  std::vector<int> group_of, slot_of;
+  std::vector<const void *> ident;  // fluid and interface pointers of the cases
+  std::vector<double> res;          // Re per case, to notice a change
+};
+std::unique_ptr<Batch> g_batch;
+
+bool same_domain_grid(const domain_t *a, const domain_t *d) {
+  return a->mysizes[0] == d->mysizes[0] && a->mysizes[1] == d->mysizes[1] && a->lengths[0] == d->lengths[0] &&
+         a->lengths[1] == d->lengths[1] && a->hy == d->hy &&
+         memcmp(a->hxxf, d->hxxf, sizeof(double) * (a->mysizes[0] + 1)) == 0;
+}
+
+bool same_grid_as(const Ctx &c, const domain_t *d) {
+  return c.nx == (int)d->mysizes[0] && c.ny == (int)d->mysizes[1] && c.lx == d->lengths[0] &&
+         c.ly == d->lengths[1] && c.g.hy == d->hy &&
+         memcmp(c.hxxf.data(), d->hxxf, sizeof(double) * (c.nx + 1)) == 0;
+}
+
+Batch *prepare_batch(int n, const domain_t *const *d, fluid_t *const *f, interface_t *const *itf) {
+  if (n <= 0 || !d || !f || !itf) {
+    fail("empty batch");
+    return nullptr;
+  }
+  if (load_coefs()) return nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!f[i] || !itf[i]) {
+      fail("case %d: null fluid or interface", i);
+      return nullptr;
+    }
+    if (check_domain(d[i])) return nullptr;
+  }
+  Batch *b = g_batch.get();
+  bool same = b && (int)b->group_of.size() == n;
+  for (int i = 0; same && i < n; ++i)
+    same = b->ident[2 * i] == f[i] && b->ident[2 * i + 1] == itf[i] &&
+           same_grid_as(*b->groups[b->group_of[i]], d[i]);
+  if (!same) {
+    g_batch.reset();
+    auto nb = std::make_unique<Batch>();
+    std::vector<int> first, count;  // first case and size of each group
+    nb->group_of.resize(n);
+    nb->slot_of.resize(n);
+    for (int i = 0; i < n; ++i) {
+      int gi = -1;
+      for (size_t q = 0; q < first.size() && gi < 0; ++q)
+        if (same_domain_grid(d[first[q]], d[i])) gi = (int)q;
+      if (gi < 0) {
+        gi = (int)first.size();
+        first.push_back(i);
+        count.push_back(0);
+      }
+      nb->group_of[i] = gi;
+      nb->slot_of[i] = count[gi]++;
+      nb->ident.push_back(f[i]);
+      nb->ident.push_back(itf[i]);
+    }
+    for (size_t q = 0; q < first.size(); ++q) {
+      auto c = std::make_unique<Ctx>();
+      if (build_ctx(c.get(), d[first[q]], count[q])) return nullptr;
+      c->phys_host.resize(count[q]);
+      nb->groups.push_back(std::move(c));
+    }
+    nb->res.assign(n, NAN);
+    g_batch = std::move(nb);
+    b = g_batch.get();
+  }
+  // physics and metrics per case (re-uploaded when they change)
+  for (size_t q = 0; q < b->groups.size(); ++q) {
+    Ctx &c = *b->groups[q];
+    std::vector<Phys> ph(c.nc);
+    std::vector<double> re(c.nc);
+    const domain_t *dq = nullptr;
+    bool re_changed = !c.met;
+    for (int i = 0; i < n; ++i) {
+      if (b->group_of[i] != (int)q) continue;
+      const int k = b->slot_of[i];
+      ph[k] = phys_of(f[i], itf[i]);
+      ph[k].dtfix = fixed_dt(c, d[i], f[i], itf[i]);
+      re[k] = f[i]->Re;
+      re_changed = re_changed || !(b->res[i] == f[i]->Re);
+      b->res[i] = f[i]->Re;
+      dq = d[i];
+    }
+    if (re_changed && upload_metrics(c, dq, re.data())) return nullptr;
+    if (re_changed || memcmp(ph.data(), c.phys_host.data(), sizeof(Phys) * c.nc) != 0) {
+      c.phys_host = ph;
+      // a group of one case has no table: its kernels take c.ph
+      if (c.phys_dev && (cudaMemcpyAsync(c.phys_dev, c.phys_host.data(), sizeof(Phys) * c.nc,
+                                         cudaMemcpyHostToDevice, c.s) != cudaSuccess ||
+                         sync(c))) {
+        fail("uploading the per-case physics");
+        return nullptr;
+      }
+    }
+    c.ph = ph[0];  // the kernels read the table; this is only their argument
+    c.dt_fixed = ph[0].dtfix;
+  }
+  return b;
+}
+
+int batch_upload(Batch &b, int n, fluid_t *const *f, interface_t *const *itf) {
+  for (int i = 0; i < n; ++i) {
+    Ctx &c = *b.groups[b.group_of[i]];
+    c.kcase = b.slot_of[i];
+    const int rc = upload_fields(c, f[i], itf[i]);
+    c.kcase = 0;
+    if (rc) return 1;
+  }
+  for (auto &c : b.groups) {
+    // rho^k of the current vof, every case of the group in one launch
+    launch_props(c->s, c->g, c->m, c->ph, c->b, true, false, false, c->DEN[c->iden]);
+    c->resident = true;
+  }
+  return 0;
+}
+
+int batch_download(Batch &b, int n, fluid_t *const *f, interface_t *const *itf, bool all) {
+  for (int i = 0; i < n; ++i) {
+    Ctx &c = *b.groups[b.group_of[i]];
+    c.kcase = b.slot_of[i];
+    const int rc = download_state(c, f[i], itf[i], all);
+    c.kcase = 0;
+    if (rc) return 1;
+  }
+  return 0;
+}
+
+// dt of every case after the last step; fails on a non-finite velocity
+int batch_read_dt(Batch &b, int n, double *dts) {
+  for (auto &c : b.groups) {
+    const size_t bytes = sizeof(double) * (size_t)kScalars * c->nc + sizeof(int) * c->nc;
+    CK(cudaMemcpyAsync(c->small_host, c->b.scalars, bytes, cudaMemcpyDeviceToHost, c->s));
+  }
+  for (auto &c : b.groups)
+    if (sync(*c)) return 1;
+  for (int i = 0; i < n; ++i) {
+    const Ctx &c = *b.groups[b.group_of[i]];
+    const int k = b.slot_of[i];
+    int status = 0;
+    memcpy(&status, reinterpret_cast<const char *>(c.small_host + (size_t)kScalars * c.nc) + sizeof(int) * k,
+           sizeof(int));
+    if (status & 1) return fail("case %d: non-finite velocity detected by decide_dt", i);
+    if (dts) dts[i] = c.small_host[(size_t)k * kScalars];
+  }
   return 0;
 }
 
@@ -857,6 +1061,71 @@ int integrate(const domain_t *d, fluid_t *f, interface_t *itf, double *dt) {
   int status = 0;
   if (read_dt_status(*c, dt, &status)) return 1;
   if (status & 1) return fail("non-finite velocity detected by decide_dt");
+  return 0;
+}
+
+int sbfs_integrate_batch(int n, const domain_t *const *domains, fluid_t *const *fluids,
+                         interface_t *const *interfaces, double *dts) {
+  Batch *b = prepare_batch(n, domains, fluids, interfaces);
+  if (!b) return 1;
+  bool upload = g_sync_mode != SBFS_SYNC_NONE;
+  for (auto &c : b->groups) upload = upload || !c->resident;
+  if (upload && batch_upload(*b, n, fluids, interfaces)) return 1;
+  for (auto &c : b->groups)
+    if (launch_step(*c)) return 1;
+  if (g_sync_mode != SBFS_SYNC_NONE) {
+    for (int i = 0; i < n; ++i) swap_data(fluids[i]->psi[0], fluids[i]->psi[1]);
+    if (batch_download(*b, n, fluids, interfaces, g_sync_mode == SBFS_SYNC_ALL)) return 1;
+  }
+  return batch_read_dt(*b, n, dts);
+}
+
+int sbfs_run_batch_steps_timed(int nsteps, float *ms) {
+  Batch *b = g_batch.get();
+  if (!b) return fail("no batch on the device: call sbfs_integrate_batch first");
+  for (auto &c : b->groups)
+    if (!c->resident) return fail("the batch's state is not on the device");
+  Ctx &c0 = *b->groups[0];
+  CK(cudaEventRecord(c0.e0, c0.s));
+  for (size_t q = 1; q < b->groups.size(); ++q) CK(cudaStreamWaitEvent(b->groups[q]->s, c0.e0, 0));
+  for (int k = 0; k < nsteps; ++k)
+    for (auto &c : b->groups)
+      if (launch_step(*c)) return 1;
+  for (size_t q = 1; q < b->groups.size(); ++q) {
+    CK(cudaEventRecord(b->groups[q]->e1, b->groups[q]->s));
+    CK(cudaStreamWaitEvent(c0.s, b->groups[q]->e1, 0));
+  }
+  CK(cudaEventRecord(c0.e1, c0.s));
+  for (auto &c : b->groups)
+    if (sync(*c)) return 1;
+  CK(cudaEventElapsedTime(ms, c0.e0, c0.e1));
+  return batch_read_dt(*b, (int)b->group_of.size(), nullptr);
+}
+
+int sbfs_batch_sync_to_host(int n, const domain_t *const *domains, fluid_t *const *fluids,
+                            interface_t *const *interfaces) {
+  (void)domains;
+  Batch *b = g_batch.get();
+  if (!b || (int)b->group_of.size() != n) return fail("no batch of %d cases on the device", n);
+  for (int i = 0; i < n; ++i)
+    if (b->ident[2 * i] != fluids[i] || b->ident[2 * i + 1] != interfaces[i])
+      return fail("case %d is not the one the batch holds", i);
+  if (batch_download(*b, n, fluids, interfaces, g_sync_mode == SBFS_SYNC_ALL)) return 1;
+  for (auto &c : b->groups)
+    if (sync(*c)) return 1;
+  return 0;
+}
+
+int sbfs_batch_groups(int *ngroups, int *cases) {
+  Batch *b = g_batch.get();
+  *ngroups = b ? (int)b->groups.size() : 0;
+  if (b && cases)
+    for (size_t q = 0; q < b->groups.size(); ++q) cases[q] = b->groups[q]->nc;
+  return 0;
+}
+
+int sbfs_batch_release(void) {
+  g_batch.reset();
   return 0;
 }
 

@@ -40,6 +40,15 @@ struct Grid {
   int p3;  // pitch of normal (3 doubles per element)
   double hy, ihy;
   double dx, idx;  // uniform cell width HXXC and its inverse
+  // batch of nc cases on this grid (the case is blockIdx.z; 1 for a single
+  // case): element strides between cases of the scalar-pitched fields, of
+  // dvof, of normal, of the Poisson spectrum (double2) and of the per-case
+  // metric columns (nuf); per-case physics, or nullptr to use the kernel's
+  // Phys argument
+  int nc;
+  int cm;
+  size_t cs1, cs2, cs3, css;
+  const struct Phys *phys;
 };
 
 // physical parameters of one case
@@ -50,7 +59,16 @@ struct Phys {
   double force_coef;  // 2 / (1 + denr) / We
   double irefden;     // 1 / refden
   double nu;          // 1 / Re
+  double dtfix;       // diffusive / capillary bound of dt (batches: per case)
 };
+
+// pointer of case blockIdx.z in a batch (null stays null)
+template <class T>
+__device__ __forceinline__ T *zp(T *p, size_t stride) {
+  return p ? p + (size_t)blockIdx.z * stride : p;
+}
+// physics of case blockIdx.z
+__device__ __forceinline__ Phys zphys(const Grid &g, const Phys &ph) { return g.phys ? g.phys[blockIdx.z] : ph; }
 
 // per-step scalars written by the time-step kernel and read by all others:
 // [0] dt; for substage k: alpha_k dt, beta_k dt, gamma_k dt, dt_old_k,

@@ -39,7 +39,7 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
-dim3 grid2d(int ni, int nj) { return dim3((ni + BX - 1) / BX, (nj + BY - 1) / BY); }
+dim3 grid2d(int ni, int nj, int nz = 1) { return dim3((ni + BX - 1) / BX, (nj + BY - 1) / BY, nz); }
 
 // ---------------------------------------------------------------------------
 // density, viscosity, corner gradients of vof
@@ -49,9 +49,15 @@ dim3 grid2d(int ni, int nj) { return dim3((ni + BX - 1) / BX, (nj + BY - 1) / BY
 // thread (I, J): I = 0..nx+1
 // ---------------------------------------------------------------------------
 template <bool DEN, bool VIS, bool GRAD>
-__global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph, const double *__restrict__ vof,
+__global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, const double *__restrict__ vof,
                                                   double *__restrict__ den, double *__restrict__ visux,
                                                   double *__restrict__ visuy, double *__restrict__ dvof) {
+  const Phys ph = zphys(g, ph0);
+  vof = zp(vof, g.cs1);
+  den = zp(den, g.cs1);
+  visux = zp(visux, g.cs1);
+  visuy = zp(visuy, g.cs1);
+  dvof = zp(dvof, g.cs2);
   const int I = blockIdx.x * BX + threadIdx.x;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -168,10 +174,21 @@ __device__ __forceinline__ double face_kappa_sum(double pl, double pr, double kl
 
 template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY = false, bool ITF_KAPPA = false>
 __global__ void __launch_bounds__(BX *BY)
-    k_flux_force(Grid g, Metrics m, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
+    k_flux_force(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
                  const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
                  const double *__restrict__ curv, double *__restrict__ fluxx, double *__restrict__ fluxy,
                  double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
+  const Phys ph = zphys(g, ph0);
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  vof = zp(vof, g.cs1);
+  normal = zp(normal, g.cs3);
+  den0 = zp(den0, g.cs1);
+  curv = zp(curv, g.cs1);
+  fluxx = zp(fluxx, g.cs1);
+  fluxy = zp(fluxy, g.cs1);
+  ifrcx = zp(ifrcx, g.cs1);
+  ifrcy = zp(ifrcy, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -257,6 +274,11 @@ __global__ void __launch_bounds__(BX *BY)
 __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const double *__restrict__ vof,
                                                       const double *__restrict__ dvof, double *__restrict__ curv,
                                                       int *__restrict__ list, int *__restrict__ count) {
+  vof = zp(vof, g.cs1);
+  dvof = zp(dvof, g.cs2);
+  curv = zp(curv, g.cs1);
+  list = zp(list, (size_t)g.nx * g.ny);
+  count = zp(count, 1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   const bool in = I <= g.nx && J <= g.ny;
@@ -294,6 +316,14 @@ __global__ void __launch_bounds__(256)
     k_interface_cells(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
                       const double *__restrict__ vof, const double *__restrict__ dvof, const int *__restrict__ list,
                       const int *__restrict__ count, double *__restrict__ fluxx, double *__restrict__ fluxy) {
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  vof = zp(vof, g.cs1);
+  dvof = zp(dvof, g.cs2);
+  list = zp(list, (size_t)g.nx * g.ny);
+  count = zp(count, 1);
+  fluxx = zp(fluxx, g.cs1);
+  fluxy = zp(fluxy, g.cs1);
   const int n = *count;
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
   const size_t q = g.p2 / 2;
@@ -330,10 +360,22 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------
 template <bool FUSED>
 __global__ void __launch_bounds__(BX *BY)
-    k_vof_advance(Grid g, Metrics m, Phys ph, const double *__restrict__ sc, int k, double *__restrict__ vof,
+    k_vof_advance(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, double *__restrict__ vof,
                   const double *__restrict__ fluxx, const double *__restrict__ fluxy, double *__restrict__ src_a,
                   const double *__restrict__ src_b, const double *__restrict__ ux, const double *__restrict__ uy,
                   double *__restrict__ mfx, double *__restrict__ mfy, double *__restrict__ den1) {
+  const Phys ph = zphys(g, ph0);
+  sc = zp(sc, kScalars);
+  vof = zp(vof, g.cs1);
+  fluxx = zp(fluxx, g.cs1);
+  fluxy = zp(fluxy, g.cs1);
+  src_a = zp(src_a, g.cs1);
+  src_b = zp(src_b, g.cs1);
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  mfx = zp(mfx, g.cs1);
+  mfy = zp(mfy, g.cs1);
+  den1 = zp(den1, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -388,6 +430,13 @@ __global__ void __launch_bounds__(BX *BY)
     k_stress(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
              const double *__restrict__ visux, const double *__restrict__ visuy, double *__restrict__ txx,
              double *__restrict__ txy, double *__restrict__ tyy) {
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  visux = zp(visux, g.cs1);
+  visuy = zp(visuy, g.cs1);
+  txx = zp(txx, g.cs1);
+  txy = zp(txy, g.cs1);
+  tyy = zp(tyy, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -420,7 +469,7 @@ __global__ void __launch_bounds__(BX *BY)
 // (I, J - 1/2); also stores e = rho_ref / rho^{k+1} - 1 at both faces
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(BX *BY)
-    k_predict(Grid g, Metrics m, Phys ph, const double *__restrict__ sc, int k, const double *__restrict__ ux,
+    k_predict(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, const double *__restrict__ ux,
               const double *__restrict__ uy, double *__restrict__ ux_out, double *__restrict__ uy_out,
               const double *__restrict__ mfx, const double *__restrict__ mfy, const double *__restrict__ txx,
               const double *__restrict__ txy, const double *__restrict__ tyy, const double *__restrict__ p,
@@ -428,6 +477,31 @@ __global__ void __launch_bounds__(BX *BY)
               const double *__restrict__ den1, double *__restrict__ sxa, const double *__restrict__ sxb,
               double *__restrict__ sxg, double *__restrict__ sya, const double *__restrict__ syb,
               double *__restrict__ syg, double *__restrict__ ex, double *__restrict__ ey) {
+  const Phys ph = zphys(g, ph0);
+  const double *__restrict__ nuf = zp(m.nuf, (size_t)g.cm);
+  sc = zp(sc, kScalars);
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  ux_out = zp(ux_out, g.cs1);
+  uy_out = zp(uy_out, g.cs1);
+  mfx = zp(mfx, g.cs1);
+  mfy = zp(mfy, g.cs1);
+  txx = zp(txx, g.cs1);
+  txy = zp(txy, g.cs1);
+  tyy = zp(tyy, g.cs1);
+  p = zp(p, g.cs1);
+  ifrcx = zp(ifrcx, g.cs1);
+  ifrcy = zp(ifrcy, g.cs1);
+  den0 = zp(den0, g.cs1);
+  den1 = zp(den1, g.cs1);
+  sxa = zp(sxa, g.cs1);
+  sxb = zp(sxb, g.cs1);
+  sxg = zp(sxg, g.cs1);
+  sya = zp(sya, g.cs1);
+  syb = zp(syb, g.cs1);
+  syg = zp(syg, g.cs1);
+  ex = zp(ex, g.cs1);
+  ey = zp(ey, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -447,7 +521,7 @@ __global__ void __launch_bounds__(BX *BY)
     double a = ifrcx[ix(g, r, I - 2)];
     const double rho0 = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];  // 2 rho^k
     a = fma(0.5 * ph.grav, rho0, a);
-    a = fma(m.nuf[I], txx[ix(g, r, I - 1)] - txx[ix(g, r, I - 2)], a);
+    a = fma(nuf[I], txx[ix(g, r, I - 1)] - txx[ix(g, r, I - 2)], a);
     a = fma(nuy, txy[ix(g, rp, I - 1)] - txy[ix(g, r, I - 1)], a);
     a = fma(-m.q4f[I], fma(sxp, up, -sxm * um), a);
     a = fma(-m.q4fy[I], fma(syp, vp, -sym * vm), a);
@@ -583,6 +657,13 @@ __global__ void __launch_bounds__(256)
     k_poisson_fwd(Grid g, const double *__restrict__ sc, int k, const double *__restrict__ ux,
                   const double *__restrict__ uy, const double *__restrict__ psi, const double *__restrict__ ex,
                   const double *__restrict__ ey, const double2 *__restrict__ tw, double2 *__restrict__ spec) {
+  sc = zp(sc, kScalars);
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  psi = zp(psi, g.cs1);
+  ex = zp(ex, g.cs1);
+  ey = zp(ey, g.cs1);
+  spec = zp(spec, g.css);
   extern __shared__ double2 smem[];
   const int ny = g.ny, M = ny >> 1;
   double2 *A = smem, *B = smem + W * M;
@@ -624,6 +705,8 @@ __global__ void __launch_bounds__(256)
 template <int W>
 __global__ void __launch_bounds__(256)
     k_poisson_inv(Grid g, const double2 *__restrict__ tw, const double2 *__restrict__ spec, double *__restrict__ psi) {
+  spec = zp(spec, g.css);
+  psi = zp(psi, g.cs1);
   extern __shared__ double2 smem[];
   const int ny = g.ny, M = ny >> 1, M1 = M + 1;
   double2 *A = smem, *B = smem + W * M;
@@ -673,6 +756,7 @@ __global__ void __launch_bounds__(256)
 // Shared memory: per system a planar array with an odd lane stride S.
 __global__ void __launch_bounds__(256)
     k_poisson_tdm(Grid g, int MB, int L, int S, const double4_32a *__restrict__ fac, double2 *__restrict__ spec) {
+  spec = zp(spec, g.css);
   extern __shared__ double2 smem_d2[];
   double *sm = reinterpret_cast<double *>(smem_d2);
   const int nx = g.nx, M1 = g.ny / 2 + 1;
@@ -770,6 +854,14 @@ __global__ void __launch_bounds__(BX *BY)
     k_correct(Grid g, Metrics m, const double *__restrict__ sc, int k, double *__restrict__ ux,
               double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ psio,
               const double *__restrict__ ex, const double *__restrict__ ey, double *__restrict__ p) {
+  sc = zp(sc, kScalars);
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  psin = zp(psin, g.cs1);
+  psio = zp(psio, g.cs1);
+  ex = zp(ex, g.cs1);
+  ey = zp(ey, g.cs1);
+  p = zp(p, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -830,9 +922,16 @@ constexpr unsigned long long kAbsMask = 0x7fffffffffffffffULL;
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
 
 __global__ void __launch_bounds__(BX *BY)
-    k_decide_dt(Grid g, Metrics m, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
+    k_decide_dt(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
                 unsigned long long *__restrict__ acc, double *__restrict__ sc, int *__restrict__ status,
                 double dt_fixed, double coef_adv) {
+  const Phys ph = zphys(g, ph0);
+  if (g.phys) dt_fixed = ph.dtfix;
+  ux = zp(ux, g.cs1);
+  uy = zp(uy, g.cs1);
+  acc = zp(acc, (size_t)g.nx + 8);
+  sc = zp(sc, kScalars);
+  status = zp(status, 1);
   __shared__ unsigned long long colmax[BY][BX];
   __shared__ unsigned long long ymax[BY * BX];
   __shared__ bool last;
@@ -1159,7 +1258,7 @@ cudaError_t configure_kernels() {
 
 void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, bool den, bool vis,
                   bool grad, double *den_out) {
-  const dim3 gr = grid2d(g.nx + 2, g.ny), bl(BX, BY);
+  const dim3 gr = grid2d(g.nx + 2, g.ny, g.nc), bl(BX, BY);
   if (den && vis && grad)
     k_props<true, true, true><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
   else if (vis && grad)
@@ -1204,12 +1303,12 @@ void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
 
 void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                             const double *ux, const double *uy, const double *den0, int stage) {
-  const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
+  const dim3 gr = grid2d(g.nx, g.ny, g.nc), bl(BX, BY);
   if (stage == 0) {
-    cudaMemsetAsync(b.icount, 0, sizeof(int), s);
+    cudaMemsetAsync(b.icount, 0, sizeof(int) * g.nc, s);
     k_curv_list<<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.curv, b.ilist, b.icount);
   } else if (stage == 1) {
-    k_interface_cells<<<4 * 152, 256, 0, s>>>(g, m, ux, uy, b.vof, b.dvof, b.ilist, b.icount, b.fluxx, b.fluxy);
+    k_interface_cells<<<dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s>>>(g, m, ux, uy, b.vof, b.dvof, b.ilist, b.icount, b.fluxx, b.fluxy);
   } else if (stage == 2) {
     k_flux_force<true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                            b.fluxy, b.ifrcx, b.ifrcy);
@@ -1222,7 +1321,7 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                         const double *sc, int k, double *src_a, const double *src_b, bool fused, const double *ux,
                         const double *uy, double *den1) {
-  const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
+  const dim3 gr = grid2d(g.nx, g.ny, g.nc), bl(BX, BY);
   if (fused)
     k_vof_advance<true><<<gr, bl, 0, s>>>(g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, b.mfluxx,
                                           b.mfluxy, den1);
@@ -1238,7 +1337,7 @@ void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, con
 
 void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *ux,
                    const double *uy) {
-  k_stress<<<grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s>>>(g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
+  k_stress<<<grid2d(g.nx + 1, g.ny, g.nc), dim3(BX, BY), 0, s>>>(g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -1246,7 +1345,7 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                     const double *mfy, const double *den0, const double *den1, double *srcux_a,
                     const double *srcux_b, double *srcux_g, double *srcuy_a, const double *srcuy_b,
                     double *srcuy_g) {
-  k_predict<<<grid2d(g.nx, g.ny), dim3(BX, BY), 0, s>>>(g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
+  k_predict<<<grid2d(g.nx, g.ny, g.nc), dim3(BX, BY), 0, s>>>(g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
                                                         b.txy, b.tyy, b.p, b.ifrcx, b.ifrcy, den0, den1, srcux_a,
                                                         srcux_b, srcux_g, srcuy_a, srcuy_b, srcuy_g, b.irhox,
                                                         b.irhoy);
@@ -1255,20 +1354,20 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                         const double *uy, const double *psi_old) {
   const int nb = (g.nx + kFftCols - 1) / kFftCols;
-  k_poisson_fwd<kFftCols><<<nb, 256, poisson_fft_smem(g.ny), s>>>(g, sc, k, ux, uy, psi_old, b.irhox, b.irhoy,
+  k_poisson_fwd<kFftCols><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny), s>>>(g, sc, k, ux, uy, psi_old, b.irhox, b.irhoy,
                                                                   b.twiddle, b.spec);
 }
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
   const int mb = poisson_tdm_modes(g.nx);
   const int M1 = g.ny / 2 + 1;
-  k_poisson_tdm<<<(M1 + mb - 1) / mb, 64 * mb, poisson_tdm_smem(g.nx), s>>>(
+  k_poisson_tdm<<<dim3((M1 + mb - 1) / mb, 1, g.nc), 64 * mb, poisson_tdm_smem(g.nx), s>>>(
       g, mb, tdm_chunk(g.nx), tdm_stride(g.nx), reinterpret_cast<const double4_32a *>(b.tdm_fac), b.spec);
 }
 
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
   const int nb = (g.nx + kFftCols - 1) / kFftCols;
-  k_poisson_inv<kFftCols><<<nb, 256, poisson_fft_smem(g.ny), s>>>(g, b.twiddle, b.spec, psi_new);
+  k_poisson_inv<kFftCols><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny), s>>>(g, b.twiddle, b.spec, psi_new);
 }
 
 void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
@@ -1280,7 +1379,7 @@ void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *
 
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
                     double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure) {
-  const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
+  const dim3 gr = grid2d(g.nx, g.ny, g.nc), bl(BX, BY);
   if (pressure)
     k_correct<true><<<gr, bl, 0, s>>>(g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
   else
@@ -1295,8 +1394,8 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
                       const double *ux, const double *uy, double dt_fixed, double coef_adv) {
   int gy = (g.ny + BY - 1) / BY;
   const int gx = (g.nx + BX) / BX;
-  while (gy > 1 && gx * gy > 4 * 152) gy = (gy + 1) / 2;
-  k_decide_dt<<<dim3(gx, gy), dim3(BX, BY), 0, s>>>(g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
+  while (gy > 1 && gx * gy * g.nc > 4 * 152) gy = (gy + 1) / 2;
+  k_decide_dt<<<dim3(gx, gy, g.nc), dim3(BX, BY), 0, s>>>(g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
                                                     coef_adv);
 }
 

@@ -74,6 +74,7 @@ extern "C" int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, cons
   e = cudaMemsetAsync(g_scratch_addr[dev], 0, sizeof(unsigned long long) * (nx + 4), s);
   if (e != cudaSuccess) return report("sbfs_decide_dt_noalloc: clearing the scratch", e);
   Grid g{};
+  g.nc = 1;
   g.nx = nx;
   g.ny = ny;
   g.p1 = pitch;

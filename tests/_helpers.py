@@ -71,3 +71,26 @@ def fma_noise_floor(wl, steps, slots=STATE):
         a_lib.integrate(a)
         b_lib.integrate(b)
     return compare_state(a, b, slots)
+
+
+def rounding_sensitivity(wl, steps, eps=1e-15, seed=0, slots=STATE):
+    """spread of the oracle's own solution after `steps` steps when the
+    initial vof of the interface cells is perturbed by a relative eps (a few
+    ulps): how far rounding-level differences in the input carry.  Cases
+    with strong surface tension amplify them through the THINC tails, where
+    the normalised corner normals are rounding noise."""
+    import oracle
+    lib = oracle.Oracle()
+    lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    set_env(wl)
+    a = new_state(wl, lib)
+    fields = wl.fields()
+    vof = fields["vof"]
+    rng = np.random.default_rng(seed)
+    itf = (vof > 0) & (vof < 1)
+    vof[itf] = np.clip(vof[itf] * (1 + eps * rng.uniform(-1, 1, int(itf.sum()))), 0.0, 1.0)
+    b = new_state(wl, lib, fields)
+    for _ in range(steps):
+        lib.integrate(a)
+        lib.integrate(b)
+    return compare_state(a, b, slots)

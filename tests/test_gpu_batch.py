@@ -1,0 +1,124 @@
+"""Batches of independent cases (sbfs_integrate_batch): every case of a
+batch must step exactly as it does alone, and match the oracle."""
+import numpy as np
+import pytest
+
+from simplebubblyflowsolver_gb300 import SYNC_NONE, SYNC_STATE, ic
+
+from ._helpers import clone, compare_state, fma_noise_floor, new_state, rounding_sensitivity, set_env
+
+SMALL_GRIDS = ((32, 16), (64, 32), (128, 64))
+SLOTS = ("ux", "uy", "p", "psi0", "psi1", "vof")
+
+
+@pytest.fixture(scope="module")
+def libs():
+    import oracle
+    from simplebubblyflowsolver_gb300 import load_library
+    return load_library(), oracle.Oracle()
+
+
+def prepare(gpu, orc, wls):
+    set_env(wls[0])
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    gpu.set_use_graphs(True)
+    return [new_state(wl, orc) for wl in wls]
+
+
+def test_ensemble_generator():
+    wls = ic.ensemble(256, seed=0)
+    assert len(wls) == 256
+    assert {(w.nx, w.ny) for w in wls} == set(ic.ENSEMBLE_GRIDS)
+    We = np.array([w.We for w in wls])
+    Re = np.array([w.Re for w in wls])
+    dr = np.array([w.denr for w in wls])
+    assert We.min() >= 1 and We.max() <= 100 and Re.min() >= 10 and Re.max() <= 100
+    assert dr.min() >= 1e-3 and dr.max() <= 1e-1
+    # log-uniform: about half of the cases below the geometric mean
+    assert 0.35 < np.mean(We < 10) < 0.65
+
+
+@pytest.mark.gpu
+def test_batch_equals_single_cases_bitwise(libs):
+    gpu, orc = libs
+    wls = ic.ensemble(12, seed=1, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    batch = [clone(s) for s in st0]
+    alone = [clone(s) for s in st0]
+    for _ in range(4):
+        dts = gpu.integrate_batch(batch)
+        for k, st in enumerate(alone):
+            assert gpu.integrate(st) == dts[k]
+    assert sorted(gpu.batch_groups()) == sorted(
+        [sum(1 for w in wls if (w.nx, w.ny) == g) for g in SMALL_GRIDS if any((w.nx, w.ny) == g for w in wls)])
+    for k, (a, b) in enumerate(zip(batch, alone)):
+        for s in SLOTS:
+            assert np.array_equal(a.field(s), b.field(s)), (k, s)
+
+
+@pytest.mark.gpu
+def test_batch_matches_oracle(libs):
+    gpu, orc = libs
+    wls = ic.ensemble(6, seed=2, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    batch = [clone(s) for s in st0]
+    ref = [clone(s) for s in st0]
+    steps = 5
+    for _ in range(steps):
+        dts = gpu.integrate_batch(batch)
+        for k, st in enumerate(ref):
+            do = orc.integrate(st)
+            # dt follows max |u|, which carries the state's rounding difference
+            assert abs(dts[k] - do) <= 1e-10 * do
+    for k, wl in enumerate(wls):
+        errs = compare_state(batch[k], ref[k])
+        # cases with strong surface tension amplify rounding (see the static
+        # drop); the bar is then ten times the larger of the spread between
+        # two faithful CPU builds and the oracle's own response to a few-ulp
+        # perturbation of the initial interface
+        tol = 1e-10
+        if max(errs.values()) > tol:
+            floor = max(max(fma_noise_floor(wl, steps).values()), max(rounding_sensitivity(wl, steps).values()))
+            tol = max(tol, 10 * floor)
+        print(k, (wl.nx, wl.ny), f"We={wl.We:.1f} Re={wl.Re:.1f} denr={wl.denr:.1e}",
+              {s: f"{v:.1e}" for s, v in errs.items()}, "tol", tol)
+        assert max(errs.values()) <= tol, (k, errs, tol)
+
+
+@pytest.mark.gpu
+def test_resident_batch_equals_synced_batch(libs):
+    gpu, orc = libs
+    wls = ic.ensemble(9, seed=4, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    synced = [clone(s) for s in st0]
+    resident = [clone(s) for s in st0]
+    for _ in range(3):
+        gpu.integrate_batch(synced)
+    gpu.set_sync_mode(SYNC_NONE)
+    try:
+        for _ in range(3):
+            gpu.integrate_batch(resident)
+        gpu.batch_sync_to_host(resident)
+    finally:
+        gpu.set_sync_mode(SYNC_STATE)
+    for k, (a, b) in enumerate(zip(resident, synced)):
+        for s in ("ux", "uy", "p", "vof"):
+            assert np.array_equal(a.field(s), b.field(s)), (k, s)
+
+
+@pytest.mark.gpu
+def test_timed_batch_runs(libs):
+    gpu, orc = libs
+    wls = ic.ensemble(8, seed=5, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    batch = [clone(s) for s in st0]
+    gpu.set_sync_mode(SYNC_NONE)
+    try:
+        gpu.integrate_batch(batch)
+        ms = gpu.run_batch_steps_timed(5)
+        assert ms > 0
+    finally:
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.batch_release()
