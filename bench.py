@@ -76,6 +76,9 @@ def parse_args():
     ap.add_argument("--profile-steps", type=int, default=10)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0, help="target seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=("swarm", "ensemble"), default="swarm",
+                    help="swarm: the 2048x1024 bubble swarm (default); ensemble: 256 independent cases in batches")
+    ap.add_argument("--cases", type=int, default=256)
     return ap.parse_args()
 
 
@@ -221,8 +224,50 @@ def load_traffic():
     return out
 
 
+def ensemble_config(wls, ws):
+    from collections import Counter
+    grids = Counter(f"{w.ny}x{w.nx}" for w in wls)
+    return {"workload": f"ensemble_{len(wls)}", "cases": len(wls), "grids_ny_x_nx": dict(grids), "seed": 0,
+            "We": "log-U[1,100]", "Re": "log-U[10,100]", "denr": "log-U[1e-3,1e-1]", "visr": 0.1, "Fr": 1.0,
+            "cfl": wls[0].coef_dt_adv, "parallelism": f"replicas{ws}",
+            "l2": "working set (~4 GB) larger than L2, no flush"}
+
+
+def cpu_ensemble(wls, seconds_cap):
+    """the CPU port on every 8th case (one warm step, then timed steps until
+    the cap); returns (Mcell-steps/s, threads, case-steps, seconds)"""
+    import oracle
+    orc = oracle.Oracle()
+    orc.set_threads(os.cpu_count() or 1)
+    orc.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
+    sample = wls[::8]
+    sts = [make_state(w, orc) for w in sample]
+    for st in sts:
+        orc.integrate(st)
+    cells, done, t0 = 0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds_cap:
+        for w, st in zip(sample, sts):
+            orc.integrate(st)
+            cells += w.cells
+            done += 1
+    el = time.perf_counter() - t0
+    return cells / el / 1e6, orc.threads(), done, el
+
+
 def reference_arm(args, ws, rank):
     if rank != 0:
+        return
+    if args.workload == "ensemble":
+        from simplebubblyflowsolver_gb300 import ic
+        wls = ic.ensemble(args.cases, seed=0)
+        val, threads, done, el = cpu_ensemble(wls, seconds_cap=60.0)
+        line = {"metric": METRIC, "value": round(val, 4), "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+                "steps": done, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": ensemble_config(wls, 1),
+                "cpu_baseline": {"value": round(val, 4), "unit": METRIC, "cores": threads, "kind": "port",
+                                 "sample": f"{done} case-steps over every 8th case, {el:.1f} s"},
+                "e2e": {"value": round(val, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     wl = workload(args)
     # warm-up steps then K timed steps, capped so the run stays within minutes
@@ -249,6 +294,10 @@ def main():
     build_library()
     lib = load_library()
     lib.set_device(local)
+    if args.workload == "ensemble":
+        run_ensemble(args, lib, dist, ws, rank, local)
+        dist.close()
+        return
     wl = workload(args)
     lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
     st = make_state(wl, lib)
@@ -328,6 +377,81 @@ def main():
                 "dt_last": dt_last}
         print(json.dumps(line), flush=True)
     dist.close()
+
+
+def run_ensemble(args, lib, dist, ws, rank, local):
+    """256 independent cases (three grids, random physics) advanced together:
+    every kernel of the step runs all cases of one grid in one launch"""
+    from simplebubblyflowsolver_gb300 import SYNC_NONE, SYNC_STATE, ic
+    wls = ic.ensemble(args.cases, seed=0)
+    lib.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
+    sts = [make_state(w, lib) for w in wls]
+    cells = sum(w.cells for w in wls)
+    lib.set_sync_mode(SYNC_NONE)
+    lib.integrate_batch(sts)
+    lib.run_batch_steps_timed(args.warmup)
+    dist.barrier()
+    with ClockSampler(local) as clk:
+        ms = lib.run_batch_steps_timed(args.steps)
+    dist.barrier()
+    t_max = dist.max(ms / 1e3)
+    value = ws * cells * args.steps / t_max / 1e6
+    clocks = clk.summary()
+    groups = lib.batch_groups()
+
+    # per-kernel shares (eager, events on each group's stream; groups overlap,
+    # so the per-class sums are upper bounds of the class's wall time)
+    prof = lib.profile_batch_steps(args.profile_steps)
+    total = sum(v[0] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    # a launch covers all cases of one group: over the profiled steps the
+    # class moved ALG * 8 B * (all cells) once per launch round of the groups
+    alg_total = ALG_DOUBLES_PER_CELL[dom] * 8 * cells * dom_n / len(groups)
+    achieved = alg_total / (dom_ms / 1e3) / 1e9
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    hbm_peak = peaks.get("hbm_gbs", HBM_FALLBACK_GBS)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                "peak_source": "measured" if peaks else "fallback",
+                "alg_bytes_per_launch": round(alg_total / dom_n),
+                "avg_launch_ms": round(dom_ms / dom_n, 4), "share": round(dom_ms / total, 4),
+                "shares": {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+                "note": "all cases of the dominant kernel class per step / summed event time of its launches"}
+    roofline["fp64_peak_gflops"] = round(lib.measure_fp64_peak(), 1)
+
+    # end to end: sbfs_integrate_batch with page-locked host state of every case
+    lib.set_sync_mode(SYNC_STATE)
+    for st in sts:
+        lib.pin_host_state(st)
+    lib.integrate_batch(sts)
+    ne = max(2, min(args.e2e_steps, args.steps) // 10)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ne):
+        lib.integrate_batch(sts)
+    t_e2e = dist.max(time.perf_counter() - t0)
+    for st in sts:
+        lib.unpin_host_state(st)
+    h2d = sum(sum(st.interior_rows(s).nbytes for s in ("ux", "uy", "p", "psi0", "vof")) for st in sts)
+    d2h = h2d + sum(st.interior_rows("psi1").nbytes for st in sts) + len(sts) * 8 * 65
+    e2e = {"value": round(ws * cells * ne / t_e2e / 1e6, 4), "unit": METRIC, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "steps": ne}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        val, threads, done, el = cpu_ensemble(wls, seconds_cap=args.cpu_sample_s)
+        cpu = {"value": round(val, 4), "unit": METRIC, "cores": threads, "kind": "port",
+               "sample": f"{done} case-steps over every 8th case, {el:.1f} s"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(ensemble_config(wls, ws), groups=groups), "e2e": e2e, "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": lib.kernels_per_step() * len(groups) * args.steps}
+        print(json.dumps(line), flush=True)
+    lib.batch_release()
 
 
 if __name__ == "__main__":

@@ -198,6 +198,9 @@ int sbfs_run_batch_steps_timed(int nsteps, float *ms);
 /* copy the device-resident batch back into the callers' structs */
 int sbfs_batch_sync_to_host(int n, const domain_t *const *domains, fluid_t *const *fluids,
                             interface_t *const *interfaces);
+/* per-kernel-class device time (ms) and launches of nsteps eager steps of
+ * the resident batch (classes as sbfs_kernel_name) */
+int sbfs_profile_batch_steps(int nsteps, float *ms_per_class, int *launches_per_class);
 /* number of grid groups and cases per group of the current batch */
 int sbfs_batch_groups(int *ngroups, int *cases_per_group);
 int sbfs_batch_release(void);

@@ -190,6 +190,15 @@ class GpuLibrary(ReferenceAPI):
         self.lib.sbfs_batch_sync_to_host.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         self._ext("sbfs_batch_sync_to_host", n, d, f, i)
 
+    def profile_batch_steps(self, nsteps: int) -> dict:
+        """{kernel name: (total ms, launches)} of nsteps eager steps of the resident batch"""
+        n = self.lib.sbfs_kernel_classes()
+        ms = (C.c_float * n)()
+        cnt = (C.c_int * n)()
+        self.lib.sbfs_profile_batch_steps.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+        self._ext("sbfs_profile_batch_steps", nsteps, ms, cnt)
+        return {self.lib.sbfs_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n)}
+
     def batch_groups(self):
         ng = C.c_int(0)
         cases = (C.c_int * 64)()

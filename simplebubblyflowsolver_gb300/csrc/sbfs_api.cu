@@ -1116,6 +1116,36 @@ int sbfs_batch_sync_to_host(int n, const domain_t *const *domains, fluid_t *cons
   return 0;
 }
 
+// per-kernel-class device time of nsteps eager steps of the resident batch
+int sbfs_profile_batch_steps(int nsteps, float *ms_per_class, int *launches_per_class) {
+  Batch *b = g_batch.get();
+  if (!b) return fail("no batch on the device: call sbfs_integrate_batch first");
+  for (auto &c : b->groups)
+    if (!c->resident) return fail("the batch's state is not on the device");
+  g_prof.on = true;
+  g_prof.used = 0;
+  g_prof.marks.clear();
+  int rc = 0;
+  for (int k = 0; k < nsteps && !rc; ++k)
+    for (auto &c : b->groups)
+      if (!rc) rc = launch_step(*c);
+  g_prof.on = false;
+  if (rc) return 1;
+  for (auto &c : b->groups)
+    if (sync(*c)) return 1;
+  for (int k = 0; k < KC_COUNT; ++k) {
+    ms_per_class[k] = 0.f;
+    launches_per_class[k] = 0;
+  }
+  for (auto &mk : g_prof.marks) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, mk.second.first, mk.second.second));
+    ms_per_class[mk.first] += ms;
+    launches_per_class[mk.first] += 1;
+  }
+  return batch_read_dt(*b, (int)b->group_of.size(), nullptr);
+}
+
 int sbfs_batch_groups(int *ngroups, int *cases) {
   Batch *b = g_batch.get();
   *ngroups = b ? (int)b->groups.size() : 0;

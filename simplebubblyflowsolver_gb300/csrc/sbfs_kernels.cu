@@ -53,15 +53,11 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, c
                                                   double *__restrict__ den, double *__restrict__ visux,
                                                   double *__restrict__ visuy, double *__restrict__ dvof) {
   const Phys ph = zphys(g, ph0);
-  vof = zp(vof, g.cs1);
-  den = zp(den, g.cs1);
-  visux = zp(visux, g.cs1);
-  visuy = zp(visuy, g.cs1);
-  dvof = zp(dvof, g.cs2);
   const int I = blockIdx.x * BX + threadIdx.x;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
-  const int r = J - 1, rm = wrap(J - 1, g.ny);
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
   const double v = vof[ix(g, r, I)];
   if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.denr - 1., v, 1.), ph.den_lo, ph.den_hi);
   if (VIS) {
@@ -179,20 +175,11 @@ __global__ void __launch_bounds__(BX *BY)
                  const double *__restrict__ curv, double *__restrict__ fluxx, double *__restrict__ fluxy,
                  double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
   const Phys ph = zphys(g, ph0);
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  vof = zp(vof, g.cs1);
-  normal = zp(normal, g.cs3);
-  den0 = zp(den0, g.cs1);
-  curv = zp(curv, g.cs1);
-  fluxx = zp(fluxx, g.cs1);
-  fluxy = zp(fluxy, g.cs1);
-  ifrcx = zp(ifrcx, g.cs1);
-  ifrcy = zp(ifrcy, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
-  const int r = J - 1, rm = wrap(J - 1, g.ny);
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
   const double v0 = vof[ix(g, r, I)];
   const double vxm = vof[ix(g, r, I - 1)];
   const double vym = vof[ix(g, rm, I)];
@@ -274,17 +261,15 @@ __global__ void __launch_bounds__(BX *BY)
 __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const double *__restrict__ vof,
                                                       const double *__restrict__ dvof, double *__restrict__ curv,
                                                       int *__restrict__ list, int *__restrict__ count) {
-  vof = zp(vof, g.cs1);
-  dvof = zp(dvof, g.cs2);
-  curv = zp(curv, g.cs1);
-  list = zp(list, (size_t)g.nx * g.ny);
-  count = zp(count, 1);
+  list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
+  count += (size_t)blockIdx.z * (1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   const bool in = I <= g.nx && J <= g.ny;
   bool itf = false;
   if (in) {
-    const int r = J - 1, rp = wrap(J + 1, g.ny);
+    const int zr = blockIdx.z * g.ny;
+    const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
     const double2 *dv = reinterpret_cast<const double2 *>(dvof);
     const size_t q = g.p2 / 2;
     const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
@@ -316,21 +301,16 @@ __global__ void __launch_bounds__(256)
     k_interface_cells(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
                       const double *__restrict__ vof, const double *__restrict__ dvof, const int *__restrict__ list,
                       const int *__restrict__ count, double *__restrict__ fluxx, double *__restrict__ fluxy) {
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  vof = zp(vof, g.cs1);
-  dvof = zp(dvof, g.cs2);
-  list = zp(list, (size_t)g.nx * g.ny);
-  count = zp(count, 1);
-  fluxx = zp(fluxx, g.cs1);
-  fluxy = zp(fluxy, g.cs1);
+  list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
+  count += (size_t)blockIdx.z * (1);
   const int n = *count;
+  const int zr = blockIdx.z * g.ny;  // first row of this case
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
   const size_t q = g.p2 / 2;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int id = list[t];
-    const int r = id / g.nx, I = id - r * g.nx + 1;
-    const int J = r + 1, rp = wrap(J + 1, g.ny);
+    const int r0 = id / g.nx, I = id - r0 * g.nx + 1;
+    const int J = r0 + 1, r = r0 + zr, rp = wrap(J + 1, g.ny) + zr;
     const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
     const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
     const double mx = (((d00.x + d10.x) + d01.x) + d11.x) * m.ihxxc[I];
@@ -365,21 +345,12 @@ __global__ void __launch_bounds__(BX *BY)
                   const double *__restrict__ src_b, const double *__restrict__ ux, const double *__restrict__ uy,
                   double *__restrict__ mfx, double *__restrict__ mfy, double *__restrict__ den1) {
   const Phys ph = zphys(g, ph0);
-  sc = zp(sc, kScalars);
-  vof = zp(vof, g.cs1);
-  fluxx = zp(fluxx, g.cs1);
-  fluxy = zp(fluxy, g.cs1);
-  src_a = zp(src_a, g.cs1);
-  src_b = zp(src_b, g.cs1);
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  mfx = zp(mfx, g.cs1);
-  mfy = zp(mfy, g.cs1);
-  den1 = zp(den1, g.cs1);
+  sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
-  const int r = J - 1, rp = wrap(J + 1, g.ny);
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
   const double fxm = fluxx[ix(g, r, I - 1)], fxp = fluxx[ix(g, r, I)];
   const double fym = fluxy[ix(g, r, I)], fyp = fluxy[ix(g, rp, I)];
   const double s = fma(m.ihxxc[I], fxm - fxp, g.ihy * (fym - fyp));
@@ -430,17 +401,11 @@ __global__ void __launch_bounds__(BX *BY)
     k_stress(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
              const double *__restrict__ visux, const double *__restrict__ visuy, double *__restrict__ txx,
              double *__restrict__ txy, double *__restrict__ tyy) {
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  visux = zp(visux, g.cs1);
-  visuy = zp(visuy, g.cs1);
-  txx = zp(txx, g.cs1);
-  txy = zp(txy, g.cs1);
-  tyy = zp(tyy, g.cs1);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
-  const int r = J - 1, rm = wrap(J - 1, g.ny), rp = wrap(J + 1, g.ny);
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
   const double u0 = ux[ix(g, r, I - 1)];
   const double vx0 = visux[ix(g, r, I - 1)];
   const double w0 = uy[ix(g, r, I)];
@@ -478,34 +443,13 @@ __global__ void __launch_bounds__(BX *BY)
               double *__restrict__ sxg, double *__restrict__ sya, const double *__restrict__ syb,
               double *__restrict__ syg, double *__restrict__ ex, double *__restrict__ ey) {
   const Phys ph = zphys(g, ph0);
-  const double *__restrict__ nuf = zp(m.nuf, (size_t)g.cm);
-  sc = zp(sc, kScalars);
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  ux_out = zp(ux_out, g.cs1);
-  uy_out = zp(uy_out, g.cs1);
-  mfx = zp(mfx, g.cs1);
-  mfy = zp(mfy, g.cs1);
-  txx = zp(txx, g.cs1);
-  txy = zp(txy, g.cs1);
-  tyy = zp(tyy, g.cs1);
-  p = zp(p, g.cs1);
-  ifrcx = zp(ifrcx, g.cs1);
-  ifrcy = zp(ifrcy, g.cs1);
-  den0 = zp(den0, g.cs1);
-  den1 = zp(den1, g.cs1);
-  sxa = zp(sxa, g.cs1);
-  sxb = zp(sxb, g.cs1);
-  sxg = zp(sxg, g.cs1);
-  sya = zp(sya, g.cs1);
-  syb = zp(syb, g.cs1);
-  syg = zp(syg, g.cs1);
-  ex = zp(ex, g.cs1);
-  ey = zp(ey, g.cs1);
+  const double *__restrict__ nuf = m.nuf + (size_t)blockIdx.z * g.cm;
+  sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
-  const int r = J - 1, rm = wrap(J - 1, g.ny), rp = wrap(J + 1, g.ny);
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
   const double adt = sc[sc_adt(k)], bdt = sc[sc_bdt(k)], gdt = sc[sc_gdt(k)];
   const double rref = ph.refden;
   const double nuy = ph.nu * g.ihy;
@@ -657,13 +601,8 @@ __global__ void __launch_bounds__(256)
     k_poisson_fwd(Grid g, const double *__restrict__ sc, int k, const double *__restrict__ ux,
                   const double *__restrict__ uy, const double *__restrict__ psi, const double *__restrict__ ex,
                   const double *__restrict__ ey, const double2 *__restrict__ tw, double2 *__restrict__ spec) {
-  sc = zp(sc, kScalars);
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  psi = zp(psi, g.cs1);
-  ex = zp(ex, g.cs1);
-  ey = zp(ey, g.cs1);
-  spec = zp(spec, g.css);
+  sc += (size_t)blockIdx.z * (kScalars);
+  spec += (size_t)blockIdx.z * (g.css);
   extern __shared__ double2 smem[];
   const int ny = g.ny, M = ny >> 1;
   double2 *A = smem, *B = smem + W * M;
@@ -675,13 +614,15 @@ __global__ void __launch_bounds__(256)
     const int I = I0 + c;
     double val = 0.;
     if (I <= g.nx) {
-      const int rm = r == 0 ? ny - 1 : r - 1, rp = r == ny - 1 ? 0 : r + 1;
-      const double ps = psi[ix(g, r, I)];
+      // global rows of this case (the case's rows follow each other)
+      const int zr = blockIdx.z * ny;
+      const int rg = r + zr, rm = (r == 0 ? ny - 1 : r - 1) + zr, rp = (r == ny - 1 ? 0 : r + 1) + zr;
+      const double ps = psi[ix(g, rg, I)];
       // (e dpsi) differences across the cell; the wall faces have dpsi = 0
-      const double X = fma(ex[ix(g, r, I)], psi[ix(g, r, I + 1)] - ps, -ex[ix(g, r, I - 1)] * (ps - psi[ix(g, r, I - 1)]));
-      const double Y = fma(ey[ix(g, rp, I)], psi[ix(g, rp, I)] - ps, -ey[ix(g, r, I)] * (ps - psi[ix(g, rm, I)]));
-      const double dux = ux[ix(g, r, I)] - ux[ix(g, r, I - 1)];
-      const double duy = uy[ix(g, rp, I)] - uy[ix(g, r, I)];
+      const double X = fma(ex[ix(g, rg, I)], psi[ix(g, rg, I + 1)] - ps, -ex[ix(g, rg, I - 1)] * (ps - psi[ix(g, rg, I - 1)]));
+      const double Y = fma(ey[ix(g, rp, I)], psi[ix(g, rp, I)] - ps, -ey[ix(g, rg, I)] * (ps - psi[ix(g, rm, I)]));
+      const double dux = ux[ix(g, rg, I)] - ux[ix(g, rg, I - 1)];
+      const double duy = uy[ix(g, rp, I)] - uy[ix(g, rg, I)];
       val = fma(pdx, dux, fma(pdy, duy, fma(pax, X, pay * Y)));
     }
     Ad[c * ny + r] = val;
@@ -705,8 +646,7 @@ __global__ void __launch_bounds__(256)
 template <int W>
 __global__ void __launch_bounds__(256)
     k_poisson_inv(Grid g, const double2 *__restrict__ tw, const double2 *__restrict__ spec, double *__restrict__ psi) {
-  spec = zp(spec, g.css);
-  psi = zp(psi, g.cs1);
+  spec += (size_t)blockIdx.z * (g.css);
   extern __shared__ double2 smem[];
   const int ny = g.ny, M = ny >> 1, M1 = M + 1;
   double2 *A = smem, *B = smem + W * M;
@@ -734,9 +674,10 @@ __global__ void __launch_bounds__(256)
     const int I = I0 + c;
     if (I > g.nx) continue;
     const double v = xd[c * ny + r];
-    psi[ix(g, r, I)] = v;
-    if (I == 1) psi[ix(g, r, 0)] = v;
-    if (I == g.nx) psi[ix(g, r, g.nx + 1)] = v;
+    const int rg = r + (int)blockIdx.z * ny;
+    psi[ix(g, rg, I)] = v;
+    if (I == 1) psi[ix(g, rg, 0)] = v;
+    if (I == g.nx) psi[ix(g, rg, g.nx + 1)] = v;
   }
 }
 
@@ -756,7 +697,6 @@ __global__ void __launch_bounds__(256)
 // Shared memory: per system a planar array with an odd lane stride S.
 __global__ void __launch_bounds__(256)
     k_poisson_tdm(Grid g, int MB, int L, int S, const double4_32a *__restrict__ fac, double2 *__restrict__ spec) {
-  spec = zp(spec, g.css);
   extern __shared__ double2 smem_d2[];
   double *sm = reinterpret_cast<double *>(smem_d2);
   const int nx = g.nx, M1 = g.ny / 2 + 1;
@@ -768,7 +708,7 @@ __global__ void __launch_bounds__(256)
     const int i = t / nm, q = t - i * nm;
     const int at = (i / L) * S + (i % L);
     double2 v = make_double2(0., 0.);
-    if (i < nx) v = spec[(size_t)i * M1 + m0 + q];
+    if (i < nx) v = spec[(size_t)blockIdx.z * g.css + (size_t)i * M1 + m0 + q];
     sm[(2 * q) * sys_len + at] = v.x;
     sm[(2 * q + 1) * sys_len + at] = v.y;
   }
@@ -837,7 +777,7 @@ __global__ void __launch_bounds__(256)
   for (int t = threadIdx.x; t < nx * nm; t += blockDim.x) {
     const int i = t / nm, q = t - i * nm;
     const int at = (i / L) * S + (i % L);
-    spec[(size_t)i * M1 + m0 + q] = make_double2(sm[(2 * q) * sys_len + at], sm[(2 * q + 1) * sys_len + at]);
+    spec[(size_t)blockIdx.z * g.css + (size_t)i * M1 + m0 + q] = make_double2(sm[(2 * q) * sys_len + at], sm[(2 * q + 1) * sys_len + at]);
   }
 }
 
@@ -854,18 +794,12 @@ __global__ void __launch_bounds__(BX *BY)
     k_correct(Grid g, Metrics m, const double *__restrict__ sc, int k, double *__restrict__ ux,
               double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ psio,
               const double *__restrict__ ex, const double *__restrict__ ey, double *__restrict__ p) {
-  sc = zp(sc, kScalars);
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  psin = zp(psin, g.cs1);
-  psio = zp(psio, g.cs1);
-  ex = zp(ex, g.cs1);
-  ey = zp(ey, g.cs1);
-  p = zp(p, g.cs1);
+  sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
-  const int r = J - 1, rm = wrap(J - 1, g.ny);
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
   const double cnew = sc[sc_cnew(k)], cold = sc[sc_cold(k)];
   const double pn0 = psin[ix(g, r, I)], po0 = psio[ix(g, r, I)];
   if (I >= 2) {
@@ -927,11 +861,9 @@ __global__ void __launch_bounds__(BX *BY)
                 double dt_fixed, double coef_adv) {
   const Phys ph = zphys(g, ph0);
   if (g.phys) dt_fixed = ph.dtfix;
-  ux = zp(ux, g.cs1);
-  uy = zp(uy, g.cs1);
-  acc = zp(acc, (size_t)g.nx + 8);
-  sc = zp(sc, kScalars);
-  status = zp(status, 1);
+  acc += (size_t)blockIdx.z * ((size_t)g.nx + 8);
+  sc += (size_t)blockIdx.z * (kScalars);
+  status += (size_t)blockIdx.z * (1);
   __shared__ unsigned long long colmax[BY][BX];
   __shared__ unsigned long long ymax[BY * BX];
   __shared__ bool last;
@@ -939,7 +871,7 @@ __global__ void __launch_bounds__(BX *BY)
   unsigned long long mx = 0ULL, my = 0ULL;
   if (I <= g.nx) {
     for (int J = blockIdx.y * BY + threadIdx.y + 1; J <= g.ny; J += gridDim.y * BY) {
-      const int r = J - 1;
+      const int r = J - 1 + (int)blockIdx.z * g.ny;
       if (I >= 2) {
         const unsigned long long b = (unsigned long long)dbits(ux[ix(g, r, I - 1)]) & kAbsMask;
         mx = b > mx ? b : mx;
