@@ -190,7 +190,8 @@ const char *sbfs_noalloc_last_error(void);
  * in one launch, and groups run on separate streams.  The sync mode applies
  * as for integrate(); in SBFS_SYNC_NONE the cases stay on the device between
  * calls as long as the same fluid/interface pointers are passed in the same
- * order.  Learned curvature is not applied to batches. */
+ * order.  The curvature model (sbfs_set_curvature_model) applies to every
+ * case of a batch. */
 int sbfs_integrate_batch(int n, const domain_t *const *domains, fluid_t *const *fluids,
                          interface_t *const *interfaces, double *dts);
 /* advance the device-resident batch nsteps steps; *ms from CUDA events */

@@ -533,7 +533,7 @@ void enqueue_substage(Ctx &c, int k) {
   const double *sc = b.scalars;
   timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
-  const bool learned = g_curv_model && c.nc == 1;
+  const bool learned = g_curv_model != 0;
   if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
   timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
   timed(c, KC_FLUX_FORCE,

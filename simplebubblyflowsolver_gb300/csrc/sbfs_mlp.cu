@@ -379,27 +379,31 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
   __nv_bfloat16(*xs)[16][NF] = reinterpret_cast<__nv_bfloat16(*)[16][NF]>(smraw + sizeof(SmemW));
   load_weights(w, params);
   __syncthreads();
+  // batches: case blockIdx.z has its own list and rows z ny .. z ny + ny - 1
+  list += (size_t)blockIdx.z * g.nx * g.ny;
+  count += blockIdx.z;
+  const int zr = blockIdx.z * g.ny;
   const int n = *count;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
   const size_t q = g.p2 / 2;
   int nused = 0;
-  for (int r0 = (blockIdx.x * nwarps + warp) * 16; r0 < n; r0 += gridDim.x * nwarps * 16) {
+  for (int e0 = (blockIdx.x * nwarps + warp) * 16; e0 < n; e0 += gridDim.x * nwarps * 16) {
     // lanes 0..15 build one feature row each
     bool ok = false;
     int cell = -1;
     if (lane < 16) {
-      const int e = r0 + lane;
+      const int e = e0 + lane;
       float fr[NF];
       for (int c = 0; c < NF; ++c) fr[c] = 0.f;
       if (e < n) {
         cell = list[e];
-        const int r = cell / g.nx, I = cell - r * g.nx + 1;
-        const int J = r + 1;
+        const int rc = cell / g.nx, I = cell - rc * g.nx + 1;
+        const int J = rc + 1, r = rc + zr;
         ok = true;
         for (int dy = -1; dy <= 1; ++dy) {
-          const int rr = wrap(J + dy, g.ny);
+          const int rr = wrap(J + dy, g.ny) + zr;
           for (int dx = -1; dx <= 1; ++dx) {
             const double v = vof[(size_t)rr * g.p1 + I + dx];
             ok = ok && v >= 0. && v <= 1.;
@@ -409,7 +413,7 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
         const double phi = vof[(size_t)r * g.p1 + I];
         ok = ok && phi >= 0.01 && phi <= 0.99;
         // the solver's cell normal: sum of the four unit corner normals, normalised
-        const int rp = wrap(J + 1, g.ny);
+        const int rp = wrap(J + 1, g.ny) + zr;
         const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
         const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
         const double mx = ((d00.x + d10.x) + d01.x) + d11.x, my = ((d00.y + d10.y) + d01.y) + d11.y;
@@ -431,8 +435,8 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
     if (lane < 16 && ok) {
       const float a = fabsf(o);
       if (a >= 0.015f && a <= 0.55f) {
-        const int r = cell / g.nx, I = cell - r * g.nx + 1;
-        curv[(size_t)r * g.p1 + I] = (double)o * g.idx;
+        const int rc = cell / g.nx, I = cell - rc * g.nx + 1;
+        curv[(size_t)(rc + zr) * g.p1 + I] = (double)o * g.idx;
         ++nused;
       }
     }
@@ -488,7 +492,8 @@ size_t smem_infer() { return sizeof(SmemW) + sizeof(__nv_bfloat16) * 8 * 16 * NF
 namespace sbfs {
 bool mlp_ready() { return g_params != nullptr; }
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b) {
-  k_mlp_curv<<<2 * 152, 256, smem_infer(), s>>>(g, g_params, b.vof, b.dvof, b.ilist, b.icount, b.curv, g_used);
+  k_mlp_curv<<<dim3(max(2, (2 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, smem_infer(), s>>>(
+      g, g_params, b.vof, b.dvof, b.ilist, b.icount, b.curv, g_used);
 }
 }  // namespace sbfs
 

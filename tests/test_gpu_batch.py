@@ -122,3 +122,30 @@ def test_timed_batch_runs(libs):
     finally:
         gpu.set_sync_mode(SYNC_STATE)
         gpu.batch_release()
+
+
+@pytest.mark.gpu
+def test_batch_learned_curvature_equals_single_cases(libs):
+    """the learned closure in a batch: each case as it steps alone"""
+    from simplebubblyflowsolver_gb300 import learned_curvature as L
+    gpu, orc = libs
+    wls = ic.ensemble(6, seed=6, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    batch = [clone(s) for s in st0]
+    alone = [clone(s) for s in st0]
+    p = L.init_params(3)
+    p[-1] = 0.05  # a bias that puts many outputs inside the closure's range
+    gpu.mlp_set_params(p)
+    gpu.set_curvature_model(1)
+    try:
+        gpu.mlp_take_usage()
+        for _ in range(3):
+            dts = gpu.integrate_batch(batch)
+            for k, st in enumerate(alone):
+                assert gpu.integrate(st) == dts[k]
+        assert gpu.mlp_take_usage() > 0
+    finally:
+        gpu.set_curvature_model(0)
+    for k, (a, b) in enumerate(zip(batch, alone)):
+        for s in SLOTS:
+            assert np.array_equal(a.field(s), b.field(s)), (k, s)
