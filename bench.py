@@ -79,6 +79,9 @@ def parse_args():
     ap.add_argument("--workload", choices=("swarm", "ensemble"), default="swarm",
                     help="swarm: the 2048x1024 bubble swarm (default); ensemble: 256 independent cases in batches")
     ap.add_argument("--cases", type=int, default=256)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--curvature", choices=("plain", "learned"), default="plain",
+                    help="learned: train the closure on the GPU first, then time the step with it")
     return ap.parse_args()
 
 
@@ -294,8 +297,17 @@ def main():
     build_library()
     lib = load_library()
     lib.set_device(local)
+    lib.set_autotune(not args.no_autotune)
+    learned = None
+    if args.curvature == "learned":
+        from simplebubblyflowsolver_gb300 import learned_curvature as L
+        t0 = time.perf_counter()
+        _, params, hist = L.train_default(lib, seed=0)
+        learned = {"train_s": round(time.perf_counter() - t0, 1), "final_loss": hist[-1]}
+        lib.mlp_set_params(params)
+        lib.set_curvature_model(1)
     if args.workload == "ensemble":
-        run_ensemble(args, lib, dist, ws, rank, local)
+        run_ensemble(args, lib, dist, ws, rank, local, learned)
         dist.close()
         return
     wl = workload(args)
@@ -372,14 +384,15 @@ def main():
         line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config_of(wl, args, ws), "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "config": dict(config_of(wl, args, ws), curvature=args.curvature), "e2e": e2e, "roofline": roofline,
+                "cpu_baseline": cpu, "learned_curvature": learned, "tiles": lib.tiles(),
                 "clocks": clocks, "gpu_launches": lib.kernels_per_step() * args.steps,
                 "dt_last": dt_last}
         print(json.dumps(line), flush=True)
     dist.close()
 
 
-def run_ensemble(args, lib, dist, ws, rank, local):
+def run_ensemble(args, lib, dist, ws, rank, local, learned=None):
     """256 independent cases (three grids, random physics) advanced together:
     every kernel of the step runs all cases of one grid in one launch"""
     from simplebubblyflowsolver_gb300 import SYNC_NONE, SYNC_STATE, ic
@@ -447,7 +460,9 @@ def run_ensemble(args, lib, dist, ws, rank, local):
         line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(ensemble_config(wls, ws), groups=groups), "e2e": e2e, "roofline": roofline,
+                "config": dict(ensemble_config(wls, ws), groups=groups, curvature=args.curvature),
+                "e2e": e2e, "roofline": roofline, "learned_curvature": learned,
+                "tiles": [lib.tiles(q) for q in range(len(groups))],
                 "cpu_baseline": cpu, "clocks": clocks,
                 "gpu_launches": lib.kernels_per_step() * len(groups) * args.steps}
         print(json.dumps(line), flush=True)

@@ -202,6 +202,16 @@ int sbfs_batch_sync_to_host(int n, const domain_t *const *domains, fluid_t *cons
 /* per-kernel-class device time (ms) and launches of nsteps eager steps of
  * the resident batch (classes as sbfs_kernel_name) */
 int sbfs_profile_batch_steps(int nsteps, float *ms_per_class, int *launches_per_class);
+/* autotuner of the launch shapes (default off): when on, the first step of
+ * each device context (the single case, every batch group) times candidate
+ * block shapes of the stencil kernels, Poisson transform widths and
+ * tridiagonal batching on the context's own state (restored after every
+ * trial) and keeps the fastest per kernel; results do not change */
+int sbfs_set_autotune(int on);
+/* shapes in use (group -1: the single-case context): bx[7], by[7] for
+ * props, curvature list, flux/force, vof advance, stress, predict,
+ * correct; the Poisson transform width and wavenumbers per tridiagonal block */
+int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb);
 /* number of grid groups and cases per group of the current batch */
 int sbfs_batch_groups(int *ngroups, int *cases_per_group);
 int sbfs_batch_release(void);

@@ -199,6 +199,24 @@ class GpuLibrary(ReferenceAPI):
         self._ext("sbfs_profile_batch_steps", nsteps, ms, cnt)
         return {self.lib.sbfs_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n)}
 
+    def set_autotune(self, on: bool):
+        self._ext("sbfs_set_autotune", 1 if on else 0)
+
+    def tiles(self, group: int = -1) -> dict:
+        """launch shapes in use (group -1: the single-case context)"""
+        bx = (C.c_int * 7)()
+        by = (C.c_int * 7)()
+        fw = C.c_int(0)
+        mb = C.c_int(0)
+        self.lib.sbfs_tiles.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int)]
+        self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb))
+        names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_stress", "k_predict", "k_correct"]
+        out = {n: f"{bx[k]}x{by[k]}" for k, n in enumerate(names)}
+        out["fft_cols"] = fw.value
+        out["tdm_modes"] = mb.value
+        return out
+
     def batch_groups(self):
         ng = C.c_int(0)
         cases = (C.c_int * 64)()

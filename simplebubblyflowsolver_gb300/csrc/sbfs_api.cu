@@ -85,6 +85,7 @@ struct Ctx {
   double *U[2], *V[2], *PSI[2], *DEN[2], *SX[2], *SY[2], *SV[2];
   int iu = 0, ipsi = 0, iden = 0, isrc = 0;
   bool resident = false;  // device holds the current state
+  bool tuned = false;     // launch shapes picked by the autotuner
   std::map<int, cudaGraphExec_t> graphs;
   // kernel arguments the graphs were captured with (physics, fixed dt, dt
   // safety factor); graphs are dropped when any of them changes
@@ -362,6 +363,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   g.cm = 0;
   g.phys = nullptr;
   Bufs &b = c->b;
+  b.tiles = default_tiles();
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
@@ -561,9 +563,110 @@ void enqueue_step(Ctx &c) {
   for (int k = 0; k < 3; ++k) enqueue_substage(c, k);
 }
 
+// ---- autotuner of the launch shapes (block shape of each stencil kernel,
+// columns per block of the Poisson transforms, wavenumbers per block of the
+// tridiagonal solves).  On the first step of a context it times each
+// candidate on the context's own state (saved before and put back after
+// every trial), two eager steps per candidate with CUDA events around every
+// launch, and keeps the fastest per kernel class.  Results do not depend on
+// the shapes.
+int g_autotune = 0;
+
+int autotune(Ctx &c) {
+  const size_t n = c.g.cs1 * c.nc;
+  double *live[6] = {c.U[c.iu], c.V[c.iu], c.b.p, c.PSI[c.ipsi], c.b.vof, c.DEN[c.iden]};
+  double *save[6] = {nullptr};
+  for (int q = 0; q < 6; ++q) {
+    CK(cudaMalloc(&save[q], n * sizeof(double)));
+    CK(cudaMemcpyAsync(save[q], live[q], n * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
+  }
+  const int iu = c.iu, ipsi = c.ipsi, iden = c.iden, isrc = c.isrc;
+  auto restore = [&]() -> int {
+    c.iu = iu;
+    c.ipsi = ipsi;
+    c.iden = iden;
+    c.isrc = isrc;
+    for (int q = 0; q < 6; ++q)
+      CK(cudaMemcpyAsync(live[q], save[q], n * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
+    return 0;
+  };
+  const unsigned short shapes[][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {32, 2}, {64, 2}, {16, 16}, {256, 1}};
+  const int nshape = sizeof(shapes) / sizeof(shapes[0]);
+  std::vector<int> fws, mbs;
+  for (int w : {2, 4, 8})
+    if (fft_w_fits(c.ny, w)) fws.push_back(w);
+  for (int mb : {1, 2, 4})
+    if (poisson_tdm_smem(c.nx) / poisson_tdm_modes(c.nx) * mb <= 200 * 1024) mbs.push_back(mb);
+  const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT,
+                               -1, -1, -1, TK_CORRECT, -1, -1};
+  Tiles best = c.b.tiles;
+  float best_ms[TK_COUNT], best_fft = 1e30f, best_tdm = 1e30f;
+  for (int k = 0; k < TK_COUNT; ++k) best_ms[k] = 1e30f;
+  const Tiles keep = c.b.tiles;
+  int rc = 0;
+  for (int t = 0; t < nshape && !rc; ++t) {
+    Tiles cand = keep;
+    for (int k = 0; k < TK_COUNT; ++k) {
+      cand.bx[k] = shapes[t][0];
+      cand.by[k] = shapes[t][1];
+    }
+    cand.fft_w = fws[t % fws.size()];
+    cand.tdm_mb = mbs[t % mbs.size()];
+    c.b.tiles = cand;
+    if (restore()) {
+      rc = 1;
+      break;
+    }
+    enqueue_step(c);  // warm-up of this shape
+    g_prof.on = true;
+    g_prof.used = 0;
+    g_prof.marks.clear();
+    for (int r = 0; r < 2; ++r) enqueue_step(c);
+    g_prof.on = false;
+    if (sync(c)) {
+      rc = 1;
+      break;
+    }
+    float ms[KC_COUNT] = {0.f};
+    for (auto &mk : g_prof.marks) {
+      float x = 0.f;
+      cudaEventElapsedTime(&x, mk.second.first, mk.second.second);
+      ms[mk.first] += x;
+    }
+    for (int kc = 0; kc < KC_COUNT; ++kc) {
+      const int tk = tk_of[kc];
+      if (tk >= 0 && ms[kc] < best_ms[tk]) {
+        best_ms[tk] = ms[kc];
+        best.bx[tk] = cand.bx[tk];
+        best.by[tk] = cand.by[tk];
+      }
+    }
+    const float fft = ms[KC_POISSON_FWD] + ms[KC_POISSON_INV];
+    if (fft < best_fft) {
+      best_fft = fft;
+      best.fft_w = cand.fft_w;
+    }
+    if (ms[KC_POISSON_TDM] < best_tdm) {
+      best_tdm = ms[KC_POISSON_TDM];
+      best.tdm_mb = cand.tdm_mb;
+    }
+  }
+  c.b.tiles = rc ? keep : best;
+  const int rr = restore();
+  const cudaError_t e = cudaStreamSynchronize(c.s);
+  for (int q = 0; q < 6; ++q) cudaFree(save[q]);
+  for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
+  c.graphs.clear();
+  c.tuned = true;
+  if (rc || rr) return 1;
+  if (e != cudaSuccess) return fail("autotune: %s", cudaGetErrorString(e));
+  return 0;
+}
+
 int role_key(const Ctx &c) { return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4); }
 
 int launch_step(Ctx &c) {
+  if (g_autotune && !c.tuned && c.resident && !g_prof.on && autotune(c)) return 1;
   if (!g_use_graphs || g_prof.on) {
     enqueue_step(c);
     CK(cudaGetLastError());
@@ -1144,6 +1247,28 @@ int sbfs_profile_batch_steps(int nsteps, float *ms_per_class, int *launches_per_
     launches_per_class[mk.first] += 1;
   }
   return batch_read_dt(*b, (int)b->group_of.size(), nullptr);
+}
+
+int sbfs_set_autotune(int on) {
+  g_autotune = on ? 1 : 0;
+  return 0;
+}
+
+// launch shapes in use: group -1 = the single-case context, else batch group
+int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb) {
+  Ctx *c = nullptr;
+  if (group < 0)
+    c = g_ctx.get();
+  else if (g_batch && group < (int)g_batch->groups.size())
+    c = g_batch->groups[group].get();
+  if (!c) return fail("no such context");
+  for (int k = 0; k < TK_COUNT; ++k) {
+    bx[k] = c->b.tiles.bx[k];
+    by[k] = c->b.tiles.by[k];
+  }
+  *fft_w = c->b.tiles.fft_w;
+  *tdm_mb = c->b.tiles.tdm_mb > 0 ? c->b.tiles.tdm_mb : poisson_tdm_modes(c->nx);
+  return 0;
 }
 
 int sbfs_batch_groups(int *ngroups, int *cases) {

@@ -40,6 +40,11 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
 dim3 grid2d(int ni, int nj, int nz = 1) { return dim3((ni + BX - 1) / BX, (nj + BY - 1) / BY, nz); }
+// grid of the block shape of kernel k
+dim3 tile_block(const Tiles &t, int k) { return dim3(t.bx[k], t.by[k]); }
+dim3 tile_grid(const Tiles &t, int k, int ni, int nj, int nz) {
+  return dim3((ni + t.bx[k] - 1) / t.bx[k], (nj + t.by[k] - 1) / t.by[k], nz);
+}
 
 // ---------------------------------------------------------------------------
 // density, viscosity, corner gradients of vof
@@ -53,8 +58,8 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, c
                                                   double *__restrict__ den, double *__restrict__ visux,
                                                   double *__restrict__ visuy, double *__restrict__ dvof) {
   const Phys ph = zphys(g, ph0);
-  const int I = blockIdx.x * BX + threadIdx.x;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
@@ -104,8 +109,8 @@ template <bool NORMAL, bool CURV, bool STORE_K>
 __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const double *__restrict__ vof,
                                                         const double *__restrict__ dvof, double *__restrict__ normal,
                                                         double *__restrict__ curv) {
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int r = J - 1, rp = wrap(J + 1, g.ny);
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
@@ -175,8 +180,8 @@ __global__ void __launch_bounds__(BX *BY)
                  const double *__restrict__ curv, double *__restrict__ fluxx, double *__restrict__ fluxy,
                  double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
   const Phys ph = zphys(g, ph0);
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
@@ -263,8 +268,8 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
                                                       int *__restrict__ list, int *__restrict__ count) {
   list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
   count += (size_t)blockIdx.z * (1);
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const bool in = I <= g.nx && J <= g.ny;
   bool itf = false;
   if (in) {
@@ -285,10 +290,11 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
     curv[ix(g, r, I)] = k;
     itf = !single_phase(vof[ix(g, r, I)]);
   }
-  // warp-aggregated append (a warp is 32 consecutive cells of one row)
+  // warp-aggregated append (a warp is 32 consecutive threads of the block,
+  // whatever its shape)
   const unsigned mask = __ballot_sync(0xffffffffu, itf);
   if (mask) {
-    const int lane = threadIdx.x & 31;
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
     const int leader = __ffs(mask) - 1;
     int base = 0;
     if (lane == leader) base = atomicAdd(count, __popc(mask));
@@ -346,8 +352,8 @@ __global__ void __launch_bounds__(BX *BY)
                   double *__restrict__ mfx, double *__restrict__ mfy, double *__restrict__ den1) {
   const Phys ph = zphys(g, ph0);
   sc += (size_t)blockIdx.z * (kScalars);
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
@@ -381,8 +387,8 @@ __global__ void __launch_bounds__(BX *BY)
 // vof flux -> mass flux in place (src/interface/mass_flux.c:10-58); I = 0..nx+1
 __global__ void k_mass_flux(Grid g, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
                             double *__restrict__ fluxx, double *__restrict__ fluxy) {
-  const int I = blockIdx.x * BX + threadIdx.x;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int r = J - 1;
   const double c = ph.denr - 1.;
@@ -401,8 +407,8 @@ __global__ void __launch_bounds__(BX *BY)
     k_stress(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
              const double *__restrict__ visux, const double *__restrict__ visuy, double *__restrict__ txx,
              double *__restrict__ txy, double *__restrict__ tyy) {
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
@@ -445,8 +451,8 @@ __global__ void __launch_bounds__(BX *BY)
   const Phys ph = zphys(g, ph0);
   const double *__restrict__ nuf = m.nuf + (size_t)blockIdx.z * g.cm;
   sc += (size_t)blockIdx.z * (kScalars);
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
@@ -795,8 +801,8 @@ __global__ void __launch_bounds__(BX *BY)
               double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ psio,
               const double *__restrict__ ex, const double *__restrict__ ey, double *__restrict__ p) {
   sc += (size_t)blockIdx.z * (kScalars);
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
@@ -833,8 +839,8 @@ __global__ void __launch_bounds__(BX *BY)
 
 // pressure update alone (fine-grained entry point); I = 1..nx
 __global__ void k_pressure(Grid g, const double *__restrict__ psin, double *__restrict__ p) {
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int r = J - 1;
   const double pv = p[ix(g, r, I)] + psin[ix(g, r, I)];
@@ -962,8 +968,8 @@ __global__ void __launch_bounds__(BX *BY)
 // from a density field, as k_predict stores it (fine-grained entry points)
 __global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, double *__restrict__ ex,
                               double *__restrict__ ey) {
-  const int I = blockIdx.x * BX + threadIdx.x + 1;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int r = J - 1, rm = wrap(J - 1, g.ny);
   ex[ix(g, r, I - 1)] = fma(ph.refden, rcp_nr(half_sum(den[ix(g, r, I - 1)], den[ix(g, r, I)])), -1.);
@@ -1064,8 +1070,8 @@ __global__ void __launch_bounds__(BX *BY) k_diag_final(const double *__restrict_
 __global__ void k_stats_collect(Grid g, const double *__restrict__ ux, const double *__restrict__ uy,
                                 const double *__restrict__ vof, double *__restrict__ ux1, double *__restrict__ uy1,
                                 double *__restrict__ vof1) {
-  const int I = blockIdx.x * BX + threadIdx.x;
-  const int J = blockIdx.y * BY + threadIdx.y + 1;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int r = J - 1;
   if (I >= 1) ux1[ix(g, r, I - 1)] += ux[ix(g, r, I - 1)];
@@ -1168,21 +1174,42 @@ cudaError_t nr_check(const double *x, double *rcp, double *rsq, int n) {
 // ===========================================================================
 
 int poisson_fft_cols(int) { return kFftCols; }
-size_t poisson_fft_smem(int ny) { return sizeof(double2) * 2 * kFftCols * (size_t)(ny / 2); }
+size_t poisson_fft_smem(int ny, int w) { return sizeof(double2) * 2 * w * (size_t)(ny / 2); }
+bool fft_w_fits(int ny, int w) { return poisson_fft_smem(ny, w) <= 227 * 1024; }
+
+Tiles default_tiles() {
+  Tiles t{};
+  for (int k = 0; k < TK_COUNT; ++k) {
+    t.bx[k] = BX;
+    t.by[k] = BY;
+  }
+  t.fft_w = kFftCols;
+  t.tdm_mb = 0;
+  return t;
+}
 int tdm_chunk(int nx) { return (nx + 31) / 32; }
 int tdm_stride(int nx) { return tdm_chunk(nx) | 1; }
 int poisson_tdm_modes(int nx) {
   const size_t per_mode = 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double);
   return per_mode * 4 <= 200 * 1024 ? 4 : (per_mode * 2 <= 200 * 1024 ? 2 : 1);
 }
-size_t poisson_tdm_smem(int nx) { return 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double) * poisson_tdm_modes(nx); }
+size_t poisson_tdm_smem(int nx, int mb) { return 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double) * mb; }
+size_t poisson_tdm_smem(int nx) { return poisson_tdm_smem(nx, poisson_tdm_modes(nx)); }
 
 cudaError_t configure_kernels() {
   cudaError_t e;
   const int big = 227 * 1024;
-  e = cudaFuncSetAttribute(k_poisson_fwd<kFftCols>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  e = cudaFuncSetAttribute(k_poisson_fwd<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_poisson_inv<kFftCols>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  e = cudaFuncSetAttribute(k_poisson_fwd<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_inv<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_inv<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_inv<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_poisson_tdm, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 4096);
   return e;
@@ -1190,7 +1217,7 @@ cudaError_t configure_kernels() {
 
 void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, bool den, bool vis,
                   bool grad, double *den_out) {
-  const dim3 gr = grid2d(g.nx + 2, g.ny, g.nc), bl(BX, BY);
+  const dim3 gr = tile_grid(b.tiles, TK_PROPS, g.nx + 2, g.ny, g.nc), bl = tile_block(b.tiles, TK_PROPS);
   if (den && vis && grad)
     k_props<true, true, true><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
   else if (vis && grad)
@@ -1235,10 +1262,10 @@ void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
 
 void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                             const double *ux, const double *uy, const double *den0, int stage) {
-  const dim3 gr = grid2d(g.nx, g.ny, g.nc), bl(BX, BY);
+  const dim3 gr = tile_grid(b.tiles, TK_FLUX_FORCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_FLUX_FORCE);
   if (stage == 0) {
     cudaMemsetAsync(b.icount, 0, sizeof(int) * g.nc, s);
-    k_curv_list<<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.curv, b.ilist, b.icount);
+    k_curv_list<<<tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s>>>(g, m, b.vof, b.dvof, b.curv, b.ilist, b.icount);
   } else if (stage == 1) {
     k_interface_cells<<<dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s>>>(g, m, ux, uy, b.vof, b.dvof, b.ilist, b.icount, b.fluxx, b.fluxy);
   } else if (stage == 2) {
@@ -1253,7 +1280,7 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                         const double *sc, int k, double *src_a, const double *src_b, bool fused, const double *ux,
                         const double *uy, double *den1) {
-  const dim3 gr = grid2d(g.nx, g.ny, g.nc), bl(BX, BY);
+  const dim3 gr = tile_grid(b.tiles, TK_VOF_ADVANCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_VOF_ADVANCE);
   if (fused)
     k_vof_advance<true><<<gr, bl, 0, s>>>(g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, b.mfluxx,
                                           b.mfluxy, den1);
@@ -1269,7 +1296,7 @@ void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, con
 
 void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *ux,
                    const double *uy) {
-  k_stress<<<grid2d(g.nx + 1, g.ny, g.nc), dim3(BX, BY), 0, s>>>(g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
+  k_stress<<<tile_grid(b.tiles, TK_STRESS, g.nx + 1, g.ny, g.nc), tile_block(b.tiles, TK_STRESS), 0, s>>>(g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -1277,29 +1304,50 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                     const double *mfy, const double *den0, const double *den1, double *srcux_a,
                     const double *srcux_b, double *srcux_g, double *srcuy_a, const double *srcuy_b,
                     double *srcuy_g) {
-  k_predict<<<grid2d(g.nx, g.ny, g.nc), dim3(BX, BY), 0, s>>>(g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
+  k_predict<<<tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s>>>(g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
                                                         b.txy, b.tyy, b.p, b.ifrcx, b.ifrcy, den0, den1, srcux_a,
                                                         srcux_b, srcux_g, srcuy_a, srcuy_b, srcuy_g, b.irhox,
                                                         b.irhoy);
 }
 
+template <int W>
+void poisson_fwd_w(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
+                   const double *uy, const double *psi_old) {
+  const int nb = (g.nx + W - 1) / W;
+  k_poisson_fwd<W><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s>>>(g, sc, k, ux, uy, psi_old, b.irhox,
+                                                                           b.irhoy, b.twiddle, b.spec);
+}
+
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                         const double *uy, const double *psi_old) {
-  const int nb = (g.nx + kFftCols - 1) / kFftCols;
-  k_poisson_fwd<kFftCols><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny), s>>>(g, sc, k, ux, uy, psi_old, b.irhox, b.irhoy,
-                                                                  b.twiddle, b.spec);
+  if (b.tiles.fft_w == 2)
+    poisson_fwd_w<2>(s, g, b, sc, k, ux, uy, psi_old);
+  else if (b.tiles.fft_w == 8)
+    poisson_fwd_w<8>(s, g, b, sc, k, ux, uy, psi_old);
+  else
+    poisson_fwd_w<4>(s, g, b, sc, k, ux, uy, psi_old);
 }
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
-  const int mb = poisson_tdm_modes(g.nx);
+  const int mb = b.tiles.tdm_mb > 0 ? b.tiles.tdm_mb : poisson_tdm_modes(g.nx);
   const int M1 = g.ny / 2 + 1;
-  k_poisson_tdm<<<dim3((M1 + mb - 1) / mb, 1, g.nc), 64 * mb, poisson_tdm_smem(g.nx), s>>>(
+  k_poisson_tdm<<<dim3((M1 + mb - 1) / mb, 1, g.nc), 64 * mb, poisson_tdm_smem(g.nx, mb), s>>>(
       g, mb, tdm_chunk(g.nx), tdm_stride(g.nx), reinterpret_cast<const double4_32a *>(b.tdm_fac), b.spec);
 }
 
+template <int W>
+void poisson_inv_w(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
+  const int nb = (g.nx + W - 1) / W;
+  k_poisson_inv<W><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s>>>(g, b.twiddle, b.spec, psi_new);
+}
+
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
-  const int nb = (g.nx + kFftCols - 1) / kFftCols;
-  k_poisson_inv<kFftCols><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny), s>>>(g, b.twiddle, b.spec, psi_new);
+  if (b.tiles.fft_w == 2)
+    poisson_inv_w<2>(s, g, b, psi_new);
+  else if (b.tiles.fft_w == 8)
+    poisson_inv_w<8>(s, g, b, psi_new);
+  else
+    poisson_inv_w<4>(s, g, b, psi_new);
 }
 
 void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
@@ -1311,7 +1359,7 @@ void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *
 
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
                     double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure) {
-  const dim3 gr = grid2d(g.nx, g.ny, g.nc), bl(BX, BY);
+  const dim3 gr = tile_grid(b.tiles, TK_CORRECT, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_CORRECT);
   if (pressure)
     k_correct<true><<<gr, bl, 0, s>>>(g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
   else

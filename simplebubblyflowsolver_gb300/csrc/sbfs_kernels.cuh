@@ -7,6 +7,17 @@ namespace sbfs {
 
 // device pointers of one case; every scalar field uses pitch Grid::p1,
 // dvof uses Grid::p2 and normal Grid::p3 (doubles)
+// launch shapes of the fused step, picked by the autotuner (sbfs_api.cu) or
+// the defaults below; results do not depend on them (every cell, column
+// and mode is computed independently of its block)
+enum TileKernel { TK_PROPS, TK_CURV_LIST, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT, TK_CORRECT, TK_COUNT };
+struct Tiles {
+  unsigned short bx[TK_COUNT], by[TK_COUNT];  // block shape (bx * by <= 256)
+  int fft_w;   // columns per block of the Poisson transforms: 2, 4 or 8
+  int tdm_mb;  // wavenumbers per block of the tridiagonal solves (0: by size)
+};
+Tiles default_tiles();
+
 struct Bufs {
   // state
   double *ux, *uy, *p, *psi0, *psi1, *vof;
@@ -30,6 +41,8 @@ struct Bufs {
   int *status;                 // device error word
   // interface cells of the current substage (linear index (J-1)*nx + I-1) and their count
   int *ilist, *icount;
+  // launch shapes (host side)
+  Tiles tiles;
 };
 
 // ---- launch helpers (defined in sbfs_kernels.cu), all on stream `s`
@@ -87,7 +100,8 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
 int poisson_fft_cols(int ny);
 int poisson_tdm_modes(int nx);
 int tdm_chunk(int nx);
-size_t poisson_fft_smem(int ny);
+size_t poisson_fft_smem(int ny, int w);
+bool fft_w_fits(int ny, int w);
 size_t poisson_tdm_smem(int nx);
 cudaError_t configure_kernels();
 // Newton-Raphson reciprocal / inverse square root of n device inputs (tests)

@@ -149,3 +149,31 @@ def test_batch_learned_curvature_equals_single_cases(libs):
     for k, (a, b) in enumerate(zip(batch, alone)):
         for s in SLOTS:
             assert np.array_equal(a.field(s), b.field(s)), (k, s)
+
+
+@pytest.mark.gpu
+def test_autotuned_batch_equals_default(libs):
+    gpu, orc = libs
+    wls = ic.ensemble(9, seed=7, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    a = [clone(s) for s in st0]
+    b = [clone(s) for s in st0]
+    gpu.batch_release()
+    for _ in range(3):
+        gpu.integrate_batch(a)
+    gpu.batch_release()
+    gpu.set_autotune(True)
+    gpu.set_sync_mode(SYNC_NONE)
+    try:
+        gpu.integrate_batch(b)  # uploads; the autotuner runs at the first step of each group
+        for _ in range(2):
+            gpu.integrate_batch(b)
+        gpu.batch_sync_to_host(b)
+        print([gpu.tiles(q) for q in range(len(gpu.batch_groups()))])
+    finally:
+        gpu.set_autotune(False)
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.batch_release()
+    for k, (x, y) in enumerate(zip(a, b)):
+        for s in ("ux", "uy", "p", "vof"):
+            assert np.array_equal(x.field(s), y.field(s)), (k, s)

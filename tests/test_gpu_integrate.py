@@ -151,3 +151,26 @@ def test_graphs_follow_physics_changes(libs):
         assert abs(dg - do) <= 1e-12 * do
     errs = compare_state(sg, so)
     assert max(errs.values()) <= 1e-10, errs
+
+
+def test_autotuned_shapes_give_identical_steps(libs):
+    """the autotuner changes launch shapes only: the steps stay bit for bit"""
+    gpu, orc = libs
+    wl = ic.single_bubble(256, 128)
+    st0 = prepare(libs, wl)
+    a, b = clone(st0), clone(st0)
+    gpu.release()
+    gpu.set_autotune(False)
+    da = [gpu.integrate(a) for _ in range(3)]
+    gpu.release()
+    gpu.set_autotune(True)
+    try:
+        db = [gpu.integrate(b) for _ in range(3)]
+        tiles = gpu.tiles()
+    finally:
+        gpu.set_autotune(False)
+        gpu.release()
+    print(tiles)
+    assert da == db
+    for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+        assert np.array_equal(a.field(s), b.field(s)), s
