@@ -108,6 +108,14 @@ struct Ctx {
 
 std::unique_ptr<Ctx> g_ctx;
 
+}  // namespace
+
+namespace sbfs {
+void set_last_error(const char *msg) { g_err = msg; }
+}  // namespace sbfs
+
+namespace {
+
 int dalloc(Ctx &c, double **p, size_t n) {
   void *q = nullptr;
   CK(cudaMalloc(&q, n * sizeof(double)));

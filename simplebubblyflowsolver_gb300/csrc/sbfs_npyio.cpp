@@ -21,9 +21,13 @@
 
 #include "sbfs_gb300.h"
 
-namespace {
+namespace sbfs {
+// the library's last-error message (sbfs_api.cu): every entry point reports
+// through sbfs_last_error()
+void set_last_error(const char *msg);
+}  // namespace sbfs
 
-std::string g_io_err;
+namespace {
 
 int io_fail(const char *fmt, ...) {
   char buf[512];
@@ -31,7 +35,7 @@ int io_fail(const char *fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
-  g_io_err = buf;
+  sbfs::set_last_error(buf);
   fprintf(stderr, "sbfs: %s\n", buf);
   return 1;
 }

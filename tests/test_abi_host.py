@@ -97,17 +97,21 @@ def test_init_errors(lib, tmp_path):
     ic.save_ic(str(d), fields)
     env = wl.env()
     # missing environment key
+    lib.sbfs_last_error.restype = C.c_char_p
     os.environ.pop("We", None)
     rc, _ = _init(lib, str(d), {k: v for k, v in env.items() if k != "We"})
     assert rc != 0
+    assert "We" in lib.sbfs_last_error().decode()
     # wrong shape
     np.save(d / "uy.npy", np.zeros((16, 33)))
     rc, _ = _init(lib, str(d), env)
     assert rc != 0
+    assert "shape" in lib.sbfs_last_error().decode()
     # wrong dtype
     np.save(d / "uy.npy", np.zeros((16, 34), dtype=np.float32))
     rc, _ = _init(lib, str(d), env)
     assert rc != 0
+    assert "dtype" in lib.sbfs_last_error().decode()
     # non-uniform x grid
     np.save(d / "uy.npy", np.zeros((16, 34)))
     xf = fields["xf"].copy()
