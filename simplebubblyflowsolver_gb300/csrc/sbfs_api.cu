@@ -210,10 +210,11 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   const int nx = c.nx, n = nx + 3;
   const double hy = d->hy;
   const double dx = d->hxxc[0];
-  std::vector<double> h(6 * (size_t)n * c.nc, 0.);
+  constexpr int NCOL = 9;
+  std::vector<double> h(NCOL * (size_t)n * c.nc, 0.);
   for (int k = 0; k < c.nc; ++k) {
     const double nu = 1. / Re[k];
-    auto A = [&](int q, int I) -> double & { return h[((size_t)k * 6 + q) * n + I]; };
+    auto A = [&](int q, int I) -> double & { return h[((size_t)k * NCOL + q) * n + I]; };
     for (int I = 1; I <= nx + 1; ++I) {
       const double hf = d->hxxf[I - 1];
       A(0, I) = 1. / hf;
@@ -221,10 +222,16 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
       A(3, I) = 0.25 * dx / (hf * hy);
       A(4, I) = nu / hf;
       A(5, I) = hf;
+      A(8, I) = 0.5 * (1. / hf);
     }
-    for (int I = 1; I <= nx; ++I) A(1, I) = 1. / d->hxxc[I - 1];
+    for (int I = 1; I <= nx; ++I) {
+      const double ihc = 1. / d->hxxc[I - 1];
+      A(1, I) = ihc;
+      A(6, I) = nu * ihc;
+      A(7, I) = 0.25 * ihc;
+    }
   }
-  c.g.cm = c.nc > 1 ? 6 * n : 0;
+  c.g.cm = c.nc > 1 ? NCOL * n : 0;
   if (!c.met) {
     if (dalloc(c, &c.met, h.size())) return 1;
   }
@@ -237,6 +244,9 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   c.m.q4fy = b + 3 * n;
   c.m.nuf = b + 4 * n;
   c.m.hxxf = b + 5 * n;
+  c.m.nuc = b + 6 * n;
+  c.m.q4c = b + 7 * n;
+  c.m.hihxxf = b + 8 * n;
   c.Re = Re[0];
   return 0;
 }
@@ -254,10 +264,15 @@ Phys phys_of(const fluid_t *f, const interface_t *itf) {
   p.force_coef = itf ? 2. / (1. + f->denr) / itf->We : 0.;
   p.irefden = 1. / f->refden;
   p.nu = 1. / f->Re;
+  p.hgrav = 0.5 * p.grav;
+  p.rref2 = 2. * p.refden;
   return p;
 }
 
-void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) { c.ph = phys_of(f, itf); }
+void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
+  c.ph = phys_of(f, itf);
+  c.ph.nuy = c.ph.nu * c.g.ihy;
+}
 
 double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
   double hxmin = 1.79769313486231570e+308;
@@ -359,6 +374,8 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   g.p3 = rnd(3 * c->nx);
   g.hy = d->hy;
   g.ihy = 1. / d->hy;
+  g.q4y = 0.25 * g.ihy;
+  g.hihy = 0.5 * g.ihy;
   g.dx = d->hxxc[0];
   g.idx = 1. / d->hxxc[0];
   const size_t n1 = (size_t)g.p1 * g.ny, n2 = (size_t)g.p2 * g.ny, n3 = (size_t)g.p3 * g.ny;
@@ -460,6 +477,9 @@ int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
     h[sc_adt(k)] = RK_A[k] * dt;
     h[sc_bdt(k)] = RK_B[k] * dt;
     h[sc_gdt(k)] = rk_g(k) * dt;
+    h[sc_adt2(k)] = 2. * (RK_A[k] * dt);
+    h[sc_bdt2(k)] = 2. * (RK_B[k] * dt);
+    h[sc_gdt2(k)] = 2. * (rk_g(k) * dt);
   }
   if (dt_new != 0.) {
     const Grid &g = c.g;
@@ -854,6 +874,7 @@ Batch *prepare_batch(int n, const domain_t *const *d, fluid_t *const *f, interfa
       if (b->group_of[i] != (int)q) continue;
       const int k = b->slot_of[i];
       ph[k] = phys_of(f[i], itf[i]);
+      ph[k].nuy = ph[k].nu * c.g.ihy;
       ph[k].dtfix = fixed_dt(c, d[i], f[i], itf[i]);
       re[k] = f[i]->Re;
       re_changed = re_changed || !(b->res[i] == f[i]->Re);

@@ -31,6 +31,9 @@ struct Metrics {
   const double *q4fy;   // 0.25 HXXC / (HXXF(I) hy) (ux advection in y)
   const double *nuf;    // (1 / Re) / HXXF(I)   (ux diffusion in x)
   const double *hxxf;   // HXXF(I)              (decide_dt)
+  const double *nuc;    // (1 / Re) / HXXC(I)   (uy diffusion in x)
+  const double *q4c;    // 0.25 / HXXC(I)       (uy advection in x)
+  const double *hihxxf; // 0.5 / HXXF(I)        (txy)
 };
 
 struct Grid {
@@ -40,6 +43,7 @@ struct Grid {
   int p3;  // pitch of normal (3 doubles per element)
   double hy, ihy;
   double dx, idx;  // uniform cell width HXXC and its inverse
+  double q4y, hihy;  // 0.25 / hy, 0.5 / hy
   // batch of nc cases on this grid (the case is blockIdx.z; 1 for a single
   // case): element strides between cases of the scalar-pitched fields, of
   // dvof, of normal, of the Poisson spectrum (double2) and of the per-case
@@ -60,6 +64,9 @@ struct Phys {
   double irefden;     // 1 / refden
   double nu;          // 1 / Re
   double dtfix;       // diffusive / capillary bound of dt (batches: per case)
+  double hgrav;       // grav / 2
+  double rref2;       // 2 refden
+  double nuy;         // nu / hy
 };
 
 // pointer of case blockIdx.z in a batch (null stays null)
@@ -88,6 +95,10 @@ __host__ __device__ constexpr int sc_pay(int k) { return 19 + 4 * k; }
 // correction: u -= cnew * ih * dpsi_new; u += cold * ih * e * dpsi_old
 __host__ __device__ constexpr int sc_cnew(int k) { return 28 + 2 * k; }
 __host__ __device__ constexpr int sc_cold(int k) { return 29 + 2 * k; }
+// 2 alpha dt, 2 beta dt, 2 gamma dt (the predictor works on 2u)
+__host__ __device__ constexpr int sc_adt2(int k) { return 34 + 3 * k; }
+__host__ __device__ constexpr int sc_bdt2(int k) { return 35 + 3 * k; }
+__host__ __device__ constexpr int sc_gdt2(int k) { return 36 + 3 * k; }
 
 // THINC constants (reference src/interface/common.c:4-14)
 constexpr double kGaussPt = 0.2886751345948129;

@@ -422,8 +422,8 @@ __global__ void __launch_bounds__(BX *BY)
   }
   const double sx = visux[ix(g, rm, I - 1)] + vx0;
   const double sy = visuy[ix(g, r, I - 1)] + vy0;
-  const double lxy = (u0 - ux[ix(g, rm, I - 1)]) * (0.5 * g.ihy);
-  const double lyx = (w0 - uy[ix(g, r, I - 1)]) * (0.5 * m.ihxxf[I]);
+  const double lxy = (u0 - ux[ix(g, rm, I - 1)]) * g.hihy;
+  const double lyx = (w0 - uy[ix(g, r, I - 1)]) * m.hihxxf[I];
   txy[ix(g, r, I - 1)] = fma(sx, lxy, sy * lyx);
 }
 
@@ -450,15 +450,18 @@ __global__ void __launch_bounds__(BX *BY)
               double *__restrict__ syg, double *__restrict__ ex, double *__restrict__ ey) {
   const Phys ph = zphys(g, ph0);
   const double *__restrict__ nuf = m.nuf + (size_t)blockIdx.z * g.cm;
+  const double *__restrict__ nuc = m.nuc + (size_t)blockIdx.z * g.cm;
   sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
-  const double adt = sc[sc_adt(k)], bdt = sc[sc_bdt(k)], gdt = sc[sc_gdt(k)];
-  const double rref = ph.refden;
-  const double nuy = ph.nu * g.ihy;
+  // the update is carried as 2u with 2 alpha dt, ... and 1 / (2 rho_face):
+  // powers of two, so every rounding is the one of the plain form
+  const double adt2 = sc[sc_adt2(k)], bdt2 = sc[sc_bdt2(k)], gdt2 = sc[sc_gdt2(k)];
+  const double rref2 = ph.rref2;
+  const double nuy = ph.nuy;
   // ---- ux at face I
   if (I >= 2) {
     const double fx0 = mfx[ix(g, r, I - 1)];
@@ -470,20 +473,20 @@ __global__ void __launch_bounds__(BX *BY)
     const double vm = ux[ix(g, rm, I - 1)] + u0, vp = u0 + ux[ix(g, rp, I - 1)];
     double a = ifrcx[ix(g, r, I - 2)];
     const double rho0 = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];  // 2 rho^k
-    a = fma(0.5 * ph.grav, rho0, a);
+    a = fma(ph.hgrav, rho0, a);
     a = fma(nuf[I], txx[ix(g, r, I - 1)] - txx[ix(g, r, I - 2)], a);
     a = fma(nuy, txy[ix(g, rp, I - 1)] - txy[ix(g, r, I - 1)], a);
     a = fma(-m.q4f[I], fma(sxp, up, -sxm * um), a);
     a = fma(-m.q4fy[I], fma(syp, vp, -sym * vm), a);
     const double gs = (p[ix(g, r, I - 1)] - p[ix(g, r, I)]) * m.ihxxf[I];
-    const double irho = rcp_nr(half_sum(den1[ix(g, r, I - 1)], den1[ix(g, r, I)]));
-    double u = fma(adt, a, (0.5 * rho0) * u0);
-    if (k != 0) u = fma(bdt, sxb[ix(g, r, I - 2)], u);
-    u = fma(gdt, gs, u);
-    ux_out[ix(g, r, I - 1)] = u * irho;
+    const double ir2 = rcp_nr(den1[ix(g, r, I - 1)] + den1[ix(g, r, I)]);  // 1 / (2 rho^{k+1})
+    double u = fma(adt2, a, rho0 * u0);
+    if (k != 0) u = fma(bdt2, sxb[ix(g, r, I - 2)], u);
+    u = fma(gdt2, gs, u);
+    ux_out[ix(g, r, I - 1)] = u * ir2;
     sxa[ix(g, r, I - 2)] = a;
     if (sxg) sxg[ix(g, r, I - 2)] = gs;
-    ex[ix(g, r, I - 1)] = fma(rref, irho, -1.);
+    ex[ix(g, r, I - 1)] = fma(rref2, ir2, -1.);
   }
   // ---- uy at face (I, J - 1/2)
   {
@@ -495,31 +498,31 @@ __global__ void __launch_bounds__(BX *BY)
     const double sym = mfy[ix(g, rm, I)] + f0, syp = f0 + mfy[ix(g, rp, I)];
     const double vm = uy[ix(g, rm, I)] + w0, vp = w0 + uy[ix(g, rp, I)];
     double a = ifrcy[ix(g, r, I - 1)];
-    a = fma(ph.nu * m.ihxxc[I], txy[ix(g, r, I)] - txy[ix(g, r, I - 1)], a);
+    a = fma(nuc[I], txy[ix(g, r, I)] - txy[ix(g, r, I - 1)], a);
     a = fma(nuy, tyy[ix(g, r, I - 1)] - tyy[ix(g, rm, I - 1)], a);
-    a = fma(-0.25 * m.ihxxc[I], fma(sxp, up, -sxm * um), a);
-    a = fma(-0.25 * g.ihy, fma(syp, vp, -sym * vm), a);
+    a = fma(-m.q4c[I], fma(sxp, up, -sxm * um), a);
+    a = fma(-g.q4y, fma(syp, vp, -sym * vm), a);
     const double gs = (p[ix(g, rm, I)] - p[ix(g, r, I)]) * g.ihy;
-    const double rho0 = half_sum(den0[ix(g, rm, I)], den0[ix(g, r, I)]);
-    const double irho = rcp_nr(half_sum(den1[ix(g, rm, I)], den1[ix(g, r, I)]));
-    double u = fma(adt, a, rho0 * w0);
-    if (k != 0) u = fma(bdt, syb[ix(g, r, I - 1)], u);
-    u = fma(gdt, gs, u);
-    uy_out[ix(g, r, I)] = u * irho;
+    const double rho0 = den0[ix(g, rm, I)] + den0[ix(g, r, I)];  // 2 rho^k
+    const double ir2 = rcp_nr(den1[ix(g, rm, I)] + den1[ix(g, r, I)]);
+    double u = fma(adt2, a, rho0 * w0);
+    if (k != 0) u = fma(bdt2, syb[ix(g, r, I - 1)], u);
+    u = fma(gdt2, gs, u);
+    uy_out[ix(g, r, I)] = u * ir2;
     sya[ix(g, r, I - 1)] = a;
     if (syg) syg[ix(g, r, I - 1)] = gs;
-    ey[ix(g, r, I)] = fma(rref, irho, -1.);
+    ey[ix(g, r, I)] = fma(rref2, ir2, -1.);
   }
   // walls: impermeable, no-slip; wall-face factors for the Poisson operator
   if (I == 1) {
     ux_out[ix(g, r, 0)] = 0.;
     uy_out[ix(g, r, 0)] = 0.;
-    ex[ix(g, r, 0)] = fma(rref, rcp_nr(half_sum(den1[ix(g, r, 0)], den1[ix(g, r, 1)])), -1.);
+    ex[ix(g, r, 0)] = fma(rref2, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -1.);
   }
   if (I == g.nx) {
     ux_out[ix(g, r, g.nx)] = 0.;
     uy_out[ix(g, r, g.nx + 1)] = 0.;
-    ex[ix(g, r, g.nx)] = fma(rref, rcp_nr(half_sum(den1[ix(g, r, g.nx)], den1[ix(g, r, g.nx + 1)])), -1.);
+    ex[ix(g, r, g.nx)] = fma(rref2, rcp_nr(den1[ix(g, r, g.nx)] + den1[ix(g, r, g.nx + 1)]), -1.);
   }
 }
 
@@ -947,6 +950,9 @@ __global__ void __launch_bounds__(BX *BY)
       sc[sc_adt(k)] = al[k] * dt;
       sc[sc_bdt(k)] = be[k] * dt;
       sc[sc_gdt(k)] = (al[k] + be[k]) * dt;
+      sc[sc_adt2(k)] = 2. * (al[k] * dt);
+      sc[sc_bdt2(k)] = 2. * (be[k] * dt);
+      sc[sc_gdt2(k)] = 2. * ((al[k] + be[k]) * dt);
       sc[sc_dtold(k)] = dtold;
       sc[sc_dtnew(k)] = dtnew;
       const double cdiv = ph.refden / dtnew * (0.5 / g.ny);
