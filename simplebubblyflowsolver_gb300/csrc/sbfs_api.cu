@@ -264,6 +264,9 @@ Phys phys_of(const fluid_t *f, const interface_t *itf) {
   p.force_coef = itf ? 2. / (1. + f->denr) / itf->We : 0.;
   p.irefden = 1. / f->refden;
   p.nu = 1. / f->Re;
+  p.dm1 = f->denr - 1.;
+  p.vm1 = f->visr - 1.;
+  p.hvm1 = 0.5 * p.vm1;
   p.hgrav = 0.5 * p.grav;
   p.rref2 = 2. * p.refden;
   return p;

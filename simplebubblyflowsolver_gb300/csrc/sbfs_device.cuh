@@ -64,6 +64,8 @@ struct Phys {
   double irefden;     // 1 / refden
   double nu;          // 1 / Re
   double dtfix;       // diffusive / capillary bound of dt (batches: per case)
+  double dm1;         // denr - 1
+  double vm1, hvm1;   // visr - 1, (visr - 1) / 2
   double hgrav;       // grav / 2
   double rref2;       // 2 refden
   double nuy;         // nu / hy

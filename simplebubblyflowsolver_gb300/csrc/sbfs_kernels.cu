@@ -64,10 +64,10 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, c
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
   const double v = vof[ix(g, r, I)];
-  if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.denr - 1., v, 1.), ph.den_lo, ph.den_hi);
+  if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.dm1, v, 1.), ph.den_lo, ph.den_hi);
   if (VIS) {
     // 1 + (visr - 1) 0.5 (a + b) = 1 + c2 (a + b), c2 = (visr - 1) / 2
-    const double c = ph.visr - 1., c2 = 0.5 * c;
+    const double c = ph.vm1, c2 = ph.hvm1;
     if (I >= 1) {
       double vis;
       if (I == 1) vis = fma(c, vof[ix(g, r, 0)], 1.);
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(BX *BY)
   if (I == 1) vof[ix(g, r, 0)] = 0.;
   if (I == g.nx) vof[ix(g, r, g.nx + 1)] = 0.;
   if (FUSED) {
-    const double c = ph.denr - 1.;
+    const double c = ph.dm1;
     den1[ix(g, r, I)] = clip_pos(fma(c, v, 1.), ph.den_lo, ph.den_hi);
     mfx[ix(g, r, I - 1)] = fma(c, fxm, ux[ix(g, r, I - 1)]);
     mfy[ix(g, r, I)] = fma(c, fym, uy[ix(g, r, I)]);
