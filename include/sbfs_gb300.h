@@ -146,6 +146,12 @@ typedef struct {
   double wall_stress[2];   /* nu sum txy at x = 0, lx     logging/stress.c:29-35 */
 } sbfs_diagnostics_t;
 int sbfs_diagnostics(const domain_t *domain, fluid_t *fluid, interface_t *interface, sbfs_diagnostics_t *out);
+/* appends the reference's monitor lines (progress, divergence, momentum,
+ * extrema, energy, stress, vof .dat; src/logging/main.c:90-108 and the line
+ * formats of src/logging/{divergence,momentum,...}.c) to the files in dirname, from the device
+ * reductions above; the progress line also goes to stdout */
+int sbfs_logging_output(const char dirname[], const domain_t *domain, fluid_t *fluid, interface_t *interface,
+                        size_t step, double time, double dt, double wtime);
 /* running sums ux1, uy1, vof1 and their count (statistics.c:99-166) */
 int sbfs_statistics_collect(const domain_t *domain, fluid_t *fluid, interface_t *interface);
 int sbfs_statistics_reset(void);

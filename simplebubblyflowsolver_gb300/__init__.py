@@ -109,6 +109,12 @@ class GpuLibrary(ReferenceAPI):
                  "momentum_y", "energy_x", "energy_y", "umax", "vmax", "wall_stress_xm", "wall_stress_xp"]
         return dict(zip(names, list(out)))
 
+    def logging_output(self, dirname: str, st: SolverState, step: int, time: float, dt: float, wtime: float = 0.0):
+        """append the reference's monitor lines to dirname/*.dat"""
+        self.lib.sbfs_logging_output.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                                 C.c_double, C.c_double, C.c_double]
+        self._ext("sbfs_logging_output", dirname.encode(), *self._ptrs(st), step, time, dt, wtime)
+
     def statistics_collect(self, st: SolverState):
         self._ext("sbfs_statistics_collect", *self._ptrs(st))
 

@@ -1006,7 +1006,8 @@ int sbfs_set_curvature_model(int model) {
 static Ctx *diag_ctx(const domain_t *d, fluid_t *f, interface_t *itf) {
   Ctx *c = prepare_step(d, f, itf);
   if (!c) return nullptr;
-  if (!c->resident) {
+  // the host is the truth unless the caller keeps the state on the device
+  if (g_sync_mode != SBFS_SYNC_NONE || !c->resident) {
     if (upload_state(*c, f, itf)) return nullptr;
     // the wall-stress log reads the caller's txy, as the reference's does
     if (h2d(*c, f->txy, L_TXY, c->b.txy)) return nullptr;
@@ -1040,6 +1041,48 @@ int sbfs_diagnostics(const domain_t *d, fluid_t *f, interface_t *itf, sbfs_diagn
   out->umax[1] = h[11];
   out->wall_stress[0] = h[12];
   out->wall_stress[1] = h[13];
+  return 0;
+}
+
+// the reference's monitor files (src/logging/main.c:90-108), appended to in
+// dirname with the reference's line formats; the quantities come from the
+// device reductions of sbfs_diagnostics
+int sbfs_logging_output(const char dirname[], const domain_t *d, fluid_t *f, interface_t *itf, size_t step,
+                        double time, double dt, double wtime) {
+  sbfs_diagnostics_t q;
+  if (sbfs_diagnostics(d, f, itf, &q)) return 1;
+  const std::string dir = dirname ? std::string(dirname) : std::string(".");
+  auto open = [&](const char *name) -> FILE * {
+    const std::string path = dir + "/" + name;
+    FILE *fp = fopen(path.c_str(), "a");
+    if (!fp) fail("%s: cannot open for appending", path.c_str());
+    return fp;
+  };
+  FILE *fp;
+  if (!(fp = open("progress.dat"))) return 1;
+  fprintf(fp, "step %10zu, time %.3f, dt %.3e, elapsed %.1f [sec]\n", step, time, dt, wtime);
+  fprintf(stdout, "step %10zu, time %.3f, dt %.3e, elapsed %.1f [sec]\n", step, time, dt, wtime);
+  fclose(fp);
+  if (!(fp = open("divergence.dat"))) return 1;
+  fprintf(fp, "%8.2f % .1e\n", time, q.divmax);
+  fclose(fp);
+  if (!(fp = open("momentum.dat"))) return 1;
+  fprintf(fp, "%8.2f % 18.15e % 18.15e\n", time, q.momentum[0], q.momentum[1]);
+  fclose(fp);
+  if (!(fp = open("extrema.dat"))) return 1;
+  fprintf(fp, "%8.2f % 18.15e % 18.15e\n", time, q.umax[0], q.umax[1]);
+  fclose(fp);
+  if (!(fp = open("energy.dat"))) return 1;
+  fprintf(fp, "%8.2f % 18.15e % 18.15e\n", time, q.energy[0], q.energy[1]);
+  fclose(fp);
+  if (!(fp = open("stress.dat"))) return 1;
+  fprintf(fp, "%8.2f % 18.15e % 18.15e\n", time, q.wall_stress[0], q.wall_stress[1]);
+  fclose(fp);
+  if (!(fp = open("vof.dat"))) return 1;
+  fprintf(fp, "%8.2f % 18.15e % 18.15e % 18.15e % 18.15e\n", time, q.vof_min, q.vof_max,
+          q.vof_integral / q.volume, q.interface_area);
+  fclose(fp);
+  fflush(stdout);
   return 0;
 }
 

@@ -767,15 +767,12 @@ __global__ void __launch_bounds__(256)
     }
     double next = __shfl_down_sync(0xffffffffu, Sx, 1);
     if (lane == 31) next = 0.;
-    double acc = 0.;
 #pragma unroll 8
-    for (int k = 0; k < L; ++k) {
-      const double v = fma(f[(size_t)k * 32].w, next, x[k]);
-      x[k] = v;
-      acc += (lane * L + k < nx) ? v : 0.;
-    }
+    for (int k = 0; k < L; ++k) x[k] = fma(f[(size_t)k * 32].w, next, x[k]);
     if (m == 0) {
       // gauge of the singular mode: zero mean over x (imaginary part is 0)
+      double acc = 0.;
+      for (int k = 0; k < L; ++k) acc += (lane * L + k < nx) ? x[k] : 0.;
 #pragma unroll
       for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
       const double mean = (warp & 1) ? 0. : acc / nx;

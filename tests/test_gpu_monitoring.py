@@ -67,3 +67,41 @@ def test_resident_diagnostics_and_statistics(libs):
     assert num == 4
     for got, want in zip((ux1, uy1, vof1), sums):
         assert np.abs(got - want).max() <= 1e-9 * max(np.abs(want).max(), 1e-300)
+
+
+def test_logging_files_in_the_reference_format(libs, tmp_path):
+    """sbfs_logging_output writes the seven monitor files with the
+    reference's line formats (src/logging/*.c), values from the oracle"""
+    gpu, orc = libs
+    wl = ic.single_bubble(128, 64)
+    set_env(wl)
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    st = new_state(wl, orc)
+    t = 0.0
+    for step in range(1, 4):
+        dt = orc.integrate(st)
+        t += dt
+        gpu.logging_output(str(tmp_path), clone(st), step, t, dt, 0.5)
+    b = orc.diagnostics(st)
+    files = {p.name: p.read_text().splitlines() for p in tmp_path.iterdir()}
+    assert sorted(files) == sorted(["progress.dat", "divergence.dat", "momentum.dat", "extrema.dat", "energy.dat",
+                                    "stress.dat", "vof.dat"])
+    assert all(len(v) == 3 for v in files.values())
+    assert files["progress.dat"][-1] == f"step {3:10d}, time {t:.3f}, dt {dt:.3e}, elapsed {0.5:.1f} [sec]"
+    assert files["divergence.dat"][-1].startswith(f"{t:8.2f} ")
+    expect = {
+        "momentum.dat": (b["momentum_x"], b["momentum_y"]),
+        "extrema.dat": (b["umax"], b["vmax"]),
+        "energy.dat": (b["energy_x"], b["energy_y"]),
+        "stress.dat": (b["wall_stress_xm"], b["wall_stress_xp"]),
+        "vof.dat": (b["vof_min"], b["vof_max"], b["vof_integral"] / b["volume"], b["interface_area"]),
+    }
+    for name, vals in expect.items():
+        line = files[name][-1]
+        ref = f"{t:8.2f} " + " ".join(f"{v: 18.15e}" for v in vals)
+        assert len(line) == len(ref) and line[:9] == ref[:9], (name, line, ref)
+        got = [float(x) for x in line.split()[1:]]
+        for g, v in zip(got, vals):
+            assert abs(g - v) <= 1e-11 * abs(v) + 1e-16, (name, g, v)
