@@ -451,11 +451,12 @@ def interface_stencils(vof_rows: np.ndarray, vofmin=1e-8):
 def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_every=0):
     """Run the static drop (r = 0.25 in the unit box, density ratio 1e-3,
     La = 12000) for `steps` steps with curvature model 0 (-div n) or 1 (the
-    learned closure with `params`) and measure the parasitic currents and
-    the Laplace pressure jump (exact: kappa / We = 4)."""
+    learned closure with `params`) and measure the parasitic currents, the
+    Laplace pressure jump (exact: kappa / We = 4) and the error of the
+    curvature the step used in the interface cells (exact: 4)."""
     import os
 
-    from . import SYNC_NONE, SYNC_STATE
+    from . import SYNC_ALL, SYNC_NONE, SYNC_STATE
     from .binding import state_from_fields
     wl = ic.static_drop(n, steps)
     for k, v in wl.env().items():
@@ -476,6 +477,7 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
             if record_every and (s + 1) % record_every == 0:
                 dg = lib.diagnostics(st)
                 hist.append((s + 1, t, max(dg["umax"], dg["vmax"])))
+        lib.set_sync_mode(SYNC_ALL)  # every array, the last curvature included
         lib.sync_to_host(st)
         used = lib.mlp_take_usage() if model else 0
     finally:
@@ -491,7 +493,13 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
     exact = 1.0 / (wl.We * 0.25)
     umax = max(float(np.abs(ux).max()), float(np.abs(uy).max()))
     st_i, _, _ = interface_stencils(st.interior_rows("vof"))
+    # curvature the last substage used, in its interface cells (exact: 1 / r = 4)
+    kap = st.interior_rows("curv")[:, 1:-1]
+    band = (vof >= 0.01) & (vof <= 0.99)
+    kerr = (kap[band] - 4.0) / 4.0
     return {"n": n, "steps": steps, "time": t, "umax": umax, "capillary_number": umax * wl.We / wl.Re,
+            "kappa_rms_rel_err": float(np.sqrt(np.mean(kerr ** 2))),
+            "kappa_median_abs_rel_err": float(np.median(np.abs(kerr))),
             "dp": float(p_in - p_out), "dp_rel_err": float(abs(p_in - p_out - exact) / exact),
             "learned_cells_per_step": used / (3.0 * steps) if model else 0.0,
             "interface_cells": int(st_i.shape[0]), "umax_history": hist}
