@@ -76,8 +76,10 @@ def parse_args():
     ap.add_argument("--profile-steps", type=int, default=10)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0, help="target seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=("swarm", "ensemble"), default="swarm",
-                    help="swarm: the 2048x1024 bubble swarm (default); ensemble: 256 independent cases in batches")
+    ap.add_argument("--workload", choices=("swarm", "single_bubble", "static_drop", "ensemble"), default="swarm",
+                    help="swarm: the 2048x1024 bubble swarm (default); single_bubble: 256x128, one bubble; "
+                         "static_drop: n x n (--n); ensemble: 256 independent cases in batches")
+    ap.add_argument("--n", type=int, default=256, help="static drop grid")
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--curvature", choices=("plain", "learned"), default="plain",
@@ -179,14 +181,23 @@ class ClockSampler:
 
 def workload(args):
     from simplebubblyflowsolver_gb300 import ic
+    if args.workload == "single_bubble":
+        return ic.single_bubble(256, 128)
+    if args.workload == "static_drop":
+        return ic.static_drop(args.n)
     return ic.bubble_swarm(args.nx, args.ny, nbubbles=args.bubbles, seed=0)
 
 
 def config_of(wl, args, ws):
-    return {"workload": f"bubble_swarm_{wl.nx}x{wl.ny}", "nx": wl.nx, "ny": wl.ny, "bubbles": len(wl.discs),
-            "radii": "U[0.05,0.10]", "seed": 0, "lx": wl.lx, "ly": wl.ly, "Re": wl.Re, "Bo": wl.We, "Fr": wl.Fr,
-            "denr": wl.denr, "visr": wl.visr, "cfl": wl.coef_dt_adv, "parallelism": f"replicas{ws}",
-            "l2": "working set (~0.5 GB) larger than L2, no flush"}
+    big = wl.cells * 8 * 35 > 129e6
+    cfg = {"workload": f"{wl.name}_{wl.nx}x{wl.ny}", "nx": wl.nx, "ny": wl.ny, "bubbles": len(wl.discs),
+           "lx": wl.lx, "ly": wl.ly, "Re": wl.Re, "Bo": wl.We, "Fr": wl.Fr, "denr": wl.denr, "visr": wl.visr,
+           "cfl": wl.coef_dt_adv, "parallelism": f"replicas{ws}",
+           "l2": ("working set larger than L2, no flush" if big else
+                  "working set fits in L2: an L2-resident, launch-latency-bound case (no flush)")}
+    if wl.name == "bubble_swarm":
+        cfg.update(radii="U[0.05,0.10]", seed=0)
+    return cfg
 
 
 def make_state(wl, backend):
