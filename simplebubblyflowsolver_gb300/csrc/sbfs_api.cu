@@ -210,7 +210,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   const int nx = c.nx, n = nx + 3;
   const double hy = d->hy;
   const double dx = d->hxxc[0];
-  constexpr int NCOL = 9;
+  constexpr int NCOL = 10;
   std::vector<double> h(NCOL * (size_t)n * c.nc, 0.);
   for (int k = 0; k < c.nc; ++k) {
     const double nu = 1. / Re[k];
@@ -229,6 +229,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
       A(1, I) = ihc;
       A(6, I) = nu * ihc;
       A(7, I) = 0.25 * ihc;
+      A(9, I) = 0.5 * ihc;
     }
   }
   c.g.cm = c.nc > 1 ? NCOL * n : 0;
@@ -247,6 +248,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   c.m.nuc = b + 6 * n;
   c.m.q4c = b + 7 * n;
   c.m.hihxxf = b + 8 * n;
+  c.m.hihxxc = b + 9 * n;
   c.Re = Re[0];
   return 0;
 }
@@ -268,6 +270,7 @@ Phys phys_of(const fluid_t *f, const interface_t *itf) {
   p.vm1 = f->visr - 1.;
   p.hvm1 = 0.5 * p.vm1;
   p.hgrav = 0.5 * p.grav;
+  p.qf = 0.25 * p.force_coef;
   p.rref2 = 2. * p.refden;
   return p;
 }
@@ -275,6 +278,7 @@ Phys phys_of(const fluid_t *f, const interface_t *itf) {
 void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
   c.ph = phys_of(f, itf);
   c.ph.nuy = c.ph.nu * c.g.ihy;
+  c.ph.qfy = c.ph.qf * c.g.ihy;
 }
 
 double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
@@ -878,6 +882,7 @@ Batch *prepare_batch(int n, const domain_t *const *d, fluid_t *const *f, interfa
       const int k = b->slot_of[i];
       ph[k] = phys_of(f[i], itf[i]);
       ph[k].nuy = ph[k].nu * c.g.ihy;
+      ph[k].qfy = ph[k].qf * c.g.ihy;
       ph[k].dtfix = fixed_dt(c, d[i], f[i], itf[i]);
       re[k] = f[i]->Re;
       re_changed = re_changed || !(b->res[i] == f[i]->Re);

@@ -34,6 +34,7 @@ struct Metrics {
   const double *nuc;    // (1 / Re) / HXXC(I)   (uy diffusion in x)
   const double *q4c;    // 0.25 / HXXC(I)       (uy advection in x)
   const double *hihxxf; // 0.5 / HXXF(I)        (txy)
+  const double *hihxxc; // 0.5 / HXXC(I)        (curvature)
 };
 
 struct Grid {
@@ -69,6 +70,7 @@ struct Phys {
   double hgrav;       // grav / 2
   double rref2;       // 2 refden
   double nuy;         // nu / hy
+  double qf, qfy;     // force_coef / 4, force_coef / 4 / hy
 };
 
 // pointer of case blockIdx.z in a batch (null stays null)

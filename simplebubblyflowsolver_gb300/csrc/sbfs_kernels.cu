@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const
     if ((any << 1) != 0) {  // some corner normal is not +-0
       const double ddx = (d10.x + d11.x) - (d00.x + d01.x);
       const double ddy = (d01.y + d11.y) - (d00.y + d10.y);
-      k = -fma(0.5 * m.ihxxc[I], ddx, (0.5 * g.ihy) * ddy);
+      k = -fma(m.hihxxc[I], ddx, g.hihy * ddy);
     }
     curv[ix(g, r, I)] = k;
   }
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(BX *BY)
         const double rho = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];
         const double kap = ITF_KAPPA ? face_kappa_sum(vxm, v0, curv[ix(g, r, I - 1)], curv[ix(g, r, I)])
                                      : curv[ix(g, r, I - 1)] + curv[ix(g, r, I)];
-        f = (rho * kap) * ((0.25 * ph.force_coef * m.ihxxf[I]) * (v0 - vxm));
+        f = (rho * kap) * ((ph.qf * m.ihxxf[I]) * (v0 - vxm));
       }
       ifrcx[ix(g, r, I - 2)] = f;
     }
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(BX *BY)
       const double rho = den0[ix(g, rm, I)] + den0[ix(g, r, I)];
       const double kap = ITF_KAPPA ? face_kappa_sum(vym, v0, curv[ix(g, rm, I)], curv[ix(g, r, I)])
                                    : curv[ix(g, rm, I)] + curv[ix(g, r, I)];
-      f = (rho * kap) * ((0.25 * ph.force_coef * g.ihy) * (v0 - vym));
+      f = (rho * kap) * (ph.qfy * (v0 - vym));
     }
     ifrcy[ix(g, r, I - 1)] = f;
   }
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
     if ((any << 1) != 0) {
       const double ddx = (d10.x + d11.x) - (d00.x + d01.x);
       const double ddy = (d01.y + d11.y) - (d00.y + d10.y);
-      k = -fma(0.5 * m.ihxxc[I], ddx, (0.5 * g.ihy) * ddy);
+      k = -fma(m.hihxxc[I], ddx, g.hihy * ddy);
     }
     curv[ix(g, r, I)] = k;
     itf = !single_phase(vof[ix(g, r, I)]);
