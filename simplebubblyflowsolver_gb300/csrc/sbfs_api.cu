@@ -500,6 +500,8 @@ int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
     h[sc_pay(0)] = cadd * (g.ihy * g.ihy);
     h[sc_cnew(0)] = dt_new * c.ph.irefden;
     h[sc_cold(0)] = -dt_old * c.ph.irefden;
+    h[sc_cnewy(0)] = h[sc_cnew(0)] * g.ihy;
+    h[sc_coldy(0)] = h[sc_cold(0)] * g.ihy;
   }
   CK(cudaMemcpyAsync(c.b.scalars, h, sizeof(double) * kScalars, cudaMemcpyHostToDevice, c.s));
   // h is reused by the next call: wait for the copy

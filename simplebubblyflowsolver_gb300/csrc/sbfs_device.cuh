@@ -103,6 +103,9 @@ __host__ __device__ constexpr int sc_cold(int k) { return 29 + 2 * k; }
 __host__ __device__ constexpr int sc_adt2(int k) { return 34 + 3 * k; }
 __host__ __device__ constexpr int sc_bdt2(int k) { return 35 + 3 * k; }
 __host__ __device__ constexpr int sc_gdt2(int k) { return 36 + 3 * k; }
+// the correction coefficients times 1 / hy
+__host__ __device__ constexpr int sc_cnewy(int k) { return 43 + 2 * k; }
+__host__ __device__ constexpr int sc_coldy(int k) { return 44 + 2 * k; }
 
 // THINC constants (reference src/interface/common.c:4-14)
 constexpr double kGaussPt = 0.2886751345948129;

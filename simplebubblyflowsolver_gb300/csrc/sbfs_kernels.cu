@@ -148,8 +148,9 @@ __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const
 // is the face position along its normal (+-1/2) and n_a, n_b the normal
 // components along and across it.  With a = K exp(-2 n_a s) and
 // b = exp(-2 n_b g) the two terms are 1 / (1 + a b) and b / (b + a).
-__device__ __forceinline__ double thinc_face(double na, double nb, double K, double s) {
-  const double a = K * exp(-2. * na * s);
+// The caller passes -2 n_a s, which for s = -+1/2 is exactly +-n_a.
+__device__ __forceinline__ double thinc_face(double m2nas, double nb, double K) {
+  const double a = K * exp(m2nas);
   const double b = exp(-2. * kGaussPt * nb);
   const double p = fma(a, b, 1.);
   const double q = b + a;
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(BX *BY)
       } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)r * g.p3 + (size_t)(iu - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
-        fluxx[ix(g, r, I - 1)] = vel * thinc_face(nv[0], nv[1], K, n ? -0.5 : 0.5);
+        fluxx[ix(g, r, I - 1)] = vel * thinc_face(n ? nv[0] : -nv[0], nv[1], K);
       }
     }
     {
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(BX *BY)
       } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)ru * g.p3 + (size_t)(I - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
-        fluxy[ix(g, r, I)] = vel * thinc_face(nv[1], nv[0], K, n ? -0.5 : 0.5);
+        fluxy[ix(g, r, I)] = vel * thinc_face(n ? nv[1] : -nv[1], nv[0], K);
       }
     }
     // impermeable walls / dummy ghost faces
@@ -326,12 +327,12 @@ __global__ void __launch_bounds__(256)
     const double K = rcp_nr(vof[ix(g, r, I)]) - 1.;
     // x faces I (left) and I + 1 (right); the wall faces belong to k_flux_force
     const double ul = ux[ix(g, r, I - 1)], ur = ux[ix(g, r, I)];
-    if (I >= 2 && neg(ul)) fluxx[ix(g, r, I - 1)] = ul * thinc_face(n0, n1, K, -0.5);
-    if (I < g.nx && !neg(ur)) fluxx[ix(g, r, I)] = ur * thinc_face(n0, n1, K, 0.5);
+    if (I >= 2 && neg(ul)) fluxx[ix(g, r, I - 1)] = ul * thinc_face(n0, n1, K);
+    if (I < g.nx && !neg(ur)) fluxx[ix(g, r, I)] = ur * thinc_face(-n0, n1, K);
     // y faces J - 1/2 (bottom, stored in row J) and J + 1/2 (row J + 1)
     const double vb = uy[ix(g, r, I)], vt = uy[ix(g, rp, I)];
-    if (neg(vb)) fluxy[ix(g, r, I)] = vb * thinc_face(n1, n0, K, -0.5);
-    if (!neg(vt)) fluxy[ix(g, rp, I)] = vt * thinc_face(n1, n0, K, 0.5);
+    if (neg(vb)) fluxy[ix(g, r, I)] = vb * thinc_face(n1, n0, K);
+    if (!neg(vt)) fluxy[ix(g, rp, I)] = vt * thinc_face(-n1, n0, K);
   }
 }
 
@@ -807,6 +808,7 @@ __global__ void __launch_bounds__(BX *BY)
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
   const double cnew = sc[sc_cnew(k)], cold = sc[sc_cold(k)];
+  const double cnewy = sc[sc_cnewy(k)], coldy = sc[sc_coldy(k)];
   const double pn0 = psin[ix(g, r, I)], po0 = psio[ix(g, r, I)];
   if (I >= 2) {
     const double ih = m.ihxxf[I];
@@ -817,8 +819,8 @@ __global__ void __launch_bounds__(BX *BY)
   }
   {
     double u = uy[ix(g, r, I)];
-    u = fma(-(cnew * g.ihy), pn0 - psin[ix(g, rm, I)], u);
-    u = fma((cold * g.ihy) * ey[ix(g, r, I)], po0 - psio[ix(g, rm, I)], u);
+    u = fma(-cnewy, pn0 - psin[ix(g, rm, I)], u);
+    u = fma(coldy * ey[ix(g, r, I)], po0 - psio[ix(g, rm, I)], u);
     uy[ix(g, r, I)] = u;
   }
   if (I == 1) {
@@ -960,6 +962,8 @@ __global__ void __launch_bounds__(BX *BY)
       sc[sc_pay(k)] = cadd * (g.ihy * g.ihy);
       sc[sc_cnew(k)] = dtnew * ph.irefden;
       sc[sc_cold(k)] = -dtold * ph.irefden;
+      sc[sc_cnewy(k)] = sc[sc_cnew(k)] * g.ihy;
+      sc[sc_coldy(k)] = sc[sc_cold(k)] * g.ihy;
     }
   }
   __syncthreads();
