@@ -415,8 +415,11 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   b.dt_acc = reinterpret_cast<unsigned long long *>(tmp);
   if (dalloc(*c, &tmp, ((size_t)c->nx * c->ny * nc + 2) / 2 + 1)) return 1;
   b.ilist = reinterpret_cast<int *>(tmp);
-  if (dalloc(*c, &tmp, (size_t)nc / 2 + 1)) return 1;
+  if (dalloc(*c, &tmp, (4 * (size_t)c->nx * c->ny * nc + 2) / 2 + 1)) return 1;
+  b.flist = reinterpret_cast<int *>(tmp);
+  if (dalloc(*c, &tmp, (size_t)nc + 1)) return 1;  // nc cell counts, then nc face counts
   b.icount = reinterpret_cast<int *>(tmp);
+  b.fcount = b.icount + nc;
   // scalars of every case, then one status word per case
   if (dalloc(*c, &tmp, (size_t)kScalars * nc + nc / 2 + 2)) return 1;
   b.scalars = tmp;

@@ -73,6 +73,12 @@ struct Phys {
   double qf, qfy;     // force_coef / 4, force_coef / 4 / hy
 };
 
+// x / 2 for a positive normal x (x >= 2^-1021), exactly: the exponent field
+// drops by one.  Integer work, so the FP64 pipe is not used.
+__device__ __forceinline__ double half_pos_normal(double x) {
+  return __longlong_as_double(__double_as_longlong(x) - (1LL << 52));
+}
+
 // pointer of case blockIdx.z in a batch (null stays null)
 template <class T>
 __device__ __forceinline__ T *zp(T *p, size_t stride) {

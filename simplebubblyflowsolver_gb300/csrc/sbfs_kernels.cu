@@ -154,7 +154,8 @@ __device__ __forceinline__ double thinc_face(double m2nas, double nb, double K) 
   const double b = exp(-2. * kGaussPt * nb);
   const double p = fma(a, b, 1.);
   const double q = b + a;
-  return 0.5 * fma(b, p, q) * rcp_nr(p * q);
+  // b p + q >= b >= exp(-2 g) > 1/2: positive and normal
+  return half_pos_normal(fma(b, p, q)) * rcp_nr(p * q);
 }
 
 // ---------------------------------------------------------------------------
@@ -254,25 +255,33 @@ __global__ void __launch_bounds__(BX *BY)
 // two exponentials per face) exists only in interface cells, a few percent
 // of the domain scattered along the bubbles; done in place it makes whole
 // warps wait on a few lanes.  So:
-//   k_curv_list       curvature of every cell (curvature_tensor.c:100-135)
-//                     and a list of the interface cells (warp-aggregated)
-//   k_interface_cells one thread per listed cell: normal and K = 1/phi - 1
-//                     (curvature_tensor.c:51-97), then the THINC flux of each
-//                     face the cell is upwind of (update/fluxx.c, fluxy.c)
+//   k_curv_list       curvature of every cell (curvature_tensor.c:100-135),
+//                     a list of the interface cells and a list of the faces
+//                     they are upwind of (warp-aggregated appends)
+//   k_interface_cells one thread per listed face: the cell's normal and
+//                     K = 1/phi - 1 (curvature_tensor.c:51-97), then the THINC
+//                     flux of that face (update/fluxx.c, fluxy.c); a cell
+//                     with two upwind faces is set up twice, but no warp
+//                     runs a face branch only some of its lanes take
 //   k_flux_force<.., BULK_ONLY>  every other face (upwind cell single-phase:
 //                     flux = vel phi) and the CSF force
 // Each face is written by exactly one of them: the upwind choice and the
 // vofmin test are the same integer tests in both.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const double *__restrict__ vof,
-                                                      const double *__restrict__ dvof, double *__restrict__ curv,
-                                                      int *__restrict__ list, int *__restrict__ count) {
+                                                      const double *__restrict__ dvof, const double *__restrict__ ux,
+                                                      const double *__restrict__ uy, double *__restrict__ curv,
+                                                      int *__restrict__ list, int *__restrict__ count,
+                                                      int *__restrict__ flist, int *__restrict__ fcount) {
   list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
   count += (size_t)blockIdx.z * (1);
+  flist += (size_t)blockIdx.z * (4 * (size_t)g.nx * g.ny);
+  fcount += (size_t)blockIdx.z * (1);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const bool in = I <= g.nx && J <= g.ny;
   bool itf = false;
+  unsigned up = 0u;  // faces this cell is upwind of: bit 0 left, 1 right, 2 bottom, 3 top
   if (in) {
     const int zr = blockIdx.z * g.ny;
     const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
@@ -290,32 +299,55 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
     }
     curv[ix(g, r, I)] = k;
     itf = !single_phase(vof[ix(g, r, I)]);
+    if (itf) {
+      // upwind tests of update/fluxx.c, fluxy.c; the wall faces belong to k_flux_force
+      up |= (I >= 2 && neg(ux[ix(g, r, I - 1)])) ? 1u : 0u;
+      up |= (I < g.nx && !neg(ux[ix(g, r, I)])) ? 2u : 0u;
+      up |= neg(uy[ix(g, r, I)]) ? 4u : 0u;
+      up |= !neg(uy[ix(g, rp, I)]) ? 8u : 0u;
+    }
   }
-  // warp-aggregated append (a warp is 32 consecutive threads of the block,
+  // warp-aggregated appends (a warp is 32 consecutive threads of the block,
   // whatever its shape)
+  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+  const int cell = (J - 1) * g.nx + (I - 1);
   const unsigned mask = __ballot_sync(0xffffffffu, itf);
   if (mask) {
-    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
     const int leader = __ffs(mask) - 1;
     int base = 0;
     if (lane == leader) base = atomicAdd(count, __popc(mask));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (itf) list[base + __popc(mask & ((1u << lane) - 1u))] = (J - 1) * g.nx + (I - 1);
+    if (itf) list[base + __popc(mask & ((1u << lane) - 1u))] = cell;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const bool has = (up >> f) & 1u;
+      const unsigned fm = __ballot_sync(0xffffffffu, has);
+      if (fm) {
+        const int fl = __ffs(fm) - 1;
+        int fb = 0;
+        if (lane == fl) fb = atomicAdd(fcount, __popc(fm));
+        fb = __shfl_sync(0xffffffffu, fb, fl);
+        if (has) flist[fb + __popc(fm & ((1u << lane) - 1u))] = 4 * cell + f;
+      }
+    }
   }
 }
 
 __global__ void __launch_bounds__(256)
     k_interface_cells(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
-                      const double *__restrict__ vof, const double *__restrict__ dvof, const int *__restrict__ list,
-                      const int *__restrict__ count, double *__restrict__ fluxx, double *__restrict__ fluxy) {
-  list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
-  count += (size_t)blockIdx.z * (1);
-  const int n = *count;
+                      const double *__restrict__ vof, const double *__restrict__ dvof, const int *__restrict__ flist,
+                      const int *__restrict__ fcount, double *__restrict__ fluxx, double *__restrict__ fluxy) {
+  flist += (size_t)blockIdx.z * (4 * (size_t)g.nx * g.ny);
+  fcount += (size_t)blockIdx.z * (1);
+  const int n = *fcount;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
   const size_t q = g.p2 / 2;
+  // one thread per upwind face of an interface cell: every thread runs the
+  // same instructions (no face branches)
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int id = list[t];
+    const int code = flist[t];
+    const int id = code >> 2, f = code & 3;
     const int r0 = id / g.nx, I = id - r0 * g.nx + 1;
     const int J = r0 + 1, r = r0 + zr, rp = wrap(J + 1, g.ny) + zr;
     const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
@@ -325,14 +357,17 @@ __global__ void __launch_bounds__(256)
     const double inv = inv_norm(fma(mx, mx, my * my));
     const double n0 = mx * inv, n1 = my * inv;
     const double K = rcp_nr(vof[ix(g, r, I)]) - 1.;
-    // x faces I (left) and I + 1 (right); the wall faces belong to k_flux_force
-    const double ul = ux[ix(g, r, I - 1)], ur = ux[ix(g, r, I)];
-    if (I >= 2 && neg(ul)) fluxx[ix(g, r, I - 1)] = ul * thinc_face(n0, n1, K);
-    if (I < g.nx && !neg(ur)) fluxx[ix(g, r, I)] = ur * thinc_face(-n0, n1, K);
-    // y faces J - 1/2 (bottom, stored in row J) and J + 1/2 (row J + 1)
-    const double vb = uy[ix(g, r, I)], vt = uy[ix(g, rp, I)];
-    if (neg(vb)) fluxy[ix(g, r, I)] = vb * thinc_face(n1, n0, K);
-    if (!neg(vt)) fluxy[ix(g, rp, I)] = vt * thinc_face(-n1, n0, K);
+    // face f: 0 left (x face I), 1 right (x face I + 1), 2 bottom (y face J - 1/2), 3 top (J + 1/2)
+    const bool xf = f < 2;
+    const double na = xf ? n0 : n1, nb = xf ? n1 : n0;
+    const double ena = (f & 1) ? -na : na;  // -2 n_a s with s = -1/2 (left, bottom) or +1/2
+    const size_t at = xf ? ix(g, r, I - 1 + f) : ix(g, f == 2 ? r : rp, I);
+    const double vel = xf ? ux[at] : uy[at];
+    const double fl = vel * thinc_face(ena, nb, K);
+    if (xf)
+      fluxx[at] = fl;
+    else
+      fluxy[at] = fl;
   }
 }
 
@@ -1271,10 +1306,12 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
                             const double *ux, const double *uy, const double *den0, int stage) {
   const dim3 gr = tile_grid(b.tiles, TK_FLUX_FORCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_FLUX_FORCE);
   if (stage == 0) {
-    cudaMemsetAsync(b.icount, 0, sizeof(int) * g.nc, s);
-    k_curv_list<<<tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s>>>(g, m, b.vof, b.dvof, b.curv, b.ilist, b.icount);
+    cudaMemsetAsync(b.icount, 0, sizeof(int) * 2 * g.nc, s);  // cell and face counts
+    k_curv_list<<<tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s>>>(
+        g, m, b.vof, b.dvof, ux, uy, b.curv, b.ilist, b.icount, b.flist, b.fcount);
   } else if (stage == 1) {
-    k_interface_cells<<<dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s>>>(g, m, ux, uy, b.vof, b.dvof, b.ilist, b.icount, b.fluxx, b.fluxy);
+    k_interface_cells<<<dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s>>>(
+        g, m, ux, uy, b.vof, b.dvof, b.flist, b.fcount, b.fluxx, b.fluxy);
   } else if (stage == 2) {
     k_flux_force<true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                            b.fluxy, b.ifrcx, b.ifrcy);

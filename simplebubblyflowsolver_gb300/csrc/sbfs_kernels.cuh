@@ -39,8 +39,11 @@ struct Bufs {
   unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
   double *scalars;             // kScalars doubles
   int *status;                 // device error word
-  // interface cells of the current substage (linear index (J-1)*nx + I-1) and their count
+  // interface cells of the current substage (linear index (J-1)*nx + I-1) and their count;
+  // the faces those cells are upwind of (4 * cell + face, face 0..3 = left, right, bottom, top)
+  // and their count (fcount = icount + nc)
   int *ilist, *icount;
+  int *flist, *fcount;
   // launch shapes (host side)
   Tiles tiles;
 };
