@@ -91,6 +91,10 @@ struct Ctx {
   // safety factor); graphs are dropped when any of them changes
   std::vector<double> graph_sig;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  // side stream of the step: decide_dt beside k_props, k_stress beside the
+  // interface kernels (fork / join events)
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t evf = nullptr, evd = nullptr, evs = nullptr;
   // diagnostics partials / result and statistics sums (allocated on first use)
   double *diag_part = nullptr, *diag_out = nullptr;
   double *st_ux1 = nullptr, *st_uy1 = nullptr, *st_vof1 = nullptr;
@@ -102,6 +106,10 @@ struct Ctx {
     if (small_host) cudaFreeHost(small_host);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
+    if (evf) cudaEventDestroy(evf);
+    if (evd) cudaEventDestroy(evd);
+    if (evs) cudaEventDestroy(evs);
+    if (s2) cudaStreamDestroy(s2);
     if (s) cudaStreamDestroy(s);
   }
 };
@@ -369,6 +377,10 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   c->hxxf.assign(d->hxxf, d->hxxf + c->nx + 1);
   CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
   CK(cudaEventCreate(&c->e0));
+  CK(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&c->evf, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->evs, cudaEventDisableTiming));
   CK(cudaEventCreate(&c->e1));
   cudaError_t e = configure_kernels();
   if (e != cudaSuccess) return fail("configure_kernels: %s", cudaGetErrorString(e));
@@ -563,7 +575,11 @@ void timed(Ctx &c, int cls, F &&launch) {
   g_prof.marks.push_back({cls, {a, b}});
 }
 
-void enqueue_substage(Ctx &c, int k) {
+// par: run decide_dt (already on the side stream, joined before the first
+// use of its scalars, when wait_dt) and k_stress on the side stream.  Both
+// only read what the main stream has finished when they are forked, and the
+// main stream waits for them before anything reads what they write.
+void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   Bufs &b = c.b;
   if (k != 0) c.isrc ^= 1;  // stash the previous stage's sources (pointer swap)
   double *ux = c.U[c.iu], *uy = c.V[c.iu], *uxs = c.U[c.iu ^ 1], *uys = c.V[c.iu ^ 1];
@@ -574,14 +590,25 @@ void enqueue_substage(Ctx &c, int k) {
   double *sva = c.SV[c.isrc], *svb = c.SV[c.isrc ^ 1];
   const double *sc = b.scalars;
   timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+  if (par) {
+    // txx, txy, tyy need the velocity and the viscosities just computed
+    cudaEventRecord(c.evf, c.s);
+    cudaStreamWaitEvent(c.s2, c.evf, 0);
+    launch_stress(c.s2, c.g, c.m, b, ux, uy);
+    cudaEventRecord(c.evs, c.s2);
+  }
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
   const bool learned = g_curv_model != 0;
   if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
   timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
   timed(c, KC_FLUX_FORCE,
         [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
+  if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
-  timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
+  if (par)
+    cudaStreamWaitEvent(c.s, c.evs, 0);
+  else
+    timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
   timed(c, KC_PREDICT, [&] {
     launch_predict(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, b.mfluxx, b.mfluxy, den0, den1, sxa, sxb,
                    nullptr, sya, syb, nullptr);
@@ -598,9 +625,18 @@ void enqueue_substage(Ctx &c, int k) {
 constexpr int kKernelsPerStep = 1 + 3 * 11;
 
 void enqueue_step(Ctx &c) {
-  timed(c, KC_DECIDE_DT,
-        [&] { launch_decide_dt(c.s, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]); });
-  for (int k = 0; k < 3; ++k) enqueue_substage(c, k);
+  // profiled steps keep every launch on the main stream (events per launch)
+  const bool par = !g_prof.on;
+  if (par) {
+    cudaEventRecord(c.evf, c.s);
+    cudaStreamWaitEvent(c.s2, c.evf, 0);
+    launch_decide_dt(c.s2, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]);
+    cudaEventRecord(c.evd, c.s2);
+  } else {
+    timed(c, KC_DECIDE_DT,
+          [&] { launch_decide_dt(c.s, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]); });
+  }
+  for (int k = 0; k < 3; ++k) enqueue_substage(c, k, par, par && k == 0);
 }
 
 // ---- autotuner of the launch shapes (block shape of each stencil kernel,
