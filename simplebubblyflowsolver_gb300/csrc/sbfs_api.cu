@@ -94,7 +94,8 @@ struct Ctx {
   // side stream of the step: decide_dt beside k_props, k_stress beside the
   // interface kernels (fork / join events)
   cudaStream_t s2 = nullptr;
-  cudaEvent_t evf = nullptr, evd = nullptr, evs = nullptr;
+  cudaEvent_t evf = nullptr, evd = nullptr, evs = nullptr, evp = nullptr;
+  bool props_ahead = false;  // the next substage's k_props is already on the side stream
   // diagnostics partials / result and statistics sums (allocated on first use)
   double *diag_part = nullptr, *diag_out = nullptr;
   double *st_ux1 = nullptr, *st_uy1 = nullptr, *st_vof1 = nullptr;
@@ -109,6 +110,7 @@ struct Ctx {
     if (evf) cudaEventDestroy(evf);
     if (evd) cudaEventDestroy(evd);
     if (evs) cudaEventDestroy(evs);
+    if (evp) cudaEventDestroy(evp);
     if (s2) cudaStreamDestroy(s2);
     if (s) cudaStreamDestroy(s);
   }
@@ -381,6 +383,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   CK(cudaEventCreateWithFlags(&c->evf, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evs, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
   CK(cudaEventCreate(&c->e1));
   cudaError_t e = configure_kernels();
   if (e != cudaSuccess) return fail("configure_kernels: %s", cudaGetErrorString(e));
@@ -589,7 +592,12 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   double *sya = c.SY[c.isrc], *syb = c.SY[c.isrc ^ 1];
   double *sva = c.SV[c.isrc], *svb = c.SV[c.isrc ^ 1];
   const double *sc = b.scalars;
-  timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+  if (c.props_ahead) {
+    cudaStreamWaitEvent(c.s, c.evp, 0);
+    c.props_ahead = false;
+  } else {
+    timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+  }
   if (par) {
     // txx, txy, tyy need the velocity and the viscosities just computed
     cudaEventRecord(c.evf, c.s);
@@ -605,6 +613,16 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
         [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
   if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
+  if (par && k < 2) {
+    // the next substage's viscosities and corner normals need only the new
+    // vof: they run beside this substage's predictor, Poisson solve and
+    // correction, none of which reads them
+    cudaEventRecord(c.evf, c.s);
+    cudaStreamWaitEvent(c.s2, c.evf, 0);
+    launch_props(c.s2, c.g, c.m, c.ph, b, false, true, true, nullptr);
+    cudaEventRecord(c.evp, c.s2);
+    c.props_ahead = true;
+  }
   if (par)
     cudaStreamWaitEvent(c.s, c.evs, 0);
   else
@@ -627,6 +645,7 @@ constexpr int kKernelsPerStep = 1 + 3 * 11;
 void enqueue_step(Ctx &c) {
   // profiled steps keep every launch on the main stream (events per launch)
   const bool par = !g_prof.on;
+  c.props_ahead = false;
   if (par) {
     cudaEventRecord(c.evf, c.s);
     cudaStreamWaitEvent(c.s2, c.evf, 0);
