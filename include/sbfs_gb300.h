@@ -216,8 +216,9 @@ int sbfs_profile_batch_steps(int nsteps, float *ms_per_class, int *launches_per_
 int sbfs_set_autotune(int on);
 /* shapes in use (group -1: the single-case context): bx[7], by[7] for
  * props, curvature list, flux/force, vof advance, stress, predict,
- * correct; the Poisson transform width and wavenumbers per tridiagonal block */
-int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb);
+ * correct; the Poisson transform width, wavenumbers per tridiagonal block
+ * and warps per tridiagonal system */
+int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps);
 /* number of grid groups and cases per group of the current batch */
 int sbfs_batch_groups(int *ngroups, int *cases_per_group);
 int sbfs_batch_release(void);

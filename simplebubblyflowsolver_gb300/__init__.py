@@ -214,13 +214,15 @@ class GpuLibrary(ReferenceAPI):
         by = (C.c_int * 7)()
         fw = C.c_int(0)
         mb = C.c_int(0)
+        gw = C.c_int(0)
         self.lib.sbfs_tiles.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                        C.POINTER(C.c_int)]
-        self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb))
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb), C.byref(gw))
         names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_stress", "k_predict", "k_correct"]
         out = {n: f"{bx[k]}x{by[k]}" for k, n in enumerate(names)}
         out["fft_cols"] = fw.value
         out["tdm_modes"] = mb.value
+        out["tdm_warps"] = gw.value
         return out
 
     def batch_groups(self):

@@ -314,53 +314,67 @@ double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interfa
 // k_poisson_tdm, and the FFT twiddles
 int upload_poisson(Ctx &c, const domain_t *d) {
   const int nx = c.nx, ny = c.ny, M1 = ny / 2 + 1;
-  const int L = tdm_chunk(nx), NP = 32 * L;
   const double pi = 3.14159265358979323846;
   const double dx = d->lengths[0] / nx;
   const double offx = 1. / (dx * dx);
   const double offy = 1. / d->hy / d->hy;
-  std::vector<double> w(NP), v(NP), P(NP), Q(NP);
-  std::vector<double> fac((size_t)M1 * NP * 4);
+  // Thomas pivots per wavenumber: x_i = w_i r_i - v_i x_{i-1} forward,
+  // x_i -= v_i x_{i+1} backward
+  std::vector<double> W((size_t)M1 * nx), V((size_t)M1 * nx);
   for (int m = 0; m < M1; ++m) {
     const double s = sin(pi * m / ny);
     const double lam = -4. * offy * s * s;
     double v_prev = 0.;
-    for (int i = 0; i < NP; ++i) {
-      if (i >= nx) {  // padding rows decouple and solve to zero
-        w[i] = 0.;
-        v[i] = 0.;
-        continue;
-      }
+    for (int i = 0; i < nx; ++i) {
       const double diag = (i == 0 || i == nx - 1 ? -offx : -2. * offx) + lam;
       const double piv = diag - (i == 0 ? 0. : offx * v_prev);
+      double w, v;
       if (i == nx - 1 && fabs(piv) < 1.e-10 * offx) {
         // singular mode (m = 0, Neumann-Neumann): pin the last unknown; the
         // kernel removes the mean afterwards
-        w[i] = 0.;
-        v[i] = 0.;
+        w = 0.;
+        v = 0.;
       } else {
-        w[i] = 1. / piv;
-        v[i] = offx * w[i];
+        w = 1. / piv;
+        v = offx * w;
       }
-      v_prev = v[i];
-    }
-    for (int l = 0; l < 32; ++l) {
-      const int s0 = l * L, e0 = s0 + L - 1;
-      double acc = 1.;
-      for (int i = s0; i <= e0; ++i) P[i] = acc *= -v[i];
-      acc = 1.;
-      for (int i = e0; i >= s0; --i) Q[i] = acc *= -v[i];
-    }
-    for (int i = 0; i < NP; ++i) {
-      const int l = i / L, k = i % L;
-      double *o = &fac[(((size_t)m * L + k) * 32 + l) * 4];
-      o[0] = w[i];
-      o[1] = v[i];
-      o[2] = P[i];
-      o[3] = Q[i];
+      W[(size_t)m * nx + i] = w;
+      V[(size_t)m * nx + i] = v;
+      v_prev = v;
     }
   }
-  CK(cudaMemcpyAsync(c.b.tdm_fac, fac.data(), fac.size() * sizeof(double), cudaMemcpyHostToDevice, c.s));
+  // chunked layouts for 1, 2 and 4 warps per system: fac[((m L + k) lanes + l)]
+  // = (w, v, P, Q) of row l L + k, P and Q the cumulative products of -v
+  // within the chunk (forward, backward); padding rows decouple and solve to 0
+  for (int gi = 0; gi < 3; ++gi) {
+    const int G = 1 << gi, lanes = 32 * G, L = tdm_chunk(nx, G), NP = lanes * L;
+    std::vector<double> fac((size_t)M1 * NP * 4);
+    std::vector<double> w(NP), v(NP), P(NP), Q(NP);
+    for (int m = 0; m < M1; ++m) {
+      for (int i = 0; i < NP; ++i) {
+        w[i] = i < nx ? W[(size_t)m * nx + i] : 0.;
+        v[i] = i < nx ? V[(size_t)m * nx + i] : 0.;
+      }
+      for (int l = 0; l < lanes; ++l) {
+        const int s0 = l * L, e0 = s0 + L - 1;
+        double acc = 1.;
+        for (int i = s0; i <= e0; ++i) P[i] = acc *= -v[i];
+        acc = 1.;
+        for (int i = e0; i >= s0; --i) Q[i] = acc *= -v[i];
+      }
+      for (int i = 0; i < NP; ++i) {
+        const int l = i / L, k = i % L;
+        double *o = &fac[(((size_t)m * L + k) * lanes + l) * 4];
+        o[0] = w[i];
+        o[1] = v[i];
+        o[2] = P[i];
+        o[3] = Q[i];
+      }
+    }
+    CK(cudaMemcpyAsync(c.b.tdm_fac[gi], fac.data(), fac.size() * sizeof(double), cudaMemcpyHostToDevice, c.s));
+    // fac dies at the end of this iteration: wait for the copy
+    CK(cudaStreamSynchronize(c.s));
+  }
   std::vector<double2> tw(M1);
   for (int m = 0; m < M1; ++m) tw[m] = make_double2(cos(2. * pi * m / ny), -sin(2. * pi * m / ny));
   CK(cudaMemcpyAsync(c.b.twiddle, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, c.s));
@@ -411,6 +425,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   g.phys = nullptr;
   Bufs &b = c->b;
   b.tiles = default_tiles();
+  b.tiles.tdm_g = tdm_warps_for(c->nx, c->ny, nc);
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
@@ -422,8 +437,11 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   double *tmp = nullptr;
   if (dalloc(*c, &tmp, 2 * (size_t)c->nx * M1 * nc)) return 1;
   b.spec = reinterpret_cast<double2 *>(tmp);
-  if (dalloc(*c, &tmp, 4 * (size_t)32 * tdm_chunk(c->nx) * M1)) return 1;
-  b.tdm_fac = reinterpret_cast<double2 *>(tmp);
+  for (int gi = 0; gi < 3; ++gi) {
+    const int G = 1 << gi;
+    if (dalloc(*c, &tmp, 4 * (size_t)32 * G * tdm_chunk(c->nx, G) * M1)) return 1;
+    b.tdm_fac[gi] = reinterpret_cast<double2 *>(tmp);
+  }
   if (dalloc(*c, &tmp, 2 * (size_t)M1)) return 1;
   b.twiddle = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, ((size_t)c->nx + 8) * nc)) return 1;
@@ -687,11 +705,13 @@ int autotune(Ctx &c) {
   };
   const unsigned short shapes[][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {32, 2}, {64, 2}, {16, 16}, {256, 1}};
   const int nshape = sizeof(shapes) / sizeof(shapes[0]);
-  std::vector<int> fws, mbs;
+  std::vector<int> fws;
+  std::vector<std::pair<int, int>> tdms;  // (wavenumbers per block, warps per system)
   for (int w : {2, 4, 8})
     if (fft_w_fits(c.ny, w)) fws.push_back(w);
+  const int G = c.b.tiles.tdm_g;  // fixed by the grid
   for (int mb : {1, 2, 4})
-    if (poisson_tdm_smem(c.nx) / poisson_tdm_modes(c.nx) * mb <= 200 * 1024) mbs.push_back(mb);
+    if (G * mb <= 4 && poisson_tdm_smem(c.nx, mb, G) <= 200 * 1024) tdms.push_back({mb, G});
   const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT,
                                -1, -1, -1, TK_CORRECT, -1, -1};
   Tiles best = c.b.tiles;
@@ -706,7 +726,8 @@ int autotune(Ctx &c) {
       cand.by[k] = shapes[t][1];
     }
     cand.fft_w = fws[t % fws.size()];
-    cand.tdm_mb = mbs[t % mbs.size()];
+    cand.tdm_mb = tdms[t % tdms.size()].first;
+    cand.tdm_g = tdms[t % tdms.size()].second;
     c.b.tiles = cand;
     if (restore()) {
       rc = 1;
@@ -744,6 +765,7 @@ int autotune(Ctx &c) {
     if (ms[KC_POISSON_TDM] < best_tdm) {
       best_tdm = ms[KC_POISSON_TDM];
       best.tdm_mb = cand.tdm_mb;
+      best.tdm_g = cand.tdm_g;
     }
   }
   c.b.tiles = rc ? keep : best;
@@ -1395,7 +1417,7 @@ int sbfs_set_autotune(int on) {
 }
 
 // launch shapes in use: group -1 = the single-case context, else batch group
-int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb) {
+int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps) {
   Ctx *c = nullptr;
   if (group < 0)
     c = g_ctx.get();
@@ -1407,7 +1429,8 @@ int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb) {
     by[k] = c->b.tiles.by[k];
   }
   *fft_w = c->b.tiles.fft_w;
-  *tdm_mb = c->b.tiles.tdm_mb > 0 ? c->b.tiles.tdm_mb : poisson_tdm_modes(c->nx);
+  *tdm_mb = tdm_modes_per_block(c->b.tiles, c->nx);
+  *tdm_warps = c->b.tiles.tdm_g > 0 ? c->b.tiles.tdm_g : 1;
   return 0;
 }
 

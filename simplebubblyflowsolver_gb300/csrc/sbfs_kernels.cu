@@ -741,15 +741,17 @@ __global__ void __launch_bounds__(256)
 // pivot pinned (w = v = 0) and is shifted to zero mean.
 // Shared memory: per system a planar array with an odd lane stride S.
 __global__ void __launch_bounds__(256)
-    k_poisson_tdm(Grid g, int MB, int L, int S, const double4_32a *__restrict__ fac, double2 *__restrict__ spec) {
+    k_poisson_tdm(Grid g, int MB, int G, int L, int S, const double4_32a *__restrict__ fac, double2 *__restrict__ spec) {
   extern __shared__ double2 smem_d2[];
   double *sm = reinterpret_cast<double *>(smem_d2);
+  __shared__ double xch[8][4][2];  // per system of the block, per warp of the system: a chunk-map total
   const int nx = g.nx, M1 = g.ny / 2 + 1;
   const int m0 = blockIdx.x * MB;
   const int nm = min(MB, M1 - m0);
-  const int sys_len = 32 * S;
+  const int lanes = 32 * G;  // chunks per system
+  const int sys_len = lanes * S;
   // ---- load: spec[i][m0 + q] -> planar (q, re) and (q, im) arrays
-  for (int t = threadIdx.x; t < 32 * L * nm; t += blockDim.x) {
+  for (int t = threadIdx.x; t < lanes * L * nm; t += blockDim.x) {
     const int i = t / nm, q = t - i * nm;
     const int at = (i / L) * S + (i % L);
     double2 v = make_double2(0., 0.);
@@ -758,21 +760,26 @@ __global__ void __launch_bounds__(256)
     sm[(2 * q + 1) * sys_len + at] = v.y;
   }
   __syncthreads();
+  // warp -> system (2 per wavenumber: real, imaginary) and its part sub of G;
+  // chunk j of the system = this lane's L rows
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < 2 * nm) {
-    const int q = warp >> 1;
-    const int m = m0 + q;
-    double *x = sm + warp * sys_len + lane * S;
-    const double4_32a *f = fac + (size_t)m * L * 32 + lane;
+  const int sys = warp / G, sub = warp - sys * G, j = sub * 32 + lane;
+  const bool act = sys < 2 * nm;  // warp-uniform
+  const int m = m0 + (sys >> 1);
+  double *x = sm + sys * sys_len + j * S;
+  const double4_32a *f = fac + (size_t)m * L * lanes + j;
+  double T = 0., B = 0.;
+  if (act) {
     // forward, local from a zero carry
     double t = 0.;
 #pragma unroll 8
     for (int k = 0; k < L; ++k) {
-      const double4_32a c = f[(size_t)k * 32];
+      const double4_32a c = f[(size_t)k * lanes];
       t = fma(-c.y, t, c.x * x[k]);
       x[k] = t;
     }
-    double T = t, B = f[(size_t)(L - 1) * 32].z;
+    T = t;
+    B = f[(size_t)(L - 1) * lanes].z;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const double Tp = __shfl_up_sync(0xffffffffu, T, d), Bp = __shfl_up_sync(0xffffffffu, B, d);
@@ -781,39 +788,79 @@ __global__ void __launch_bounds__(256)
         B *= Bp;
       }
     }
-    double carry = __shfl_up_sync(0xffffffffu, T, 1);
-    if (lane == 0) carry = 0.;
+  }
+  // the map of the system's chunks before this warp's (G > 1: warp totals)
+  double Cin = 0.;
+  if (G > 1) {
+    if (act && lane == 31) {
+      xch[sys][sub][0] = T;
+      xch[sys][sub][1] = B;
+    }
+    __syncthreads();
+    if (act)
+      for (int q = 0; q < sub; ++q) Cin = fma(xch[sys][q][1], Cin, xch[sys][q][0]);
+    __syncthreads();
+  }
+  double Sx = 0., Cc = 0.;
+  if (act) {
+    const double Tu = __shfl_up_sync(0xffffffffu, T, 1), Bu = __shfl_up_sync(0xffffffffu, B, 1);
+    const double carry = lane == 0 ? Cin : fma(Bu, Cin, Tu);
     // fix up the forward solution, then the backward sweep from a zero carry
     double u = 0.;
 #pragma unroll 8
     for (int k = L - 1; k >= 0; --k) {
-      const double4_32a c = f[(size_t)k * 32];
+      const double4_32a c = f[(size_t)k * lanes];
       const double y = fma(c.z, carry, x[k]);
       u = fma(-c.y, u, y);
       x[k] = u;
     }
-    double Sx = u, C = f[0].w;
+    Sx = u;
+    Cc = f[0].w;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      const double Sp = __shfl_down_sync(0xffffffffu, Sx, d), Cp = __shfl_down_sync(0xffffffffu, C, d);
+      const double Sp = __shfl_down_sync(0xffffffffu, Sx, d), Cp = __shfl_down_sync(0xffffffffu, Cc, d);
       if (lane + d < 32) {
-        Sx = fma(C, Sp, Sx);
-        C *= Cp;
+        Sx = fma(Cc, Sp, Sx);
+        Cc *= Cp;
       }
     }
-    double next = __shfl_down_sync(0xffffffffu, Sx, 1);
-    if (lane == 31) next = 0.;
+  }
+  // the map of the chunks after this warp's
+  double Din = 0.;
+  if (G > 1) {
+    if (act && lane == 0) {
+      xch[sys][sub][0] = Sx;
+      xch[sys][sub][1] = Cc;
+    }
+    __syncthreads();
+    if (act)
+      for (int q = G - 1; q > sub; --q) Din = fma(xch[sys][q][1], Din, xch[sys][q][0]);
+    __syncthreads();
+  }
+  const bool gauge = act && m == 0;  // the singular mode: zero mean over x (imaginary part is 0)
+  double acc = 0.;
+  if (act) {
+    const double Sd = __shfl_down_sync(0xffffffffu, Sx, 1), Cd = __shfl_down_sync(0xffffffffu, Cc, 1);
+    const double next = lane == 31 ? Din : fma(Cd, Din, Sd);
 #pragma unroll 8
-    for (int k = 0; k < L; ++k) x[k] = fma(f[(size_t)k * 32].w, next, x[k]);
-    if (m == 0) {
-      // gauge of the singular mode: zero mean over x (imaginary part is 0)
-      double acc = 0.;
-      for (int k = 0; k < L; ++k) acc += (lane * L + k < nx) ? x[k] : 0.;
+    for (int k = 0; k < L; ++k) x[k] = fma(f[(size_t)k * lanes].w, next, x[k]);
+    if (gauge) {
+      for (int k = 0; k < L; ++k) acc += (j * L + k < nx) ? x[k] : 0.;
 #pragma unroll
       for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
-      const double mean = (warp & 1) ? 0. : acc / nx;
-      for (int k = 0; k < L; ++k) x[k] = (warp & 1) ? 0. : x[k] - mean;
     }
+  }
+  if (G > 1) {
+    if (gauge && lane == 0) xch[sys][sub][0] = acc;
+    __syncthreads();
+    if (gauge) {
+      acc = 0.;
+      for (int q = 0; q < G; ++q) acc += xch[sys][q][0];
+    }
+  }
+  if (gauge) {
+    const double mean = (sys & 1) ? 0. : acc / nx;
+    for (int k = 0; k < L; ++k) x[k] = (sys & 1) ? 0. : x[k] - mean;
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nx * nm; t += blockDim.x) {
@@ -1227,16 +1274,35 @@ Tiles default_tiles() {
   }
   t.fft_w = kFftCols;
   t.tdm_mb = 0;
+  t.tdm_g = 1;
   return t;
 }
-int tdm_chunk(int nx) { return (nx + 31) / 32; }
-int tdm_stride(int nx) { return tdm_chunk(nx) | 1; }
+int tdm_chunk(int nx, int G) { return (nx + 32 * G - 1) / (32 * G); }
+int tdm_stride(int nx, int G) { return tdm_chunk(nx, G) | 1; }
 int poisson_tdm_modes(int nx) {
-  const size_t per_mode = 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double);
+  const size_t per_mode = 2 * 32 * (size_t)tdm_stride(nx, 1) * sizeof(double);
   return per_mode * 4 <= 200 * 1024 ? 4 : (per_mode * 2 <= 200 * 1024 ? 2 : 1);
 }
-size_t poisson_tdm_smem(int nx, int mb) { return 2 * 32 * (size_t)tdm_stride(nx) * sizeof(double) * mb; }
-size_t poisson_tdm_smem(int nx) { return poisson_tdm_smem(nx, poisson_tdm_modes(nx)); }
+size_t poisson_tdm_smem(int nx, int mb, int G) {
+  return 2 * 32 * (size_t)G * tdm_stride(nx, G) * sizeof(double) * mb;
+}
+size_t poisson_tdm_smem(int nx) { return poisson_tdm_smem(nx, poisson_tdm_modes(nx), 1); }
+int tdm_group_index(int G) { return G == 4 ? 2 : (G == 2 ? 1 : 0); }
+// warps per tridiagonal system for a grid of nc cases: the fewest (1, 2, 4)
+// that put about 2048 warps in flight (13 per SM), as long as every lane
+// keeps at least two rows.  A rule of the grid, not a tuned choice: it sets
+// how the chunk maps are combined, and so the rounding of the solve.
+int tdm_modes_per_block(const Tiles &t, int nx) {
+  const int G = t.tdm_g > 0 ? t.tdm_g : 1;
+  const int mb = t.tdm_mb > 0 ? t.tdm_mb : poisson_tdm_modes(nx);
+  return mb * G > 4 ? 4 / G : mb;  // at most 256 threads a block
+}
+int tdm_warps_for(int nx, int ny, int nc) {
+  const long systems = 2L * (ny / 2 + 1) * nc;
+  int G = 1;
+  while (G < 4 && systems * G < 2048 && tdm_chunk(nx, 2 * G) >= 2) G *= 2;
+  return G;
+}
 
 cudaError_t configure_kernels() {
   cudaError_t e;
@@ -1373,10 +1439,12 @@ void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const doub
 }
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
-  const int mb = b.tiles.tdm_mb > 0 ? b.tiles.tdm_mb : poisson_tdm_modes(g.nx);
+  const int G = b.tiles.tdm_g > 0 ? b.tiles.tdm_g : 1;
+  const int mb = tdm_modes_per_block(b.tiles, g.nx);
   const int M1 = g.ny / 2 + 1;
-  k_poisson_tdm<<<dim3((M1 + mb - 1) / mb, 1, g.nc), 64 * mb, poisson_tdm_smem(g.nx, mb), s>>>(
-      g, mb, tdm_chunk(g.nx), tdm_stride(g.nx), reinterpret_cast<const double4_32a *>(b.tdm_fac), b.spec);
+  k_poisson_tdm<<<dim3((M1 + mb - 1) / mb, 1, g.nc), 64 * mb * G, poisson_tdm_smem(g.nx, mb, G), s>>>(
+      g, mb, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
+      reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]), b.spec);
 }
 
 template <int W>

@@ -15,6 +15,8 @@ struct Tiles {
   unsigned short bx[TK_COUNT], by[TK_COUNT];  // block shape (bx * by <= 256)
   int fft_w;   // columns per block of the Poisson transforms: 2, 4 or 8
   int tdm_mb;  // wavenumbers per block of the tridiagonal solves (0: by size)
+  int tdm_g;   // warps per tridiagonal system: 1, 2 or 4 (tdm_g * tdm_mb <= 4), set by
+               // tdm_warps_for from the grid (it changes the rounding, so it is not tuned)
 };
 Tiles default_tiles();
 
@@ -33,7 +35,8 @@ struct Bufs {
   // face factors e = rho_ref / rho^{k+1} - 1 at ux and uy faces
   double *irhox, *irhoy;
   // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
-  double2 *spec, *tdm_fac;  // tdm_fac: (w, v, P, Q) per row, see k_poisson_tdm
+  double2 *spec;
+  double2 *tdm_fac[3];  // (w, v, P, Q) per row for 1, 2, 4 warps per system, see k_poisson_tdm
   double2 *twiddle;  // exp(-2 pi i m / ny), m = 0..ny/2
   // decide_dt accumulators and per-step scalars
   unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
@@ -102,7 +105,11 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
 // smem budget checks (host side)
 int poisson_fft_cols(int ny);
 int poisson_tdm_modes(int nx);
-int tdm_chunk(int nx);
+int tdm_chunk(int nx, int G);
+int tdm_group_index(int G);  // 1, 2, 4 -> 0, 1, 2
+int tdm_warps_for(int nx, int ny, int nc);
+int tdm_modes_per_block(const Tiles &t, int nx);
+size_t poisson_tdm_smem(int nx, int mb, int G);
 size_t poisson_fft_smem(int ny, int w);
 bool fft_w_fits(int ny, int w);
 size_t poisson_tdm_smem(int nx);
