@@ -674,17 +674,14 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   double2 *Z = fft_rows<W>(A, B, M, tw, false);
-  // real-to-complex split, times 2: X_m = (z_m + conj z_{M-m}) + w^m (-i)(z_m - conj z_{M-m})
+  // the packed transform z_m, m < M; k_poisson_tdm does the real-to-complex
+  // split (there the FP64 pipe has room)
   const int M1 = M + 1;
-  for (int t = threadIdx.x; t < W * M1; t += blockDim.x) {
-    const int c = t / M1, mm = t - c * M1;
+  for (int t = threadIdx.x; t < W * M; t += blockDim.x) {
+    const int c = t / M, mm = t - c * M;
     const int I = I0 + c;
     if (I > g.nx) continue;
-    const double2 zm = Z[c * M + (mm == M ? 0 : mm)];
-    const double2 zr = Z[c * M + (mm == 0 ? 0 : M - mm)];
-    const double2 E = make_double2(zm.x + zr.x, zm.y - zr.y);
-    const double2 O = make_double2(zm.y + zr.y, zr.x - zm.x);  // -i (zm - conj zr)
-    spec[(size_t)(I - 1) * M1 + mm] = cadd(E, cmul(tw[mm], O));
+    spec[(size_t)(I - 1) * M1 + mm] = Z[c * M + mm];
   }
 }
 
@@ -699,17 +696,9 @@ __global__ void __launch_bounds__(256)
   for (int t = threadIdx.x; t < W * M; t += blockDim.x) {
     const int c = t / M, mm = t - c * M;
     const int I = I0 + c;
-    double2 z = make_double2(0., 0.);
-    if (I <= g.nx) {
-      const double2 xm = spec[(size_t)(I - 1) * M1 + mm];
-      const double2 xr = spec[(size_t)(I - 1) * M1 + (M - mm)];
-      const double2 E = make_double2(xm.x + xr.x, xm.y - xr.y);
-      const double2 D = make_double2(xm.x - xr.x, xm.y + xr.y);
-      const double2 w = make_double2(tw[mm].x, -tw[mm].y);
-      const double2 O = cmul(D, w);
-      z = make_double2(E.x - O.y, E.y + O.x);
-    }
-    A[c * M + mm] = z;
+    // the packed input of the inverse transform, complex-to-real split done
+    // by k_poisson_tdm
+    A[c * M + mm] = I <= g.nx ? spec[(size_t)(I - 1) * M1 + mm] : make_double2(0., 0.);
   }
   __syncthreads();
   const double2 *zr = fft_rows<W>(A, B, M, tw, true);
@@ -740,32 +729,49 @@ __global__ void __launch_bounds__(256)
 // The singular m = 0 mode (Neumann in x, constant null space) has its last
 // pivot pinned (w = v = 0) and is shifted to zero mean.
 // Shared memory: per system a planar array with an odd lane stride S.
-__global__ void __launch_bounds__(256)
-    k_poisson_tdm(Grid g, int MB, int G, int L, int S, const double4_32a *__restrict__ fac, double2 *__restrict__ spec) {
+__global__ void __launch_bounds__(512)
+    k_poisson_tdm(Grid g, int PB, int G, int L, int S, const double4_32a *__restrict__ fac,
+                  const double2 *__restrict__ tw, double2 *__restrict__ spec) {
   extern __shared__ double2 smem_d2[];
   double *sm = reinterpret_cast<double *>(smem_d2);
-  __shared__ double xch[8][4][2];  // per system of the block, per warp of the system: a chunk-map total
-  const int nx = g.nx, M1 = g.ny / 2 + 1;
-  const int m0 = blockIdx.x * MB;
-  const int nm = min(MB, M1 - m0);
-  const int lanes = 32 * G;  // chunks per system
+  __shared__ double xch[16][4][2];  // per system of the block, per warp of the system: a chunk-map total
+  const int nx = g.nx, M = g.ny / 2, M1 = M + 1;
+  const int p0 = blockIdx.x * PB;
+  const int np = min(PB, M / 2 + 1 - p0);  // pairs (p, M - p), p = 0 .. M/2
+  const int lanes = 32 * G;                // chunks per system
   const int sys_len = lanes * S;
-  // ---- load: spec[i][m0 + q] -> planar (q, re) and (q, im) arrays
-  for (int t = threadIdx.x; t < lanes * L * nm; t += blockDim.x) {
-    const int i = t / nm, q = t - i * nm;
+  double2 *sp = spec + (size_t)blockIdx.z * g.css;
+  // ---- load the packed transform of both wavenumbers of each pair, split
+  // it (real-to-complex, times 2: X_m = (z_m + conj z_{M-m}) + w^m (-i)(z_m -
+  // conj z_{M-m})) into four planar systems: X_p re, im, X_{M-p} re, im
+  for (int t = threadIdx.x; t < lanes * L * np; t += blockDim.x) {
+    const int i = t / np, q = t - i * np;
+    const int p = p0 + q;
     const int at = (i / L) * S + (i % L);
-    double2 v = make_double2(0., 0.);
-    if (i < nx) v = spec[(size_t)blockIdx.z * g.css + (size_t)i * M1 + m0 + q];
-    sm[(2 * q) * sys_len + at] = v.x;
-    sm[(2 * q + 1) * sys_len + at] = v.y;
+    double2 xa = make_double2(0., 0.), xb = make_double2(0., 0.);
+    if (i < nx) {
+      const double2 zm = sp[(size_t)i * M1 + p];
+      const double2 zr = sp[(size_t)i * M1 + (p == 0 ? 0 : M - p)];
+      const double2 E = make_double2(zm.x + zr.x, zm.y - zr.y);
+      const double2 O = make_double2(zm.y + zr.y, zr.x - zm.x);  // -i (zm - conj zr)
+      xa = cadd(E, cmul(tw[p], O));
+      const double2 E2 = make_double2(zr.x + zm.x, zr.y - zm.y);
+      const double2 O2 = make_double2(zr.y + zm.y, zm.x - zr.x);
+      xb = cadd(E2, cmul(tw[M - p], O2));
+    }
+    sm[(4 * q) * sys_len + at] = xa.x;
+    sm[(4 * q + 1) * sys_len + at] = xa.y;
+    sm[(4 * q + 2) * sys_len + at] = xb.x;
+    sm[(4 * q + 3) * sys_len + at] = xb.y;
   }
   __syncthreads();
-  // warp -> system (2 per wavenumber: real, imaginary) and its part sub of G;
-  // chunk j of the system = this lane's L rows
+  // warp -> system (4 per pair) and its part sub of G; chunk j of the
+  // system = this lane's L rows
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sys = warp / G, sub = warp - sys * G, j = sub * 32 + lane;
-  const bool act = sys < 2 * nm;  // warp-uniform
-  const int m = m0 + (sys >> 1);
+  const bool act = sys < 4 * np;  // warp-uniform
+  const int pq = p0 + (sys >> 2);
+  const int m = (sys & 2) ? M - pq : pq;  // the wavenumber of this system
   double *x = sm + sys * sys_len + j * S;
   const double4_32a *f = fac + (size_t)m * L * lanes + j;
   double T = 0., B = 0.;
@@ -837,7 +843,8 @@ __global__ void __launch_bounds__(256)
       for (int q = G - 1; q > sub; --q) Din = fma(xch[sys][q][1], Din, xch[sys][q][0]);
     __syncthreads();
   }
-  const bool gauge = act && m == 0;  // the singular mode: zero mean over x (imaginary part is 0)
+  // the singular mode m = 0 (systems 0, 1 of pair 0): zero mean over x, imaginary part 0
+  const bool gauge = act && m == 0 && (sys & 2) == 0;
   double acc = 0.;
   if (act) {
     const double Sd = __shfl_down_sync(0xffffffffu, Sx, 1), Cd = __shfl_down_sync(0xffffffffu, Cc, 1);
@@ -863,10 +870,27 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < L; ++k) x[k] = (sys & 1) ? 0. : x[k] - mean;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nx * nm; t += blockDim.x) {
-    const int i = t / nm, q = t - i * nm;
+  // ---- complex-to-real split of the solved pair into the packed input of the
+  // inverse transform: z_m = E + i O, E = X_m + conj X_{M-m},
+  // O = (X_m - conj X_{M-m}) conj w^m, for m = p and m = M - p (< M)
+  for (int t = threadIdx.x; t < nx * np; t += blockDim.x) {
+    const int i = t / np, q = t - i * np;
+    const int p = p0 + q;
     const int at = (i / L) * S + (i % L);
-    spec[(size_t)blockIdx.z * g.css + (size_t)i * M1 + m0 + q] = make_double2(sm[(2 * q) * sys_len + at], sm[(2 * q + 1) * sys_len + at]);
+    const double2 Xa = make_double2(sm[(4 * q) * sys_len + at], sm[(4 * q + 1) * sys_len + at]);
+    const double2 Xb = make_double2(sm[(4 * q + 2) * sys_len + at], sm[(4 * q + 3) * sys_len + at]);
+    {
+      const double2 E = make_double2(Xa.x + Xb.x, Xa.y - Xb.y);
+      const double2 D = make_double2(Xa.x - Xb.x, Xa.y + Xb.y);
+      const double2 O = cmul(D, make_double2(tw[p].x, -tw[p].y));
+      sp[(size_t)i * M1 + p] = make_double2(E.x - O.y, E.y + O.x);
+    }
+    if (p != 0 && 2 * p != M) {
+      const double2 E = make_double2(Xb.x + Xa.x, Xb.y - Xa.y);
+      const double2 D = make_double2(Xb.x - Xa.x, Xb.y + Xa.y);
+      const double2 O = cmul(D, make_double2(tw[M - p].x, -tw[M - p].y));
+      sp[(size_t)i * M1 + (M - p)] = make_double2(E.x - O.y, E.y + O.x);
+    }
   }
 }
 
@@ -1280,11 +1304,12 @@ Tiles default_tiles() {
 int tdm_chunk(int nx, int G) { return (nx + 32 * G - 1) / (32 * G); }
 int tdm_stride(int nx, int G) { return tdm_chunk(nx, G) | 1; }
 int poisson_tdm_modes(int nx) {
-  const size_t per_mode = 2 * 32 * (size_t)tdm_stride(nx, 1) * sizeof(double);
+  const size_t per_mode = 4 * 32 * (size_t)tdm_stride(nx, 1) * sizeof(double);
   return per_mode * 4 <= 200 * 1024 ? 4 : (per_mode * 2 <= 200 * 1024 ? 2 : 1);
 }
+// mb: wavenumber pairs (p, M - p) per block, four systems each
 size_t poisson_tdm_smem(int nx, int mb, int G) {
-  return 2 * 32 * (size_t)G * tdm_stride(nx, G) * sizeof(double) * mb;
+  return 4 * 32 * (size_t)G * tdm_stride(nx, G) * sizeof(double) * mb;
 }
 size_t poisson_tdm_smem(int nx) { return poisson_tdm_smem(nx, poisson_tdm_modes(nx), 1); }
 int tdm_group_index(int G) { return G == 4 ? 2 : (G == 2 ? 1 : 0); }
@@ -1295,10 +1320,10 @@ int tdm_group_index(int G) { return G == 4 ? 2 : (G == 2 ? 1 : 0); }
 int tdm_modes_per_block(const Tiles &t, int nx) {
   const int G = t.tdm_g > 0 ? t.tdm_g : 1;
   const int mb = t.tdm_mb > 0 ? t.tdm_mb : poisson_tdm_modes(nx);
-  return mb * G > 4 ? 4 / G : mb;  // at most 256 threads a block
+  return mb * G > 4 ? 4 / G : mb;  // at most 512 threads a block
 }
 int tdm_warps_for(int nx, int ny, int nc) {
-  const long systems = 2L * (ny / 2 + 1) * nc;
+  const long systems = 4L * (ny / 4 + 1) * nc;
   int G = 1;
   while (G < 4 && systems * G < 2048 && tdm_chunk(nx, 2 * G) >= 2) G *= 2;
   return G;
@@ -1440,11 +1465,11 @@ void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const doub
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
   const int G = b.tiles.tdm_g > 0 ? b.tiles.tdm_g : 1;
-  const int mb = tdm_modes_per_block(b.tiles, g.nx);
-  const int M1 = g.ny / 2 + 1;
-  k_poisson_tdm<<<dim3((M1 + mb - 1) / mb, 1, g.nc), 64 * mb * G, poisson_tdm_smem(g.nx, mb, G), s>>>(
+  const int mb = tdm_modes_per_block(b.tiles, g.nx);  // wavenumber pairs per block
+  const int pairs = g.ny / 4 + 1;
+  k_poisson_tdm<<<dim3((pairs + mb - 1) / mb, 1, g.nc), 128 * mb * G, poisson_tdm_smem(g.nx, mb, G), s>>>(
       g, mb, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
-      reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]), b.spec);
+      reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]), b.twiddle, b.spec);
 }
 
 template <int W>
