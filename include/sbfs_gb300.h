@@ -18,7 +18,7 @@
  * it back on exit (see sbfs_set_sync_mode for the device-resident mode).
  *
  * Limits: NDIMS == 2; uniform x grid (as the reference requires,
- * src/domain.c:213-219); ny a power of two >= 8; 4 <= nx <= 8192.
+ * src/domain.c:213-219); ny a power of two, 8 <= ny <= 8192; 4 <= nx <= 8192.
  */
 #ifndef SBFS_GB300_H
 #define SBFS_GB300_H

@@ -202,7 +202,7 @@ int check_domain(const domain_t *d) {
   if (d->glsizes[0] != d->mysizes[0] || d->glsizes[1] != d->mysizes[1])
     return fail("domain is decomposed; this library runs the whole domain on one GPU");
   if (nx < 4 || nx > 8192) return fail("nx = %ld outside 4..8192", nx);
-  if (ny < 8 || (ny & (ny - 1)) != 0) return fail("ny = %ld must be a power of two >= 8", ny);
+  if (ny < 8 || ny > 8192 || (ny & (ny - 1)) != 0) return fail("ny = %ld must be a power of two in 8..8192", ny);
   // the reference accepts uniform x grids only (src/domain.c:78-98, 213-219)
   double lo = 1e300, hi = -1e300;
   for (long i = 0; i < nx; ++i) {
@@ -424,7 +424,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   g.cm = 0;
   g.phys = nullptr;
   Bufs &b = c->b;
-  b.tiles = default_tiles();
+  b.tiles = default_tiles(c->ny);
   b.tiles.tdm_g = tdm_warps_for(c->nx, c->ny, nc);
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
@@ -442,6 +442,9 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
     if (dalloc(*c, &tmp, 4 * (size_t)32 * G * tdm_chunk(c->nx, G) * M1)) return 1;
     b.tdm_fac[gi] = reinterpret_cast<double2 *>(tmp);
   }
+  b.tdm_stage = nullptr;
+  if (const size_t ns = tdm_stage_doubles(c->nx, c->ny, nc, b.tiles.tdm_g))
+    if (dalloc(*c, &b.tdm_stage, ns)) return 1;
   if (dalloc(*c, &tmp, 2 * (size_t)M1)) return 1;
   b.twiddle = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, ((size_t)c->nx + 8) * nc)) return 1;
@@ -709,9 +712,11 @@ int autotune(Ctx &c) {
   std::vector<std::pair<int, int>> tdms;  // (wavenumbers per block, warps per system)
   for (int w : {2, 4, 8})
     if (fft_w_fits(c.ny, w)) fws.push_back(w);
+  if (fws.empty()) fws.push_back(poisson_fft_cols(c.ny));
   const int G = c.b.tiles.tdm_g;  // fixed by the grid
   for (int mb : {1, 2, 4})
     if (G * mb <= 4 && poisson_tdm_smem(c.nx, mb, G) <= 200 * 1024) tdms.push_back({mb, G});
+  if (tdms.empty()) tdms.push_back({1, G});  // one pair per block (staged in global memory above ~6900 rows)
   const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT,
                                -1, -1, -1, TK_CORRECT, -1, -1};
   Tiles best = c.b.tiles;

@@ -728,18 +728,22 @@ __global__ void __launch_bounds__(256)
 // parallel per system.  fac[(m*L + k)*32 + l] = (w, v, P, Q) for row l*L+k.
 // The singular m = 0 mode (Neumann in x, constant null space) has its last
 // pivot pinned (w = v = 0) and is shifted to zero mean.
-// Shared memory: per system a planar array with an odd lane stride S.
+// Staging: per system a planar array with an odd lane stride S, in shared
+// memory; when four systems of nx rows exceed it (nx above about 6900), in
+// this block's slab of the global buffer stage (L2-resident, same arithmetic).
+template <bool kGlobalStage>
 __global__ void __launch_bounds__(512)
     k_poisson_tdm(Grid g, int PB, int G, int L, int S, const double4_32a *__restrict__ fac,
-                  const double2 *__restrict__ tw, double2 *__restrict__ spec) {
+                  const double2 *__restrict__ tw, double2 *__restrict__ spec, double *__restrict__ stage) {
   extern __shared__ double2 smem_d2[];
-  double *sm = reinterpret_cast<double *>(smem_d2);
   __shared__ double xch[16][4][2];  // per system of the block, per warp of the system: a chunk-map total
   const int nx = g.nx, M = g.ny / 2, M1 = M + 1;
   const int p0 = blockIdx.x * PB;
   const int np = min(PB, M / 2 + 1 - p0);  // pairs (p, M - p), p = 0 .. M/2
   const int lanes = 32 * G;                // chunks per system
   const int sys_len = lanes * S;
+  double *sm = kGlobalStage ? stage + ((size_t)blockIdx.z * gridDim.x + blockIdx.x) * 4 * PB * sys_len
+                            : reinterpret_cast<double *>(smem_d2);
   double2 *sp = spec + (size_t)blockIdx.z * g.css;
   // ---- load the packed transform of both wavenumbers of each pair, split
   // it (real-to-complex, times 2: X_m = (z_m + conj z_{M-m}) + w^m (-i)(z_m -
@@ -1227,6 +1231,8 @@ __global__ void k_nr_check(const double *__restrict__ x, double *__restrict__ rc
 }
 
 constexpr int kFftCols = 4;
+// dynamic shared memory of k_poisson_tdm<false> (its static xch lies beside)
+constexpr size_t kTdmSmemMax = 227 * 1024 - 4096;
 
 // FP64 fused multiply-add throughput: 8 independent chains per thread, every
 // thread writes only its own output element
@@ -1286,17 +1292,23 @@ cudaError_t nr_check(const double *x, double *rcp, double *rsq, int n) {
 // launch helpers
 // ===========================================================================
 
-int poisson_fft_cols(int) { return kFftCols; }
+// columns per block of the transforms: kFftCols, halved while a block's two
+// ny/2 complex rows per column exceed shared memory (ny = 8192 takes 1)
+int poisson_fft_cols(int ny) {
+  int w = kFftCols;
+  while (w > 1 && !fft_w_fits(ny, w)) w >>= 1;
+  return w;
+}
 size_t poisson_fft_smem(int ny, int w) { return sizeof(double2) * 2 * w * (size_t)(ny / 2); }
 bool fft_w_fits(int ny, int w) { return poisson_fft_smem(ny, w) <= 227 * 1024; }
 
-Tiles default_tiles() {
+Tiles default_tiles(int ny) {
   Tiles t{};
   for (int k = 0; k < TK_COUNT; ++k) {
     t.bx[k] = BX;
     t.by[k] = BY;
   }
-  t.fft_w = kFftCols;
+  t.fft_w = poisson_fft_cols(ny);
   t.tdm_mb = 0;
   t.tdm_g = 1;
   return t;
@@ -1312,6 +1324,10 @@ size_t poisson_tdm_smem(int nx, int mb, int G) {
   return 4 * 32 * (size_t)G * tdm_stride(nx, G) * sizeof(double) * mb;
 }
 size_t poisson_tdm_smem(int nx) { return poisson_tdm_smem(nx, poisson_tdm_modes(nx), 1); }
+bool tdm_global_stage(int nx, int G) { return poisson_tdm_smem(nx, 1, G) > kTdmSmemMax; }
+size_t tdm_stage_doubles(int nx, int ny, int nc, int G) {
+  return tdm_global_stage(nx, G) ? (size_t)(ny / 4 + 1) * nc * 4 * 32 * G * tdm_stride(nx, G) : 0;
+}
 int tdm_group_index(int G) { return G == 4 ? 2 : (G == 2 ? 1 : 0); }
 // warps per tridiagonal system for a grid of nc cases: the fewest (1, 2, 4)
 // that put about 2048 warps in flight (13 per SM), as long as every lane
@@ -1344,7 +1360,11 @@ cudaError_t configure_kernels() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_poisson_inv<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_poisson_tdm, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 4096);
+  e = cudaFuncSetAttribute(k_poisson_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_inv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_tdm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTdmSmemMax);
   return e;
 }
 
@@ -1455,7 +1475,9 @@ void poisson_fwd_w(cudaStream_t s, const Grid &g, const Bufs &b, const double *s
 
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                         const double *uy, const double *psi_old) {
-  if (b.tiles.fft_w == 2)
+  if (b.tiles.fft_w == 1)
+    poisson_fwd_w<1>(s, g, b, sc, k, ux, uy, psi_old);
+  else if (b.tiles.fft_w == 2)
     poisson_fwd_w<2>(s, g, b, sc, k, ux, uy, psi_old);
   else if (b.tiles.fft_w == 8)
     poisson_fwd_w<8>(s, g, b, sc, k, ux, uy, psi_old);
@@ -1465,11 +1487,16 @@ void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const doub
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
   const int G = b.tiles.tdm_g > 0 ? b.tiles.tdm_g : 1;
-  const int mb = tdm_modes_per_block(b.tiles, g.nx);  // wavenumber pairs per block
   const int pairs = g.ny / 4 + 1;
-  k_poisson_tdm<<<dim3((pairs + mb - 1) / mb, 1, g.nc), 128 * mb * G, poisson_tdm_smem(g.nx, mb, G), s>>>(
-      g, mb, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
-      reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]), b.twiddle, b.spec);
+  const double4_32a *fac = reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]);
+  if (tdm_global_stage(g.nx, G)) {  // one pair per block, staged in b.tdm_stage
+    k_poisson_tdm<true><<<dim3(pairs, 1, g.nc), 128 * G, 0, s>>>(g, 1, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
+                                                                 fac, b.twiddle, b.spec, b.tdm_stage);
+    return;
+  }
+  const int mb = tdm_modes_per_block(b.tiles, g.nx);  // wavenumber pairs per block
+  k_poisson_tdm<false><<<dim3((pairs + mb - 1) / mb, 1, g.nc), 128 * mb * G, poisson_tdm_smem(g.nx, mb, G), s>>>(
+      g, mb, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G), fac, b.twiddle, b.spec, nullptr);
 }
 
 template <int W>
@@ -1479,7 +1506,9 @@ void poisson_inv_w(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new
 }
 
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
-  if (b.tiles.fft_w == 2)
+  if (b.tiles.fft_w == 1)
+    poisson_inv_w<1>(s, g, b, psi_new);
+  else if (b.tiles.fft_w == 2)
     poisson_inv_w<2>(s, g, b, psi_new);
   else if (b.tiles.fft_w == 8)
     poisson_inv_w<8>(s, g, b, psi_new);

@@ -13,12 +13,12 @@ namespace sbfs {
 enum TileKernel { TK_PROPS, TK_CURV_LIST, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT, TK_CORRECT, TK_COUNT };
 struct Tiles {
   unsigned short bx[TK_COUNT], by[TK_COUNT];  // block shape (bx * by <= 256)
-  int fft_w;   // columns per block of the Poisson transforms: 2, 4 or 8
+  int fft_w;   // columns per block of the Poisson transforms: 1, 2, 4 or 8
   int tdm_mb;  // wavenumbers per block of the tridiagonal solves (0: by size)
   int tdm_g;   // warps per tridiagonal system: 1, 2 or 4 (tdm_g * tdm_mb <= 4), set by
                // tdm_warps_for from the grid (it changes the rounding, so it is not tuned)
 };
-Tiles default_tiles();
+Tiles default_tiles(int ny);
 
 struct Bufs {
   // state
@@ -37,6 +37,7 @@ struct Bufs {
   // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
   double2 *spec;
   double2 *tdm_fac[3];  // (w, v, P, Q) per row for 1, 2, 4 warps per system, see k_poisson_tdm
+  double *tdm_stage;    // systems of k_poisson_tdm when they exceed shared memory (else null)
   double2 *twiddle;  // exp(-2 pi i m / ny), m = 0..ny/2
   // decide_dt accumulators and per-step scalars
   unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
@@ -113,6 +114,8 @@ size_t poisson_tdm_smem(int nx, int mb, int G);
 size_t poisson_fft_smem(int ny, int w);
 bool fft_w_fits(int ny, int w);
 size_t poisson_tdm_smem(int nx);
+bool tdm_global_stage(int nx, int G);                   // k_poisson_tdm stages its systems in global memory
+size_t tdm_stage_doubles(int nx, int ny, int nc, int G);  // size of Bufs::tdm_stage (0 if not staged)
 cudaError_t configure_kernels();
 // Newton-Raphson reciprocal / inverse square root of n device inputs (tests)
 cudaError_t nr_check(const double *x, double *rcp, double *rsq, int n);
