@@ -6,6 +6,7 @@
 // per process and rebuilt when the grid changes; this replaces the
 // reference's function-static solver state (src/fluid/compute_potential.c:
 // 427-437, src/decide_dt.c:19-22).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -934,9 +935,13 @@ Batch *prepare_batch(int n, const domain_t *const *d, fluid_t *const *f, interfa
     nb->group_of.resize(n);
     nb->slot_of.resize(n);
     for (int i = 0; i < n; ++i) {
+      // cases per group: the face list holds 4 * cell + face of every case as
+      // an int, and the case is blockIdx.z; a full group starts another one
+      const long cells = (long)d[i]->mysizes[0] * (long)d[i]->mysizes[1];
+      const int cap = (int)std::min(65535L, (1L << 29) / cells);
       int gi = -1;
       for (size_t q = 0; q < first.size() && gi < 0; ++q)
-        if (same_domain_grid(d[first[q]], d[i])) gi = (int)q;
+        if (count[q] < cap && same_domain_grid(d[first[q]], d[i])) gi = (int)q;
       if (gi < 0) {
         gi = (int)first.size();
         first.push_back(i);
