@@ -96,6 +96,18 @@ int sbfs_invalidate_device(void);
 /* capture each time step into a CUDA graph (default 1) */
 int sbfs_set_use_graphs(int on);
 
+/* In SBFS_SYNC_STATE mode, let the step copy the state itself (default 1):
+ * when the GPU can address the caller's arrays (pageable host memory on a
+ * system with host page-table access, such as Grace-Blackwell, or arrays
+ * registered with cudaHostRegister), kernels inside the step read ux, uy, p,
+ * psi[0] and vof from them and write the results back, each field as early as
+ * the step allows, overlapped with the step's own kernels.  Otherwise the
+ * state moves by cudaMemcpy before and after the step.  Same results either
+ * way, bit for bit.  sbfs_host_link_used says whether the last integrate()
+ * was host-linked. */
+int sbfs_set_host_link(int on);
+int sbfs_host_link_used(void);
+
 /* safety factors of decide_dt, overriding the environment keys */
 int sbfs_set_dt_coefs(double adv, double dif, double itf);
 

@@ -37,6 +37,7 @@ class GpuLibrary(ReferenceAPI):
         lib.sbfs_last_error.restype = C.c_char_p
         lib.sbfs_set_sync_mode.argtypes = [C.c_int]
         lib.sbfs_set_use_graphs.argtypes = [C.c_int]
+        lib.sbfs_set_host_link.argtypes = [C.c_int]
         lib.sbfs_set_dt_coefs.argtypes = [C.c_double] * 3
         lib.sbfs_sync_to_host.argtypes = [C.c_void_p] * 3
         lib.sbfs_run_steps_timed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
@@ -74,6 +75,15 @@ class GpuLibrary(ReferenceAPI):
 
     def set_use_graphs(self, on: bool):
         self._ext("sbfs_set_use_graphs", 1 if on else 0)
+
+    def set_host_link(self, on: bool):
+        """strict-mode steps copy the state in and out themselves, overlapped
+        with their kernels, when the GPU can address the host arrays"""
+        self._ext("sbfs_set_host_link", 1 if on else 0)
+
+    def host_link_used(self) -> bool:
+        """whether the last integrate() was host-linked"""
+        return bool(self.lib.sbfs_host_link_used())
 
     def set_dt_coefs(self, adv, dif, itf):
         self._ext("sbfs_set_dt_coefs", adv, dif, itf)

@@ -50,6 +50,8 @@ double rk_g(int k) { return RK_A[k] + RK_B[k]; }
 
 int g_sync_mode = SBFS_SYNC_STATE;
 int g_use_graphs = 1;
+int g_host_link = 1;    // strict-mode steps copy the state themselves when they can
+bool g_link_used = false;  // the last integrate() did
 double g_coef[3] = {-1., -1., -1.};
 
 // extra cells of every field (reference include/array_macros/)
@@ -97,6 +99,18 @@ struct Ctx {
   cudaStream_t s2 = nullptr;
   cudaEvent_t evf = nullptr, evd = nullptr, evs = nullptr, evp = nullptr;
   bool props_ahead = false;  // the next substage's k_props is already on the side stream
+  // host-linked step (strict sync mode, host arrays the GPU can address): the
+  // step copies the state in and out itself, on the copy stream s3, each
+  // field as early as the step allows.  link_tab: page-locked table of the
+  // caller's arrays as the GPU addresses them (HL_* slots), read by the copy
+  // kernels; link_host: the same arrays' host addresses, for the copy-engine
+  // copies (baked into a captured graph: graph_hosts keeps them per graph)
+  bool link = false;
+  cudaStream_t s3 = nullptr;
+  cudaEvent_t evh[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // vof, velocity, p, psi in; fork
+  double **link_tab = nullptr, **link_tab_dev = nullptr;
+  std::vector<const void *> link_host;
+  std::map<int, std::vector<const void *>> graph_hosts;
   // diagnostics partials / result and statistics sums (allocated on first use)
   double *diag_part = nullptr, *diag_out = nullptr;
   double *st_ux1 = nullptr, *st_uy1 = nullptr, *st_vof1 = nullptr;
@@ -112,6 +126,10 @@ struct Ctx {
     if (evd) cudaEventDestroy(evd);
     if (evs) cudaEventDestroy(evs);
     if (evp) cudaEventDestroy(evp);
+    for (cudaEvent_t e : evh)
+      if (e) cudaEventDestroy(e);
+    if (link_tab) cudaFreeHost(link_tab);
+    if (s3) cudaStreamDestroy(s3);
     if (s2) cudaStreamDestroy(s2);
     if (s) cudaStreamDestroy(s);
   }
@@ -399,6 +417,10 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evs, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
+  for (cudaEvent_t &e : c->evh) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  CK(cudaHostAlloc(reinterpret_cast<void **>(&c->link_tab), sizeof(double *) * 16, cudaHostAllocMapped));
+  CK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->link_tab_dev), c->link_tab, 0));
   CK(cudaEventCreate(&c->e1));
   cudaError_t e = configure_kernels();
   if (e != cudaSuccess) return fail("configure_kernels: %s", cudaGetErrorString(e));
@@ -600,6 +622,69 @@ void timed(Ctx &c, int cls, F &&launch) {
   g_prof.marks.push_back({cls, {a, b}});
 }
 
+// ---- host-linked step: slots of Ctx::link_tab, the arrays read at the start
+// of the step and those written at its end (the psi pointers as the reference
+// leaves them, swapped)
+enum { HL_UX_IN, HL_UY_IN, HL_P_IN, HL_PSI_IN, HL_VOF_IN, HL_UX_OUT, HL_UY_OUT, HL_P_OUT, HL_PSI0_OUT, HL_PSI1_OUT,
+       HL_VOF_OUT, HL_COUNT };
+
+HostRows host_rows(const Ctx &c, int slot, const Layout &l, double *dev) {
+  return HostRows{slot, c.nx + l.ax0 + l.ax1, l.ay0, l.ay1, dev};
+}
+
+// Copies that run beside the step's kernels go through the copy engines: a
+// kernel copying over the CPU-GPU link slows the kernels sharing its SMs by
+// about its own duration (measured on the bubble swarm).  Copies with nothing
+// beside them are kernels: they reach the link's full read rate.
+
+// copy-engine copy of a scalar field between a host array (slot) and its
+// device rows; out also fills the host's y ghost rows from their periodic
+// images
+void link_dma(Ctx &c, bool in, int slot, const Layout &l, double *dev) {
+  const size_t row = (size_t)c.nx + l.ax0 + l.ax1, pitch = sizeof(double) * c.g.p1;
+  double *h = const_cast<double *>(static_cast<const double *>(c.link_host[slot]));
+  if (in) {
+    cudaMemcpy2DAsync(dev, pitch, h + (size_t)l.ay0 * row, sizeof(double) * row, sizeof(double) * row, c.ny,
+                      cudaMemcpyHostToDevice, c.s3);
+    return;
+  }
+  cudaMemcpy2DAsync(h + (size_t)l.ay0 * row, sizeof(double) * row, dev, pitch, sizeof(double) * row, c.ny,
+                    cudaMemcpyDeviceToHost, c.s3);
+  for (int J = 1 - l.ay0; J <= c.ny + l.ay1; ++J) {
+    if (J >= 1 && J <= c.ny) continue;
+    const int r = J < 1 ? J - 1 + c.ny : J - 1 - c.ny;
+    cudaMemcpyAsync(h + (size_t)(J - 1 + l.ay0) * row, dev + (size_t)r * c.g.p1, sizeof(double) * row,
+                    cudaMemcpyDeviceToHost, c.s3);
+  }
+}
+
+// the copies in, on the copy stream in the order the step first needs them:
+// vof (densities, viscosities, corner normals), the velocity (everything
+// else of the interface chain), p (first predictor), psi (first Poisson
+// right-hand side); rho^k as soon as vof is in
+void link_in(Ctx &c) {
+  cudaEventRecord(c.evh[4], c.s);
+  cudaStreamWaitEvent(c.s3, c.evh[4], 0);
+  launch_host_rows(c.s3, c.g, c.link_tab_dev, true, host_rows(c, HL_VOF_IN, L_VOF, c.b.vof), HostRows{}, 1);
+  cudaEventRecord(c.evh[0], c.s3);
+  launch_host_rows(c.s3, c.g, c.link_tab_dev, true, host_rows(c, HL_UX_IN, L_UX, c.U[c.iu]),
+                   host_rows(c, HL_UY_IN, L_UY, c.V[c.iu]), 2);
+  cudaEventRecord(c.evh[1], c.s3);
+  link_dma(c, true, HL_P_IN, L_P, c.b.p);
+  cudaEventRecord(c.evh[2], c.s3);
+  link_dma(c, true, HL_PSI_IN, L_P, c.PSI[c.ipsi]);
+  cudaEventRecord(c.evh[3], c.s3);
+  cudaStreamWaitEvent(c.s, c.evh[0], 0);
+  launch_props(c.s, c.g, c.m, c.ph, c.b, true, false, false, c.DEN[c.iden]);
+}
+
+// a copy out on the copy stream, of a field the main stream has finished
+void link_out(Ctx &c, int slot, const Layout &l, double *dev) {
+  cudaEventRecord(c.evh[4], c.s);
+  cudaStreamWaitEvent(c.s3, c.evh[4], 0);
+  link_dma(c, false, slot, l, dev);
+}
+
 // par: run decide_dt (already on the side stream, joined before the first
 // use of its scalars, when wait_dt) and k_stress on the side stream.  Both
 // only read what the main stream has finished when they are forked, and the
@@ -627,6 +712,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     launch_stress(c.s2, c.g, c.m, b, ux, uy);
     cudaEventRecord(c.evs, c.s2);
   }
+  if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
   const bool learned = g_curv_model != 0;
   if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
@@ -635,6 +721,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
         [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
   if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
+  if (c.link && k == 2) link_out(c, HL_VOF_OUT, L_VOF, b.vof);  // vof is final
   if (par && k < 2) {
     // the next substage's viscosities and corner normals need only the new
     // vof: they run beside this substage's predictor, Poisson solve and
@@ -649,13 +736,17 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     cudaStreamWaitEvent(c.s, c.evs, 0);
   else
     timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
+  if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[2], 0);  // p is in
   timed(c, KC_PREDICT, [&] {
     launch_predict(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, b.mfluxx, b.mfluxy, den0, den1, sxa, sxb,
                    nullptr, sya, syb, nullptr);
   });
+  if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[3], 0);  // psi is in
   timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, b, sc, k, uxs, uys, psio); });
   timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
   timed(c, KC_POISSON_INV, [&] { launch_poisson_inv(c.s, c.g, b, psin); });
+  // psi of substages 2 and 3 are final: the caller's psi[1] and psi[0] after the step
+  if (c.link && k >= 1) link_out(c, k == 1 ? HL_PSI1_OUT : HL_PSI0_OUT, L_P, psin);
   timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, b, sc, k, uxs, uys, psin, psio, true); });
   c.iu ^= 1;
   c.ipsi ^= 1;
@@ -668,16 +759,27 @@ void enqueue_step(Ctx &c) {
   // profiled steps keep every launch on the main stream (events per launch)
   const bool par = !g_prof.on;
   c.props_ahead = false;
+  if (c.link) link_in(c);
   if (par) {
     cudaEventRecord(c.evf, c.s);
     cudaStreamWaitEvent(c.s2, c.evf, 0);
+    if (c.link) cudaStreamWaitEvent(c.s2, c.evh[1], 0);
     launch_decide_dt(c.s2, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]);
     cudaEventRecord(c.evd, c.s2);
   } else {
+    if (c.link) cudaStreamWaitEvent(c.s, c.evh[1], 0);
     timed(c, KC_DECIDE_DT,
           [&] { launch_decide_dt(c.s, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]); });
   }
   for (int k = 0; k < 3; ++k) enqueue_substage(c, k, par, par && k == 0);
+  if (c.link) {
+    // the velocity and p of the last correction, then the copy stream joins
+    launch_host_rows(c.s, c.g, c.link_tab_dev, false, host_rows(c, HL_UX_OUT, L_UX, c.U[c.iu]),
+                     host_rows(c, HL_UY_OUT, L_UY, c.V[c.iu]), 2);
+    launch_host_rows(c.s, c.g, c.link_tab_dev, false, host_rows(c, HL_P_OUT, L_P, c.b.p), HostRows{}, 1);
+    cudaEventRecord(c.evh[4], c.s3);
+    cudaStreamWaitEvent(c.s, c.evh[4], 0);
+  }
 }
 
 // ---- autotuner of the launch shapes (block shape of each stencil kernel,
@@ -786,10 +888,18 @@ int autotune(Ctx &c) {
   return 0;
 }
 
-int role_key(const Ctx &c) { return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4); }
+int role_key(const Ctx &c) {
+  return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5);
+}
 
 int launch_step(Ctx &c) {
-  if (g_autotune && !c.tuned && c.resident && !g_prof.on && autotune(c)) return 1;
+  if (g_autotune && !c.tuned && c.resident && !g_prof.on) {
+    const bool link = c.link;  // the trials step the device state only
+    c.link = false;
+    const int rc = autotune(c);
+    c.link = link;
+    if (rc) return 1;
+  }
   if (!g_use_graphs || g_prof.on) {
     enqueue_step(c);
     CK(cudaGetLastError());
@@ -814,6 +924,14 @@ int launch_step(Ctx &c) {
   }
   const int key = role_key(c);
   auto it = c.graphs.find(key);
+  // a host-linked graph holds copy-engine copies of the caller's arrays: it
+  // is captured again when the arrays are others
+  const std::vector<const void *> hosts = c.link ? c.link_host : std::vector<const void *>();
+  if (it != c.graphs.end() && c.graph_hosts[key] != hosts) {
+    cudaGraphExecDestroy(it->second);
+    c.graphs.erase(it);
+    it = c.graphs.end();
+  }
   if (it == c.graphs.end()) {
     const int iu = c.iu, ipsi = c.ipsi, iden = c.iden, isrc = c.isrc;
     cudaGraph_t graph;
@@ -826,6 +944,7 @@ int launch_step(Ctx &c) {
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail("graph instantiate: %s", cudaGetErrorString(e));
     it = c.graphs.emplace(key, exec).first;
+    c.graph_hosts[key] = hosts;
     // capturing advanced the roles; restore, the launch below advances them
     c.iu = iu;
     c.ipsi = ipsi;
@@ -1065,6 +1184,13 @@ Ctx *prepare_step(const domain_t *d, fluid_t *f, interface_t *itf) {
 extern "C" {
 
 const char *sbfs_last_error(void) { return g_err.c_str(); }
+
+int sbfs_set_host_link(int on) {
+  g_host_link = on ? 1 : 0;
+  return 0;
+}
+
+int sbfs_host_link_used(void) { return g_link_used ? 1 : 0; }
 
 int sbfs_set_sync_mode(int mode) {
   if (mode < SBFS_SYNC_STATE || mode > SBFS_SYNC_NONE) return fail("bad sync mode %d", mode);
@@ -1321,10 +1447,63 @@ int sbfs_sync_to_host(const domain_t *d, fluid_t *f, interface_t *itf) {
   return sync(*c);
 }
 
+// host memory the GPU can address: any on a system whose GPU reads pageable
+// memory through the host page tables, else memory registered with CUDA
+int g_pageable = -1;
+bool host_addressable(void *p, double **dev) {
+  if (g_pageable < 0) {
+    int d = 0, v = 0;
+    g_pageable = cudaGetDevice(&d) == cudaSuccess &&
+                 cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, d) == cudaSuccess && v == 1;
+    cudaGetLastError();
+  }
+  if (g_pageable) {
+    *dev = static_cast<double *>(p);
+    return true;
+  }
+  void *q = nullptr;
+  if (cudaHostGetDevicePointer(&q, p, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  *dev = static_cast<double *>(q);
+  return true;
+}
+
+// fills the link table for a strict-mode step, or says the step cannot be
+// host-linked (then the state goes through cudaMemcpy as before)
+bool link_tab_fill(Ctx &c, fluid_t *f, interface_t *itf) {
+  if (!g_host_link || g_prof.on || g_sync_mode != SBFS_SYNC_STATE) return false;
+  const array_t *arr[HL_COUNT] = {&f->ux, &f->uy, &f->p, &f->psi[0], &itf->vof, &f->ux, &f->uy, &f->p,
+                                  &f->psi[1], &f->psi[0], &itf->vof};
+  const Layout *lay[HL_COUNT] = {&L_UX, &L_UY, &L_P, &L_P, &L_VOF, &L_UX, &L_UY, &L_P, &L_P, &L_P, &L_VOF};
+  c.link_host.assign(HL_COUNT, nullptr);
+  for (int q = 0; q < HL_COUNT; ++q) {
+    if (!layout_ok(*arr[q], *lay[q]) || !host_addressable(arr[q]->data, &c.link_tab[q])) return false;
+    c.link_host[q] = arr[q]->data;
+  }
+  return true;
+}
+
 // reference src/integrate.c:11-70
 int integrate(const domain_t *d, fluid_t *f, interface_t *itf, double *dt) {
   Ctx *c = prepare_step(d, f, itf);
   if (!c) return 1;
+  g_link_used = link_tab_fill(*c, f, itf);
+  if (g_link_used) {
+    // the step reads the caller's arrays and writes them back itself; the
+    // reference's psi pointers end a step swapped (three swaps)
+    c->link = true;
+    const int rc = launch_step(*c);
+    c->link = false;
+    if (rc) return 1;
+    c->resident = true;
+    swap_data(f->psi[0], f->psi[1]);
+    int status = 0;
+    if (read_dt_status(*c, dt, &status)) return 1;
+    if (status & 1) return fail("non-finite velocity detected by decide_dt");
+    return 0;
+  }
   if (g_sync_mode != SBFS_SYNC_NONE || !c->resident) {
     if (upload_state(*c, f, itf)) return 1;
   }

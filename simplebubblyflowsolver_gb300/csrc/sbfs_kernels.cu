@@ -1576,4 +1576,53 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof) {
   k_bc_vof<<<(g.ny + 127) / 128, 128, 0, s>>>(g, vof);
 }
 
+// ---------------------------------------------------------------------------
+// the caller's host arrays <-> device fields, copied by the GPU itself over
+// the CPU-GPU link (host memory the device can address: pageable memory on a
+// system with host page-table access, or registered memory).  In: host rows
+// J = 1..ny (x ghosts included) into the pitched device rows.  Out: every host
+// row J = 1 - ay0 .. ny + ay1, the y ghost rows from their periodic images
+// (what the reference's halo exchange leaves there, src/halo.c:18-76).  Each
+// thread keeps four loads in flight: the link's latency is microseconds.
+template <bool kIn>
+__global__ void __launch_bounds__(256) k_host_rows(Grid g, double *const *tab, HostRows a, HostRows b, int nf) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (int q = 0; q < nf; ++q) {
+    const HostRows f = q == 0 ? a : b;
+    double *h = tab[f.slot];
+    const long n = (long)(kIn ? g.ny : g.ny + f.ay0 + f.ay1) * f.row;
+    for (long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x; t0 < n; t0 += 4 * stride) {
+      double v[4];
+      long src[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const long t = t0 + u * stride;
+        const int r = (int)(t / f.row), i = (int)(t - (long)r * f.row);
+        // in: host element t of rows J >= 1 -> device row r; out: host element t <- device row of J
+        src[u] = kIn ? (long)(r + f.ay0) * f.row + i : (long)wrap(r - f.ay0 + 1, g.ny) * g.p1 + i;
+        if (t < n) v[u] = kIn ? h[src[u]] : f.dev[src[u]];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const long t = t0 + u * stride;
+        if (t >= n) break;
+        if (kIn) {
+          const int r = (int)(t / f.row), i = (int)(t - (long)r * f.row);
+          f.dev[(size_t)r * g.p1 + i] = v[u];
+        } else {
+          h[t] = v[u];
+        }
+      }
+    }
+  }
+}
+
+void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in, HostRows a, HostRows b, int nf) {
+  const int blocks = 2 * 152;
+  if (in)
+    k_host_rows<true><<<blocks, 256, 0, s>>>(g, tab, a, b, nf);
+  else
+    k_host_rows<false><<<blocks, 256, 0, s>>>(g, tab, a, b, nf);
+}
+
 }  // namespace sbfs

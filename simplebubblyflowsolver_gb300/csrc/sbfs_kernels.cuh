@@ -126,4 +126,13 @@ cudaError_t measure_fp64_peak(double *gflops);
 bool mlp_ready();
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b);
 
+// one scalar field between a host array of the reference's layout (tab[slot],
+// rows of `row` doubles, ay0 / ay1 ghost rows) and its device field (pitch p1)
+struct HostRows {
+  int slot, row, ay0, ay1;
+  double *dev;
+};
+// nf (1 or 2) fields, host -> device when in, else device -> host
+void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in, HostRows a, HostRows b, int nf);
+
 }  // namespace sbfs

@@ -1,0 +1,85 @@
+"""Host-linked steps (strict sync mode): the step's own kernels read the
+caller's host arrays and write the results back, overlapped with the step.
+Every host array must end exactly as after the cudaMemcpy path, ghost rows
+included."""
+import numpy as np
+import pytest
+
+from simplebubblyflowsolver_gb300 import SYNC_STATE, ic
+
+from ._helpers import clone, new_state, set_env
+
+pytestmark = pytest.mark.gpu
+
+HOST_SLOTS = ("ux", "uy", "p", "psi0", "psi1", "vof")
+
+
+@pytest.fixture(scope="module")
+def libs():
+    import oracle
+    from simplebubblyflowsolver_gb300 import load_library
+    return load_library(), oracle.Oracle()
+
+
+def run(gpu, st, steps, link, graphs):
+    gpu.set_host_link(link)
+    gpu.set_use_graphs(graphs)
+    dts, used = [], []
+    try:
+        for _ in range(steps):
+            dts.append(gpu.integrate(st))
+            used.append(gpu.host_link_used())
+    finally:
+        gpu.set_host_link(True)
+        gpu.set_use_graphs(True)
+    return dts, used
+
+
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph", "eager"])
+@pytest.mark.parametrize("grid", [(256, 128), (130, 64)], ids=["256x128", "130x64"])
+def test_host_linked_equals_memcpy(libs, grid, graphs):
+    gpu, orc = libs
+    nx, ny = grid
+    wl = ic.bubble_swarm(nx, ny, nbubbles=6, seed=3)
+    set_env(wl)
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    st0 = new_state(wl, orc)
+    a, b = clone(st0), clone(st0)
+    # poison the ghost rows of the outputs: the step must write them
+    for st in (a, b):
+        for s in HOST_SLOTS:
+            st.field(s)[0] = np.nan
+            st.field(s)[-1] = np.nan
+    dta, used_a = run(gpu, a, 4, True, graphs)
+    dtb, used_b = run(gpu, b, 4, False, graphs)
+    assert all(used_a), "the GPU could not address the host arrays"
+    assert not any(used_b)
+    assert dta == dtb
+    for s in HOST_SLOTS:
+        fa, fb = a.field(s), b.field(s)
+        assert np.array_equal(fa, fb), s
+        assert np.isfinite(fa).all(), s
+
+
+def test_host_linked_follows_host_changes(libs):
+    """a strict-mode step starts from what the host arrays hold at the call"""
+    gpu, orc = libs
+    wl = ic.single_bubble(128, 64)
+    set_env(wl)
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    st0 = new_state(wl, orc)
+    a, b = clone(st0), clone(st0)
+    run(gpu, a, 1, True, True)
+    run(gpu, b, 1, False, True)
+    # the caller edits its arrays between steps: both paths must see the edit
+    for st in (a, b):
+        st.field("ux")[...] *= 0.5
+        st.field("vof")[...] = np.clip(st.field("vof") * 1.01, 0.0, 1.0)
+    run(gpu, a, 2, True, True)
+    run(gpu, b, 2, False, True)
+    for s in HOST_SLOTS:
+        assert np.array_equal(a.field(s), b.field(s)), s
