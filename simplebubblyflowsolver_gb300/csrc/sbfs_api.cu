@@ -419,7 +419,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
   CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
   for (cudaEvent_t &e : c->evh) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  CK(cudaHostAlloc(reinterpret_cast<void **>(&c->link_tab), sizeof(double *) * 16, cudaHostAllocMapped));
+  CK(cudaHostAlloc(reinterpret_cast<void **>(&c->link_tab), sizeof(double *) * kLinkSlots * nc, cudaHostAllocMapped));
   CK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->link_tab_dev), c->link_tab, 0));
   CK(cudaEventCreate(&c->e1));
   cudaError_t e = configure_kernels();
@@ -635,7 +635,10 @@ HostRows host_rows(const Ctx &c, int slot, const Layout &l, double *dev) {
 // Copies that run beside the step's kernels go through the copy engines: a
 // kernel copying over the CPU-GPU link slows the kernels sharing its SMs by
 // about its own duration (measured on the bubble swarm).  Copies with nothing
-// beside them are kernels: they reach the link's full read rate.
+// beside them are kernels on the whole GPU: they reach the link's full read
+// rate.  A batch of many cases copies by kernels only (one launch for all its
+// cases instead of a copy-engine call per case), beside the step on few blocks.
+constexpr int kLinkWide = 2 * 152, kLinkNarrow = 64;
 
 // copy-engine copy of a scalar field between a host array (slot) and its
 // device rows; out also fills the host's y ghost rows from their periodic
@@ -658,6 +661,14 @@ void link_dma(Ctx &c, bool in, int slot, const Layout &l, double *dev) {
   }
 }
 
+// a copy beside the step's kernels, on the copy stream
+void link_side(Ctx &c, bool in, int slot, const Layout &l, double *dev) {
+  if (c.nc == 1)
+    link_dma(c, in, slot, l, dev);
+  else
+    launch_host_rows(c.s3, c.g, c.link_tab_dev, in, host_rows(c, slot, l, dev), HostRows{}, 1, kLinkNarrow);
+}
+
 // the copies in, on the copy stream in the order the step first needs them:
 // vof (densities, viscosities, corner normals), the velocity (everything
 // else of the interface chain), p (first predictor), psi (first Poisson
@@ -665,14 +676,15 @@ void link_dma(Ctx &c, bool in, int slot, const Layout &l, double *dev) {
 void link_in(Ctx &c) {
   cudaEventRecord(c.evh[4], c.s);
   cudaStreamWaitEvent(c.s3, c.evh[4], 0);
-  launch_host_rows(c.s3, c.g, c.link_tab_dev, true, host_rows(c, HL_VOF_IN, L_VOF, c.b.vof), HostRows{}, 1);
+  launch_host_rows(c.s3, c.g, c.link_tab_dev, true, host_rows(c, HL_VOF_IN, L_VOF, c.b.vof), HostRows{}, 1,
+                   kLinkWide);
   cudaEventRecord(c.evh[0], c.s3);
   launch_host_rows(c.s3, c.g, c.link_tab_dev, true, host_rows(c, HL_UX_IN, L_UX, c.U[c.iu]),
-                   host_rows(c, HL_UY_IN, L_UY, c.V[c.iu]), 2);
+                   host_rows(c, HL_UY_IN, L_UY, c.V[c.iu]), 2, kLinkWide);
   cudaEventRecord(c.evh[1], c.s3);
-  link_dma(c, true, HL_P_IN, L_P, c.b.p);
+  link_side(c, true, HL_P_IN, L_P, c.b.p);
   cudaEventRecord(c.evh[2], c.s3);
-  link_dma(c, true, HL_PSI_IN, L_P, c.PSI[c.ipsi]);
+  link_side(c, true, HL_PSI_IN, L_P, c.PSI[c.ipsi]);
   cudaEventRecord(c.evh[3], c.s3);
   cudaStreamWaitEvent(c.s, c.evh[0], 0);
   launch_props(c.s, c.g, c.m, c.ph, c.b, true, false, false, c.DEN[c.iden]);
@@ -682,7 +694,7 @@ void link_in(Ctx &c) {
 void link_out(Ctx &c, int slot, const Layout &l, double *dev) {
   cudaEventRecord(c.evh[4], c.s);
   cudaStreamWaitEvent(c.s3, c.evh[4], 0);
-  link_dma(c, false, slot, l, dev);
+  link_side(c, false, slot, l, dev);
 }
 
 // par: run decide_dt (already on the side stream, joined before the first
@@ -775,8 +787,9 @@ void enqueue_step(Ctx &c) {
   if (c.link) {
     // the velocity and p of the last correction, then the copy stream joins
     launch_host_rows(c.s, c.g, c.link_tab_dev, false, host_rows(c, HL_UX_OUT, L_UX, c.U[c.iu]),
-                     host_rows(c, HL_UY_OUT, L_UY, c.V[c.iu]), 2);
-    launch_host_rows(c.s, c.g, c.link_tab_dev, false, host_rows(c, HL_P_OUT, L_P, c.b.p), HostRows{}, 1);
+                     host_rows(c, HL_UY_OUT, L_UY, c.V[c.iu]), 2, kLinkWide);
+    launch_host_rows(c.s, c.g, c.link_tab_dev, false, host_rows(c, HL_P_OUT, L_P, c.b.p), HostRows{}, 1,
+                     kLinkWide);
     cudaEventRecord(c.evh[4], c.s3);
     cudaStreamWaitEvent(c.s, c.evh[4], 0);
   }
@@ -926,7 +939,7 @@ int launch_step(Ctx &c) {
   auto it = c.graphs.find(key);
   // a host-linked graph holds copy-engine copies of the caller's arrays: it
   // is captured again when the arrays are others
-  const std::vector<const void *> hosts = c.link ? c.link_host : std::vector<const void *>();
+  const std::vector<const void *> hosts = c.link && c.nc == 1 ? c.link_host : std::vector<const void *>();
   if (it != c.graphs.end() && c.graph_hosts[key] != hosts) {
     cudaGraphExecDestroy(it->second);
     c.graphs.erase(it);
@@ -1470,17 +1483,18 @@ bool host_addressable(void *p, double **dev) {
   return true;
 }
 
-// fills the link table for a strict-mode step, or says the step cannot be
-// host-linked (then the state goes through cudaMemcpy as before)
-bool link_tab_fill(Ctx &c, fluid_t *f, interface_t *itf) {
+// fills the link table of case k for a strict-mode step, or says the step
+// cannot be host-linked (then the state goes through cudaMemcpy as before)
+bool link_tab_fill(Ctx &c, int k, fluid_t *f, interface_t *itf) {
   if (!g_host_link || g_prof.on || g_sync_mode != SBFS_SYNC_STATE) return false;
   const array_t *arr[HL_COUNT] = {&f->ux, &f->uy, &f->p, &f->psi[0], &itf->vof, &f->ux, &f->uy, &f->p,
                                   &f->psi[1], &f->psi[0], &itf->vof};
   const Layout *lay[HL_COUNT] = {&L_UX, &L_UY, &L_P, &L_P, &L_VOF, &L_UX, &L_UY, &L_P, &L_P, &L_P, &L_VOF};
-  c.link_host.assign(HL_COUNT, nullptr);
+  if (c.nc == 1) c.link_host.assign(HL_COUNT, nullptr);
   for (int q = 0; q < HL_COUNT; ++q) {
-    if (!layout_ok(*arr[q], *lay[q]) || !host_addressable(arr[q]->data, &c.link_tab[q])) return false;
-    c.link_host[q] = arr[q]->data;
+    if (!layout_ok(*arr[q], *lay[q]) || !host_addressable(arr[q]->data, &c.link_tab[(size_t)k * kLinkSlots + q]))
+      return false;
+    if (c.nc == 1) c.link_host[q] = arr[q]->data;
   }
   return true;
 }
@@ -1489,7 +1503,7 @@ bool link_tab_fill(Ctx &c, fluid_t *f, interface_t *itf) {
 int integrate(const domain_t *d, fluid_t *f, interface_t *itf, double *dt) {
   Ctx *c = prepare_step(d, f, itf);
   if (!c) return 1;
-  g_link_used = link_tab_fill(*c, f, itf);
+  g_link_used = link_tab_fill(*c, 0, f, itf);
   if (g_link_used) {
     // the step reads the caller's arrays and writes them back itself; the
     // reference's psi pointers end a step swapped (three swaps)
@@ -1522,6 +1536,22 @@ int sbfs_integrate_batch(int n, const domain_t *const *domains, fluid_t *const *
                          interface_t *const *interfaces, double *dts) {
   Batch *b = prepare_batch(n, domains, fluids, interfaces);
   if (!b) return 1;
+  bool link = true;
+  for (int i = 0; i < n && link; ++i)
+    link = link_tab_fill(*b->groups[b->group_of[i]], b->slot_of[i], fluids[i], interfaces[i]);
+  g_link_used = link;
+  if (link) {
+    // every group's step copies its cases in and out itself (see integrate)
+    for (auto &c : b->groups) {
+      c->link = true;
+      const int rc = launch_step(*c);
+      c->link = false;
+      if (rc) return 1;
+      c->resident = true;
+    }
+    for (int i = 0; i < n; ++i) swap_data(fluids[i]->psi[0], fluids[i]->psi[1]);
+    return batch_read_dt(*b, n, dts);
+  }
   bool upload = g_sync_mode != SBFS_SYNC_NONE;
   for (auto &c : b->groups) upload = upload || !c->resident;
   if (upload && batch_upload(*b, n, fluids, interfaces)) return 1;

@@ -20,6 +20,7 @@
 //     pattern of the double; cells whose stencil inputs are bitwise equal
 //     (single-phase bulk) take the exact short cut.
 // The reference file:line each kernel follows is cited at the kernel.
+#include <algorithm>
 #include <cfloat>
 
 #include "sbfs_kernels.cuh"
@@ -1582,33 +1583,36 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof) {
 // system with host page-table access, or registered memory).  In: host rows
 // J = 1..ny (x ghosts included) into the pitched device rows.  Out: every host
 // row J = 1 - ay0 .. ny + ay1, the y ghost rows from their periodic images
-// (what the reference's halo exchange leaves there, src/halo.c:18-76).  Each
-// thread keeps four loads in flight: the link's latency is microseconds.
+// (what the reference's halo exchange leaves there, src/halo.c:18-76).  Case
+// z of a batch is blockIdx.y: its arrays are tab[z * kLinkSlots + slot], its
+// device rows start at dev + z * cs1.  Each thread keeps four loads in flight:
+// the link's latency is microseconds.
 template <bool kIn>
 __global__ void __launch_bounds__(256) k_host_rows(Grid g, double *const *tab, HostRows a, HostRows b, int nf) {
-  const long stride = (long)gridDim.x * blockDim.x;
+  const int z = blockIdx.y;
+  const int stride = gridDim.x * blockDim.x;
   for (int q = 0; q < nf; ++q) {
     const HostRows f = q == 0 ? a : b;
-    double *h = tab[f.slot];
-    const long n = (long)(kIn ? g.ny : g.ny + f.ay0 + f.ay1) * f.row;
-    for (long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x; t0 < n; t0 += 4 * stride) {
+    double *h = tab[(size_t)z * kLinkSlots + f.slot];
+    double *dev = f.dev + (size_t)z * g.cs1;
+    const int n = (kIn ? g.ny : g.ny + f.ay0 + f.ay1) * f.row;
+    for (int t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < n; t0 += 4 * stride) {
       double v[4];
-      long src[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const long t = t0 + u * stride;
-        const int r = (int)(t / f.row), i = (int)(t - (long)r * f.row);
-        // in: host element t of rows J >= 1 -> device row r; out: host element t <- device row of J
-        src[u] = kIn ? (long)(r + f.ay0) * f.row + i : (long)wrap(r - f.ay0 + 1, g.ny) * g.p1 + i;
-        if (t < n) v[u] = kIn ? h[src[u]] : f.dev[src[u]];
+        const int t = t0 + u * stride;
+        if (t >= n) break;
+        const int r = t / f.row, i = t - r * f.row;
+        // in: host row J = r + 1 (index r + ay0); out: host row index r holds J = r + 1 - ay0
+        v[u] = kIn ? h[(size_t)(r + f.ay0) * f.row + i] : dev[(size_t)wrap(r - f.ay0 + 1, g.ny) * g.p1 + i];
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const long t = t0 + u * stride;
+        const int t = t0 + u * stride;
         if (t >= n) break;
         if (kIn) {
-          const int r = (int)(t / f.row), i = (int)(t - (long)r * f.row);
-          f.dev[(size_t)r * g.p1 + i] = v[u];
+          const int r = t / f.row, i = t - r * f.row;
+          dev[(size_t)r * g.p1 + i] = v[u];
         } else {
           h[t] = v[u];
         }
@@ -1617,12 +1621,13 @@ __global__ void __launch_bounds__(256) k_host_rows(Grid g, double *const *tab, H
   }
 }
 
-void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in, HostRows a, HostRows b, int nf) {
-  const int blocks = 2 * 152;
+void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in, HostRows a, HostRows b, int nf,
+                      int width) {
+  const dim3 grid(std::max(1, width / g.nc), g.nc);
   if (in)
-    k_host_rows<true><<<blocks, 256, 0, s>>>(g, tab, a, b, nf);
+    k_host_rows<true><<<grid, 256, 0, s>>>(g, tab, a, b, nf);
   else
-    k_host_rows<false><<<blocks, 256, 0, s>>>(g, tab, a, b, nf);
+    k_host_rows<false><<<grid, 256, 0, s>>>(g, tab, a, b, nf);
 }
 
 }  // namespace sbfs

@@ -126,13 +126,17 @@ cudaError_t measure_fp64_peak(double *gflops);
 bool mlp_ready();
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b);
 
-// one scalar field between a host array of the reference's layout (tab[slot],
-// rows of `row` doubles, ay0 / ay1 ghost rows) and its device field (pitch p1)
+// one scalar field between a host array of the reference's layout (tab[z *
+// kLinkSlots + slot] for case z, rows of `row` doubles, ay0 / ay1 ghost rows)
+// and its device field (pitch p1, case z at dev + z * cs1)
+constexpr int kLinkSlots = 16;
 struct HostRows {
   int slot, row, ay0, ay1;
   double *dev;
 };
-// nf (1 or 2) fields, host -> device when in, else device -> host
-void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in, HostRows a, HostRows b, int nf);
+// nf (1 or 2) fields of every case, host -> device when in, else device ->
+// host, on about `width` blocks (at least one per case)
+void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in, HostRows a, HostRows b, int nf,
+                      int width);
 
 }  // namespace sbfs

@@ -83,3 +83,38 @@ def test_host_linked_follows_host_changes(libs):
     run(gpu, b, 2, False, True)
     for s in HOST_SLOTS:
         assert np.array_equal(a.field(s), b.field(s)), s
+
+
+def test_batch_host_linked_equals_memcpy(libs):
+    """a batch copies all cases of a grid group in one launch per field"""
+    gpu, orc = libs
+    wls = ic.ensemble(9, seed=11, grids=((32, 16), (64, 32), (128, 64)))
+    set_env(wls[0])
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    st0 = [new_state(wl, orc) for wl in wls]
+    a = [clone(s) for s in st0]
+    b = [clone(s) for s in st0]
+    for st in a + b:
+        for s in HOST_SLOTS:
+            st.field(s)[0] = np.nan
+            st.field(s)[-1] = np.nan
+    try:
+        gpu.batch_release()
+        for _ in range(3):
+            dta = gpu.integrate_batch(a)
+            assert gpu.host_link_used()
+        gpu.batch_release()
+        gpu.set_host_link(False)
+        for _ in range(3):
+            dtb = gpu.integrate_batch(b)
+            assert not gpu.host_link_used()
+    finally:
+        gpu.set_host_link(True)
+        gpu.batch_release()
+    assert list(dta) == list(dtb)
+    for k, (x, y) in enumerate(zip(a, b)):
+        for s in HOST_SLOTS:
+            assert np.array_equal(x.field(s), y.field(s)), (k, s)
+            assert np.isfinite(x.field(s)).all(), (k, s)
