@@ -394,8 +394,17 @@ int upload_poisson(Ctx &c, const domain_t *d) {
     // fac dies at the end of this iteration: wait for the copy
     CK(cudaStreamSynchronize(c.s));
   }
-  std::vector<double2> tw(M1);
+  // tw[m] = exp(-2 pi i m / ny), m = 0..M (the real-to-complex splits), then
+  // the butterflies' W_M^e, e < M, forward and inverse: W_M^e = tw[2e] or
+  // -tw[2e - M], the inverse its conjugate (exact sign flips of the same values)
+  const int M = ny / 2;
+  std::vector<double2> tw(M1 + 2 * (size_t)M);
   for (int m = 0; m < M1; ++m) tw[m] = make_double2(cos(2. * pi * m / ny), -sin(2. * pi * m / ny));
+  for (int e = 0; e < M; ++e) {
+    const double2 w = 2 * e <= M ? tw[2 * e] : make_double2(-tw[2 * e - M].x, -tw[2 * e - M].y);
+    tw[M1 + e] = w;
+    tw[M1 + M + e] = make_double2(w.x, -w.y);
+  }
   CK(cudaMemcpyAsync(c.b.twiddle, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, c.s));
   // the staging vectors die here: wait for the copies
   CK(cudaStreamSynchronize(c.s));
@@ -468,7 +477,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   b.tdm_stage = nullptr;
   if (const size_t ns = tdm_stage_doubles(c->nx, c->ny, nc, b.tiles.tdm_g))
     if (dalloc(*c, &b.tdm_stage, ns)) return 1;
-  if (dalloc(*c, &tmp, 2 * (size_t)M1)) return 1;
+  if (dalloc(*c, &tmp, 2 * ((size_t)M1 + 2 * (size_t)(c->ny / 2)))) return 1;
   b.twiddle = reinterpret_cast<double2 *>(tmp);
   if (dalloc(*c, &tmp, ((size_t)c->nx + 8) * nc)) return 1;
   b.dt_acc = reinterpret_cast<unsigned long long *>(tmp);

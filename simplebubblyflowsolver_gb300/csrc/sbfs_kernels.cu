@@ -583,18 +583,13 @@ __global__ void __launch_bounds__(BX *BY)
 // into the right-hand-side coefficients.
 // ---------------------------------------------------------------------------
 
-// twiddle W_M^e, e in [0, M), from tw[m] = exp(-2 pi i m / 2M), m = 0..M
-__device__ __forceinline__ double2 twiddle(const double2 *__restrict__ tw, int M, int e, bool inverse) {
-  const int idx = 2 * e;
-  double2 w = idx <= M ? tw[idx] : make_double2(-tw[idx - M].x, -tw[idx - M].y);
-  if (inverse) w.y = -w.y;
-  return w;
-}
-
 // Stockham FFT (radix 4, one radix-2 stage first when log2 M is odd) of W
 // rows of length M in shared memory.  Returns the buffer holding the result.
+// tw: the twiddle buffer, exp(-2 pi i m / 2M) for m = 0..M, then W_M^e for
+// e < M, then their conjugates (the inverse's): one load per twiddle.
 template <int W>
 __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__restrict__ tw, bool inverse) {
+  const double2 *__restrict__ wm = tw + (M + 1) + (inverse ? M : 0);
   int Ns = 1;
   if ((__ffs(M) - 1) & 1) {  // log2 M odd
     const int half = M >> 1;
@@ -621,9 +616,9 @@ __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__res
       double2 v0 = xr[j], v1 = xr[j + q4], v2 = xr[j + 2 * q4], v3 = xr[j + 3 * q4];
       if (Ns > 1) {
         const int e = kk * step;
-        v1 = cmul(v1, twiddle(tw, M, e, inverse));
-        v2 = cmul(v2, twiddle(tw, M, 2 * e, inverse));
-        v3 = cmul(v3, twiddle(tw, M, 3 * e, inverse));
+        v1 = cmul(v1, wm[e]);
+        v2 = cmul(v2, wm[2 * e]);
+        v3 = cmul(v3, wm[3 * e]);
       }
       const double2 a0 = cadd(v0, v2), a1 = csub(v0, v2), a2 = cadd(v1, v3), a3 = csub(v1, v3);
       // -i a3 (forward) or +i a3 (inverse)
