@@ -104,7 +104,8 @@ int sbfs_set_use_graphs(int on);
  * the step allows, overlapped with the step's own kernels.  Otherwise the
  * state moves by cudaMemcpy before and after the step.  Same results either
  * way, bit for bit.  sbfs_host_link_used says whether the last integrate()
- * was host-linked. */
+ * was host-linked.  on = 2 links registered arrays only, as on a system
+ * without host page-table access. */
 int sbfs_set_host_link(int on);
 int sbfs_host_link_used(void);
 

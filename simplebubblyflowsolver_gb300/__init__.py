@@ -76,10 +76,11 @@ class GpuLibrary(ReferenceAPI):
     def set_use_graphs(self, on: bool):
         self._ext("sbfs_set_use_graphs", 1 if on else 0)
 
-    def set_host_link(self, on: bool):
+    def set_host_link(self, on):
         """strict-mode steps copy the state in and out themselves, overlapped
-        with their kernels, when the GPU can address the host arrays"""
-        self._ext("sbfs_set_host_link", 1 if on else 0)
+        with their kernels, when the GPU can address the host arrays (True or
+        1); 2 links registered arrays only; False or 0 never"""
+        self._ext("sbfs_set_host_link", int(on))
 
     def host_link_used(self) -> bool:
         """whether the last integrate() was host-linked"""

@@ -50,7 +50,10 @@ double rk_g(int k) { return RK_A[k] + RK_B[k]; }
 
 int g_sync_mode = SBFS_SYNC_STATE;
 int g_use_graphs = 1;
-int g_host_link = 1;    // strict-mode steps copy the state themselves when they can
+// strict-mode steps copy the state themselves when they can: 1 = any host
+// memory the GPU addresses, 2 = registered memory only (as on a system
+// without host page-table access), 0 = never
+int g_host_link = 1;
 bool g_link_used = false;  // the last integrate() did
 double g_coef[3] = {-1., -1., -1.};
 
@@ -1208,7 +1211,8 @@ extern "C" {
 const char *sbfs_last_error(void) { return g_err.c_str(); }
 
 int sbfs_set_host_link(int on) {
-  g_host_link = on ? 1 : 0;
+  if (on < 0 || on > 2) return fail("bad host-link mode %d", on);
+  g_host_link = on;
   return 0;
 }
 
@@ -1479,16 +1483,18 @@ bool host_addressable(void *p, double **dev) {
                  cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, d) == cudaSuccess && v == 1;
     cudaGetLastError();
   }
-  if (g_pageable) {
+  if (g_pageable && g_host_link == 1) {
     *dev = static_cast<double *>(p);
     return true;
   }
-  void *q = nullptr;
-  if (cudaHostGetDevicePointer(&q, p, 0) != cudaSuccess) {
+  // registered (or cudaHostAlloc'd) memory and its device address
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  *dev = static_cast<double *>(q);
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return false;
+  *dev = static_cast<double *>(at.devicePointer);
   return true;
 }
 

@@ -118,3 +118,30 @@ def test_batch_host_linked_equals_memcpy(libs):
         for s in HOST_SLOTS:
             assert np.array_equal(x.field(s), y.field(s)), (k, s)
             assert np.isfinite(x.field(s)).all(), (k, s)
+
+
+def test_registered_only_link(libs):
+    """without host page-table access only registered arrays are linked
+    (mode 2 stands in for such a system): pinned arrays link, plain ones
+    take the cudaMemcpy path, and both give the same bits"""
+    gpu, orc = libs
+    wl = ic.single_bubble(128, 64)
+    set_env(wl)
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    st0 = new_state(wl, orc)
+    a, b = clone(st0), clone(st0)
+    gpu.pin_host_state(a)
+    try:
+        gpu.set_host_link(2)
+        for _ in range(3):
+            gpu.integrate(a)
+            assert gpu.host_link_used()
+            gpu.integrate(b)
+            assert not gpu.host_link_used()
+    finally:
+        gpu.set_host_link(True)
+        gpu.unpin_host_state(a)
+    for s in HOST_SLOTS:
+        assert np.array_equal(a.field(s), b.field(s)), s
