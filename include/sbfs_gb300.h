@@ -96,6 +96,11 @@ int sbfs_invalidate_device(void);
 /* capture each time step into a CUDA graph (default 1) */
 int sbfs_set_use_graphs(int on);
 
+/* launch the step's kernels with programmatic dependent launch (default 1):
+ * a kernel's blocks may start while the kernel before it on its stream
+ * finishes, and wait on the GPU for its results.  Same results either way. */
+int sbfs_set_pdl(int on);
+
 /* In SBFS_SYNC_STATE mode, let the step copy the state itself (default 1):
  * when the GPU can address the caller's arrays (pageable host memory on a
  * system with host page-table access, such as Grace-Blackwell, or arrays

@@ -38,6 +38,7 @@ class GpuLibrary(ReferenceAPI):
         lib.sbfs_set_sync_mode.argtypes = [C.c_int]
         lib.sbfs_set_use_graphs.argtypes = [C.c_int]
         lib.sbfs_set_host_link.argtypes = [C.c_int]
+        lib.sbfs_set_pdl.argtypes = [C.c_int]
         lib.sbfs_set_dt_coefs.argtypes = [C.c_double] * 3
         lib.sbfs_sync_to_host.argtypes = [C.c_void_p] * 3
         lib.sbfs_run_steps_timed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
@@ -75,6 +76,10 @@ class GpuLibrary(ReferenceAPI):
 
     def set_use_graphs(self, on: bool):
         self._ext("sbfs_set_use_graphs", 1 if on else 0)
+
+    def set_pdl(self, on: bool):
+        """launch the step's kernels with programmatic dependent launch"""
+        self._ext("sbfs_set_pdl", 1 if on else 0)
 
     def set_host_link(self, on):
         """strict-mode steps copy the state in and out themselves, overlapped

@@ -914,7 +914,8 @@ int autotune(Ctx &c) {
 }
 
 int role_key(const Ctx &c) {
-  return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5);
+  return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
+         (g_pdl << 6);
 }
 
 int launch_step(Ctx &c) {
@@ -1209,6 +1210,11 @@ Ctx *prepare_step(const domain_t *d, fluid_t *f, interface_t *itf) {
 extern "C" {
 
 const char *sbfs_last_error(void) { return g_err.c_str(); }
+
+int sbfs_set_pdl(int on) {
+  g_pdl = on ? 1 : 0;
+  return 0;
+}
 
 int sbfs_set_host_link(int on) {
   if (on < 0 || on > 2) return fail("bad host-link mode %d", on);

@@ -117,6 +117,16 @@ __host__ __device__ constexpr int sc_coldy(int k) { return 44 + 2 * k; }
 constexpr double kGaussPt = 0.2886751345948129;
 constexpr double kVofMin = 1.e-8;
 
+// programmatic dependent launch: every kernel of the step starts here and
+// waits until the kernel before it on the stream has completed and its
+// writes are visible.  The next kernel's launch is prepared while this one
+// runs and its blocks start as this one's last blocks exit (the implicit
+// trigger).  An explicit early trigger (griddepcontrol.launch_dependents at
+// entry) was slower: 1% on the 2048 x 1024 swarm, 12% on the 256 x 128
+// bubble, its waiting blocks sharing the SMs with an FP64-bound kernel.  A
+// kernel launched without the attribute passes the wait at once.
+__device__ __forceinline__ void pdl_entry() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // periodic row of J (J may be -1 .. ny + 2)
 __device__ __forceinline__ int wrap(int J, int ny) {
   int r = J - 1;

@@ -27,6 +27,8 @@
 
 namespace sbfs {
 
+int g_pdl = 1;  // step kernels launched with programmatic stream serialisation
+
 namespace {
 
 constexpr int BX = 32, BY = 8;
@@ -58,6 +60,7 @@ template <bool DEN, bool VIS, bool GRAD>
 __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, const double *__restrict__ vof,
                                                   double *__restrict__ den, double *__restrict__ visux,
                                                   double *__restrict__ visuy, double *__restrict__ dvof) {
+  pdl_entry();
   const Phys ph = zphys(g, ph0);
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -110,6 +113,7 @@ template <bool NORMAL, bool CURV, bool STORE_K>
 __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const double *__restrict__ vof,
                                                         const double *__restrict__ dvof, double *__restrict__ normal,
                                                         double *__restrict__ curv) {
+  pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -182,6 +186,7 @@ __global__ void __launch_bounds__(BX *BY)
                  const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
                  const double *__restrict__ curv, double *__restrict__ fluxx, double *__restrict__ fluxy,
                  double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
+  pdl_entry();
   const Phys ph = zphys(g, ph0);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -274,6 +279,7 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
                                                       const double *__restrict__ uy, double *__restrict__ curv,
                                                       int *__restrict__ list, int *__restrict__ count,
                                                       int *__restrict__ flist, int *__restrict__ fcount) {
+  pdl_entry();
   list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
   count += (size_t)blockIdx.z * (1);
   flist += (size_t)blockIdx.z * (4 * (size_t)g.nx * g.ny);
@@ -338,6 +344,7 @@ __global__ void __launch_bounds__(256)
     k_interface_cells(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
                       const double *__restrict__ vof, const double *__restrict__ dvof, const int *__restrict__ flist,
                       const int *__restrict__ fcount, double *__restrict__ fluxx, double *__restrict__ fluxy) {
+  pdl_entry();
   flist += (size_t)blockIdx.z * (4 * (size_t)g.nx * g.ny);
   fcount += (size_t)blockIdx.z * (1);
   const int n = *fcount;
@@ -387,6 +394,7 @@ __global__ void __launch_bounds__(BX *BY)
                   const double *__restrict__ fluxx, const double *__restrict__ fluxy, double *__restrict__ src_a,
                   const double *__restrict__ src_b, const double *__restrict__ ux, const double *__restrict__ uy,
                   double *__restrict__ mfx, double *__restrict__ mfy, double *__restrict__ den1) {
+  pdl_entry();
   const Phys ph = zphys(g, ph0);
   sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -424,6 +432,7 @@ __global__ void __launch_bounds__(BX *BY)
 // vof flux -> mass flux in place (src/interface/mass_flux.c:10-58); I = 0..nx+1
 __global__ void k_mass_flux(Grid g, Phys ph, const double *__restrict__ ux, const double *__restrict__ uy,
                             double *__restrict__ fluxx, double *__restrict__ fluxy) {
+  pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -444,6 +453,7 @@ __global__ void __launch_bounds__(BX *BY)
     k_stress(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
              const double *__restrict__ visux, const double *__restrict__ visuy, double *__restrict__ txx,
              double *__restrict__ txy, double *__restrict__ tyy) {
+  pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -485,6 +495,7 @@ __global__ void __launch_bounds__(BX *BY)
               const double *__restrict__ den1, double *__restrict__ sxa, const double *__restrict__ sxb,
               double *__restrict__ sxg, double *__restrict__ sya, const double *__restrict__ syb,
               double *__restrict__ syg, double *__restrict__ ex, double *__restrict__ ey) {
+  pdl_entry();
   const Phys ph = zphys(g, ph0);
   const double *__restrict__ nuf = m.nuf + (size_t)blockIdx.z * g.cm;
   const double *__restrict__ nuc = m.nuc + (size_t)blockIdx.z * g.cm;
@@ -642,6 +653,7 @@ __global__ void __launch_bounds__(256)
     k_poisson_fwd(Grid g, const double *__restrict__ sc, int k, const double *__restrict__ ux,
                   const double *__restrict__ uy, const double *__restrict__ psi, const double *__restrict__ ex,
                   const double *__restrict__ ey, const double2 *__restrict__ tw, double2 *__restrict__ spec) {
+  pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   spec += (size_t)blockIdx.z * (g.css);
   extern __shared__ double2 smem[];
@@ -684,6 +696,7 @@ __global__ void __launch_bounds__(256)
 template <int W>
 __global__ void __launch_bounds__(256)
     k_poisson_inv(Grid g, const double2 *__restrict__ tw, const double2 *__restrict__ spec, double *__restrict__ psi) {
+  pdl_entry();
   spec += (size_t)blockIdx.z * (g.css);
   extern __shared__ double2 smem[];
   const int ny = g.ny, M = ny >> 1, M1 = M + 1;
@@ -731,6 +744,7 @@ template <bool kGlobalStage>
 __global__ void __launch_bounds__(512)
     k_poisson_tdm(Grid g, int PB, int G, int L, int S, const double4_32a *__restrict__ fac,
                   const double2 *__restrict__ tw, double2 *__restrict__ spec, double *__restrict__ stage) {
+  pdl_entry();
   extern __shared__ double2 smem_d2[];
   __shared__ double xch[16][4][2];  // per system of the block, per warp of the system: a chunk-map total
   const int nx = g.nx, M = g.ny / 2, M1 = M + 1;
@@ -907,6 +921,7 @@ __global__ void __launch_bounds__(BX *BY)
     k_correct(Grid g, Metrics m, const double *__restrict__ sc, int k, double *__restrict__ ux,
               double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ psio,
               const double *__restrict__ ex, const double *__restrict__ ey, double *__restrict__ p) {
+  pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -947,6 +962,7 @@ __global__ void __launch_bounds__(BX *BY)
 
 // pressure update alone (fine-grained entry point); I = 1..nx
 __global__ void k_pressure(Grid g, const double *__restrict__ psin, double *__restrict__ p) {
+  pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -973,6 +989,7 @@ __global__ void __launch_bounds__(BX *BY)
     k_decide_dt(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
                 unsigned long long *__restrict__ acc, double *__restrict__ sc, int *__restrict__ status,
                 double dt_fixed, double coef_adv) {
+  pdl_entry();
   const Phys ph = zphys(g, ph0);
   if (g.phys) dt_fixed = ph.dtfix;
   acc += (size_t)blockIdx.z * ((size_t)g.nx + 8);
@@ -1081,6 +1098,7 @@ __global__ void __launch_bounds__(BX *BY)
 // from a density field, as k_predict stores it (fine-grained entry points)
 __global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, double *__restrict__ ex,
                               double *__restrict__ ey) {
+  pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -1121,6 +1139,7 @@ __global__ void __launch_bounds__(BX *BY)
     k_diag_partial(Grid g, Metrics m, const double *__restrict__ ux, const double *__restrict__ uy,
                    const double *__restrict__ vof, const double *__restrict__ den, const double *__restrict__ txy,
                    double nu, double *__restrict__ part) {
+  pdl_entry();
   __shared__ double sm[kDiag][BX * BY];
   const int I = blockIdx.x * BX + threadIdx.x + 1;
   const int J = blockIdx.y * BY + threadIdx.y + 1;
@@ -1163,6 +1182,7 @@ __global__ void __launch_bounds__(BX *BY)
 
 __global__ void __launch_bounds__(BX *BY) k_diag_final(const double *__restrict__ part, int nblocks,
                                                        double *__restrict__ out) {
+  pdl_entry();
   __shared__ double sm[kDiag][BX * BY];
   const int tid = threadIdx.x;
   double v[kDiag];
@@ -1183,6 +1203,7 @@ __global__ void __launch_bounds__(BX *BY) k_diag_final(const double *__restrict_
 __global__ void k_stats_collect(Grid g, const double *__restrict__ ux, const double *__restrict__ uy,
                                 const double *__restrict__ vof, double *__restrict__ ux1, double *__restrict__ uy1,
                                 double *__restrict__ vof1) {
+  pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -1194,24 +1215,28 @@ __global__ void k_stats_collect(Grid g, const double *__restrict__ ux, const dou
 
 // ---- boundary kernels of the fine-grained entry points (one thread per row)
 __global__ void k_bc_ux(Grid g, double *ux) {
+  pdl_entry();
   const int J = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (J > g.ny) return;
   ux[ix(g, J - 1, 0)] = 0.;
   ux[ix(g, J - 1, g.nx)] = 0.;
 }
 __global__ void k_bc_uy(Grid g, double *uy) {
+  pdl_entry();
   const int J = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (J > g.ny) return;
   uy[ix(g, J - 1, 0)] = 0.;
   uy[ix(g, J - 1, g.nx + 1)] = 0.;
 }
 __global__ void k_bc_neumann(Grid g, double *f) {
+  pdl_entry();
   const int J = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (J > g.ny) return;
   f[ix(g, J - 1, 0)] = f[ix(g, J - 1, 1)];
   f[ix(g, J - 1, g.nx + 1)] = f[ix(g, J - 1, g.nx)];
 }
 __global__ void k_bc_vof(Grid g, double *vof) {
+  pdl_entry();
   const int J = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (J > g.ny) return;
   vof[ix(g, J - 1, 0)] = 0.;
@@ -1368,44 +1393,44 @@ void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &p
                   bool grad, double *den_out) {
   const dim3 gr = tile_grid(b.tiles, TK_PROPS, g.nx + 2, g.ny, g.nc), bl = tile_block(b.tiles, TK_PROPS);
   if (den && vis && grad)
-    k_props<true, true, true><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<true, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
   else if (vis && grad)
-    k_props<false, true, true><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<false, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
   else if (den)
-    k_props<true, false, false><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<true, false, false>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
   else if (vis)
-    k_props<false, true, false><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<false, true, false>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
   else if (grad)
-    k_props<false, false, true><<<gr, bl, 0, s>>>(g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<false, false, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
 }
 
 void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv,
                         bool store_k) {
   const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
   if (normal && curv && store_k)
-    k_normal_curv<true, true, true><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+    launch_pdl(k_normal_curv<true, true, true>, gr, bl, 0, s, g, m, b.vof, b.dvof, b.normal, b.curv);
   else if (normal && curv)
-    k_normal_curv<true, true, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+    launch_pdl(k_normal_curv<true, true, false>, gr, bl, 0, s, g, m, b.vof, b.dvof, b.normal, b.curv);
   else if (normal)
-    k_normal_curv<true, false, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+    launch_pdl(k_normal_curv<true, false, false>, gr, bl, 0, s, g, m, b.vof, b.dvof, b.normal, b.curv);
   else if (curv)
-    k_normal_curv<false, true, false><<<gr, bl, 0, s>>>(g, m, b.vof, b.dvof, b.normal, b.curv);
+    launch_pdl(k_normal_curv<false, true, false>, gr, bl, 0, s, g, m, b.vof, b.dvof, b.normal, b.curv);
 }
 
 void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                        const double *ux, const double *uy, const double *den0, bool flux, bool force, bool have_k) {
   const dim3 gr = grid2d(g.nx, g.ny), bl(BX, BY);
   if (flux && force && have_k)
-    k_flux_force<true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+    launch_pdl(k_flux_force<true, true, true>, gr, bl, 0, s, g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                      b.fluxy, b.ifrcx, b.ifrcy);
   else if (flux && force)
-    k_flux_force<true, true, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+    launch_pdl(k_flux_force<true, true, false>, gr, bl, 0, s, g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                       b.fluxy, b.ifrcx, b.ifrcy);
   else if (flux)
-    k_flux_force<true, false, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+    launch_pdl(k_flux_force<true, false, false>, gr, bl, 0, s, g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                        b.fluxy, b.ifrcx, b.ifrcy);
   else if (force)
-    k_flux_force<false, true, false><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+    launch_pdl(k_flux_force<false, true, false>, gr, bl, 0, s, g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                        b.fluxy, b.ifrcx, b.ifrcy);
 }
 
@@ -1414,16 +1439,16 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
   const dim3 gr = tile_grid(b.tiles, TK_FLUX_FORCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_FLUX_FORCE);
   if (stage == 0) {
     cudaMemsetAsync(b.icount, 0, sizeof(int) * 2 * g.nc, s);  // cell and face counts
-    k_curv_list<<<tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s>>>(
+    launch_pdl(k_curv_list, tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s,
         g, m, b.vof, b.dvof, ux, uy, b.curv, b.ilist, b.icount, b.flist, b.fcount);
   } else if (stage == 1) {
-    k_interface_cells<<<dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s>>>(
+    launch_pdl(k_interface_cells, dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s,
         g, m, ux, uy, b.vof, b.dvof, b.flist, b.fcount, b.fluxx, b.fluxy);
   } else if (stage == 2) {
-    k_flux_force<true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
+    launch_pdl(k_flux_force<true, true, true, true>, gr, bl, 0, s, g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv, b.fluxx,
                                                            b.fluxy, b.ifrcx, b.ifrcy);
   } else {
-    k_flux_force<true, true, true, true, true><<<gr, bl, 0, s>>>(g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv,
+    launch_pdl(k_flux_force<true, true, true, true, true>, gr, bl, 0, s, g, m, ph, ux, uy, b.vof, b.normal, den0, b.curv,
                                                                  b.fluxx, b.fluxy, b.ifrcx, b.ifrcy);
   }
 }
@@ -1433,21 +1458,21 @@ void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const P
                         const double *uy, double *den1) {
   const dim3 gr = tile_grid(b.tiles, TK_VOF_ADVANCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_VOF_ADVANCE);
   if (fused)
-    k_vof_advance<true><<<gr, bl, 0, s>>>(g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, b.mfluxx,
+    launch_pdl(k_vof_advance<true>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, b.mfluxx,
                                           b.mfluxy, den1);
   else
-    k_vof_advance<false><<<gr, bl, 0, s>>>(g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, nullptr,
+    launch_pdl(k_vof_advance<false>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, nullptr,
                                            nullptr, nullptr);
 }
 
 void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *ux,
                               const double *uy) {
-  k_mass_flux<<<grid2d(g.nx + 2, g.ny), dim3(BX, BY), 0, s>>>(g, ph, ux, uy, b.fluxx, b.fluxy);
+  launch_pdl(k_mass_flux, grid2d(g.nx + 2, g.ny), dim3(BX, BY), 0, s, g, ph, ux, uy, b.fluxx, b.fluxy);
 }
 
 void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *ux,
                    const double *uy) {
-  k_stress<<<tile_grid(b.tiles, TK_STRESS, g.nx + 1, g.ny, g.nc), tile_block(b.tiles, TK_STRESS), 0, s>>>(g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
+  launch_pdl(k_stress, tile_grid(b.tiles, TK_STRESS, g.nx + 1, g.ny, g.nc), tile_block(b.tiles, TK_STRESS), 0, s, g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -1455,7 +1480,7 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                     const double *mfy, const double *den0, const double *den1, double *srcux_a,
                     const double *srcux_b, double *srcux_g, double *srcuy_a, const double *srcuy_b,
                     double *srcuy_g) {
-  k_predict<<<tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s>>>(g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
+  launch_pdl(k_predict, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
                                                         b.txy, b.tyy, b.p, b.ifrcx, b.ifrcy, den0, den1, srcux_a,
                                                         srcux_b, srcux_g, srcuy_a, srcuy_b, srcuy_g, b.irhox,
                                                         b.irhoy);
@@ -1465,7 +1490,7 @@ template <int W>
 void poisson_fwd_w(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                    const double *uy, const double *psi_old) {
   const int nb = (g.nx + W - 1) / W;
-  k_poisson_fwd<W><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s>>>(g, sc, k, ux, uy, psi_old, b.irhox,
+  launch_pdl(k_poisson_fwd<W>, dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s, g, sc, k, ux, uy, psi_old, b.irhox,
                                                                            b.irhoy, b.twiddle, b.spec);
 }
 
@@ -1486,19 +1511,19 @@ void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
   const int pairs = g.ny / 4 + 1;
   const double4_32a *fac = reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]);
   if (tdm_global_stage(g.nx, G)) {  // one pair per block, staged in b.tdm_stage
-    k_poisson_tdm<true><<<dim3(pairs, 1, g.nc), 128 * G, 0, s>>>(g, 1, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
+    launch_pdl(k_poisson_tdm<true>, dim3(pairs, 1, g.nc), 128 * G, 0, s, g, 1, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
                                                                  fac, b.twiddle, b.spec, b.tdm_stage);
     return;
   }
   const int mb = tdm_modes_per_block(b.tiles, g.nx);  // wavenumber pairs per block
-  k_poisson_tdm<false><<<dim3((pairs + mb - 1) / mb, 1, g.nc), 128 * mb * G, poisson_tdm_smem(g.nx, mb, G), s>>>(
+  launch_pdl(k_poisson_tdm<false>, dim3((pairs + mb - 1) / mb, 1, g.nc), 128 * mb * G, poisson_tdm_smem(g.nx, mb, G), s,
       g, mb, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G), fac, b.twiddle, b.spec, nullptr);
 }
 
 template <int W>
 void poisson_inv_w(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
   const int nb = (g.nx + W - 1) / W;
-  k_poisson_inv<W><<<dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s>>>(g, b.twiddle, b.spec, psi_new);
+  launch_pdl(k_poisson_inv<W>, dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s, g, b.twiddle, b.spec, psi_new);
 }
 
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new) {
@@ -1523,13 +1548,13 @@ void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs 
                     double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure) {
   const dim3 gr = tile_grid(b.tiles, TK_CORRECT, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_CORRECT);
   if (pressure)
-    k_correct<true><<<gr, bl, 0, s>>>(g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
+    launch_pdl(k_correct<true>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
   else
-    k_correct<false><<<gr, bl, 0, s>>>(g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
+    launch_pdl(k_correct<false>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
 }
 
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new) {
-  k_pressure<<<grid2d(g.nx, g.ny), dim3(BX, BY), 0, s>>>(g, psi_new, b.p);
+  launch_pdl(k_pressure, grid2d(g.nx, g.ny), dim3(BX, BY), 0, s, g, psi_new, b.p);
 }
 
 void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
@@ -1537,12 +1562,12 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
   int gy = (g.ny + BY - 1) / BY;
   const int gx = (g.nx + BX) / BX;
   while (gy > 1 && gx * gy * g.nc > 4 * 152) gy = (gy + 1) / 2;
-  k_decide_dt<<<dim3(gx, gy, g.nc), dim3(BX, BY), 0, s>>>(g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
+  launch_pdl(k_decide_dt, dim3(gx, gy, g.nc), dim3(BX, BY), 0, s, g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
                                                     coef_adv);
 }
 
 void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey) {
-  k_face_factor<<<grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s>>>(g, ph, den, ex, ey);
+  launch_pdl(k_face_factor, grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s, g, ph, den, ex, ey);
 }
 
 int diag_partial_blocks(const Grid &g) {
@@ -1554,22 +1579,22 @@ void launch_diagnostics(cudaStream_t s, const Grid &g, const Metrics &m, const d
                         const double *vof, const double *den, const double *txy, double nu, double *part,
                         double *out) {
   const dim3 gr = grid2d(g.nx, g.ny);
-  k_diag_partial<<<gr, dim3(BX, BY), 0, s>>>(g, m, ux, uy, vof, den, txy, nu, part);
-  k_diag_final<<<1, BX * BY, 0, s>>>(part, (int)(gr.x * gr.y), out);
+  launch_pdl(k_diag_partial, gr, dim3(BX, BY), 0, s, g, m, ux, uy, vof, den, txy, nu, part);
+  launch_pdl(k_diag_final, 1, BX * BY, 0, s, part, (int)(gr.x * gr.y), out);
 }
 
 void launch_stats_collect(cudaStream_t s, const Grid &g, const double *ux, const double *uy, const double *vof,
                           double *ux1, double *uy1, double *vof1) {
-  k_stats_collect<<<grid2d(g.nx + 2, g.ny), dim3(BX, BY), 0, s>>>(g, ux, uy, vof, ux1, uy1, vof1);
+  launch_pdl(k_stats_collect, grid2d(g.nx + 2, g.ny), dim3(BX, BY), 0, s, g, ux, uy, vof, ux1, uy1, vof1);
 }
 
-void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux) { k_bc_ux<<<(g.ny + 127) / 128, 128, 0, s>>>(g, ux); }
-void launch_bc_uy(cudaStream_t s, const Grid &g, double *uy) { k_bc_uy<<<(g.ny + 127) / 128, 128, 0, s>>>(g, uy); }
+void launch_bc_ux(cudaStream_t s, const Grid &g, double *ux) { launch_pdl(k_bc_ux, (g.ny + 127) / 128, 128, 0, s, g, ux); }
+void launch_bc_uy(cudaStream_t s, const Grid &g, double *uy) { launch_pdl(k_bc_uy, (g.ny + 127) / 128, 128, 0, s, g, uy); }
 void launch_bc_neumann(cudaStream_t s, const Grid &g, double *f) {
-  k_bc_neumann<<<(g.ny + 127) / 128, 128, 0, s>>>(g, f);
+  launch_pdl(k_bc_neumann, (g.ny + 127) / 128, 128, 0, s, g, f);
 }
 void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof) {
-  k_bc_vof<<<(g.ny + 127) / 128, 128, 0, s>>>(g, vof);
+  launch_pdl(k_bc_vof, (g.ny + 127) / 128, 128, 0, s, g, vof);
 }
 
 // ---------------------------------------------------------------------------
@@ -1584,6 +1609,7 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof) {
 // the link's latency is microseconds.
 template <bool kIn>
 __global__ void __launch_bounds__(256) k_host_rows(Grid g, double *const *tab, HostRows a, HostRows b, int nf) {
+  pdl_entry();
   const int z = blockIdx.y;
   const int stride = gridDim.x * blockDim.x;
   for (int q = 0; q < nf; ++q) {
@@ -1620,9 +1646,9 @@ void launch_host_rows(cudaStream_t s, const Grid &g, double *const *tab, bool in
                       int width) {
   const dim3 grid(std::max(1, width / g.nc), g.nc);
   if (in)
-    k_host_rows<true><<<grid, 256, 0, s>>>(g, tab, a, b, nf);
+    launch_pdl(k_host_rows<true>, grid, 256, 0, s, g, tab, a, b, nf);
   else
-    k_host_rows<false><<<grid, 256, 0, s>>>(g, tab, a, b, nf);
+    launch_pdl(k_host_rows<false>, grid, 256, 0, s, g, tab, a, b, nf);
 }
 
 }  // namespace sbfs

@@ -103,6 +103,26 @@ void launch_bc_uy(cudaStream_t s, const Grid &g, double *uy);
 void launch_bc_neumann(cudaStream_t s, const Grid &g, double *f);
 void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
 
+// launches of the step kernels: programmatic stream serialisation, so that a
+// kernel's blocks may start before the one before it on the stream ends (each
+// kernel begins with pdl_entry, which waits for it); g_pdl = 0 launches
+// them plainly
+extern int g_pdl;
+template <typename... P, typename... A>
+void launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A &&...a) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = g_pdl ? 1 : 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(a)...);
+}
+
 // smem budget checks (host side)
 int poisson_fft_cols(int ny);
 int poisson_tdm_modes(int nx);

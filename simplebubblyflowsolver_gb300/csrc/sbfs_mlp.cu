@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
                                                       const double *__restrict__ vof, const double *__restrict__ dvof,
                                                       const int *__restrict__ list, const int *__restrict__ count,
                                                       double *__restrict__ curv, int *__restrict__ used) {
+  pdl_entry();
   extern __shared__ unsigned char smraw[];
   SmemW &w = *reinterpret_cast<SmemW *>(smraw);
   __nv_bfloat16(*xs)[16][NF] = reinterpret_cast<__nv_bfloat16(*)[16][NF]>(smraw + sizeof(SmemW));
@@ -492,7 +493,7 @@ size_t smem_infer() { return sizeof(SmemW) + sizeof(__nv_bfloat16) * 8 * 16 * NF
 namespace sbfs {
 bool mlp_ready() { return g_params != nullptr; }
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b) {
-  k_mlp_curv<<<dim3(max(2, (2 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, smem_infer(), s>>>(
+  launch_pdl(k_mlp_curv, dim3(max(2, (2 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, smem_infer(), s,
       g, g_params, b.vof, b.dvof, b.ilist, b.icount, b.curv, g_used);
 }
 }  // namespace sbfs

@@ -104,6 +104,33 @@ def test_graphs_equal_eager(libs):
         assert np.array_equal(a.interior_rows(s), b.interior_rows(s)), s
 
 
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph", "eager"])
+def test_pdl_equals_plain_launches(libs, graphs):
+    """programmatic dependent launch changes when blocks start, not what they
+    compute: same bits as plain launches, in graphs and eagerly, resident too"""
+    gpu, orc = libs
+    wl = ic.bubble_swarm(256, 128, nbubbles=8, seed=2)
+    st0 = prepare(libs, wl)
+    a, b = clone(st0), clone(st0)
+    gpu.set_use_graphs(graphs)
+    try:
+        for st, pdl in ((a, True), (b, False)):
+            gpu.set_pdl(pdl)
+            for _ in range(2):
+                gpu.integrate(st)
+            gpu.set_sync_mode(SYNC_NONE)
+            for _ in range(2):
+                gpu.integrate(st)
+            gpu.sync_to_host(st)
+            gpu.set_sync_mode(SYNC_STATE)
+    finally:
+        gpu.set_pdl(True)
+        gpu.set_use_graphs(True)
+        gpu.set_sync_mode(SYNC_STATE)
+    for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+        assert np.array_equal(a.field(s), b.field(s)), s
+
+
 def test_matches_reference_fixtures(libs):
     """the GPU against the reference's own results (golden fixtures made by
     tests/golden/make_golden.py from the reference sources)"""
