@@ -261,9 +261,12 @@ int sbfs_mlp_train_epoch(const void *X, const float *Y, const int *idx, int n, i
 int sbfs_mlp_predict(const void *X, int n, float *out);
 /* 0: kappa = -div n (the reference, default); 1: the learned closure in
  * interface cells whose stencil is in range (centre vof in [0.01, 0.99], a
- * prediction |kappa dx| in [0.015, 0.55]), plain kappa elsewhere.  Square
- * cells.  Applies to integrate() and the timed runs. */
+ * prediction |kappa dx| in the closure's range), plain kappa elsewhere.
+ * Square cells.  Applies to integrate() and the timed runs. */
 int sbfs_set_curvature_model(int model);
+/* the closure's range in |kappa dx| (default [0.02, 0.5]: the training
+ * circles' radii, 2 .. 50 cells) */
+int sbfs_mlp_set_range(double lo, double hi);
 /* interface cells that took the learned curvature since the last call */
 int sbfs_mlp_take_usage(long long *used);
 const char *sbfs_mlp_last_error(void);

@@ -270,6 +270,7 @@ class GpuLibrary(ReferenceAPI):
         L.sbfs_mlp_predict.argtypes = [vp, C.c_int, vp]
         L.sbfs_mlp_take_usage.argtypes = [C.POINTER(C.c_longlong)]
         L.sbfs_set_curvature_model.argtypes = [C.c_int]
+        L.sbfs_mlp_set_range.argtypes = [C.c_double, C.c_double]
         L._mlp_typed = True
 
     def mlp_set_params(self, params):
@@ -310,6 +311,11 @@ class GpuLibrary(ReferenceAPI):
         u = C.c_longlong(0)
         self._mlp("sbfs_mlp_take_usage", C.byref(u))
         return u.value
+
+    def mlp_set_range(self, lo: float, hi: float):
+        """the closure's range in |kappa dx| (default 0.02 .. 0.5)"""
+        self._mlp_types()
+        self._mlp("sbfs_mlp_set_range", lo, hi)
 
     def set_curvature_model(self, model: int):
         """0: the reference's kappa = -div n; 1: the learned closure"""

@@ -933,9 +933,11 @@ int launch_step(Ctx &c) {
   }
   {
     const Phys &p = c.ph;
+    float klo, khi;  // the learned closure's range (a kernel argument when it runs)
+    mlp_range(&klo, &khi);
     const std::vector<double> sig = {p.denr, p.visr,   p.refden,   p.den_lo,   p.den_hi,   p.vis_lo,
                                      p.vis_hi, p.grav, p.force_coef, p.irefden, p.nu,      c.dt_fixed,
-                                     g_coef[0], g_coef[1], g_coef[2]};
+                                     g_coef[0], g_coef[1], g_coef[2], klo, khi};
     std::vector<double> all(sig);
     for (const Phys &q : c.phys_host) {
       const double *w = reinterpret_cast<const double *>(&q);

@@ -144,6 +144,7 @@ cudaError_t measure_fp64_peak(double *gflops);
 // learned curvature closure (sbfs_mlp.cu): parameters present, and the
 // in-step kernel overwriting curv in the listed interface cells
 bool mlp_ready();
+void mlp_range(float *lo, float *hi);  // the closure's range in |kappa dx|
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b);
 
 // one scalar field between a host array of the reference's layout (tab[z *

@@ -368,12 +368,13 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_predict(const float *__restric
 
 // In the fused step: curvature of the listed interface cells from the
 // network when the stencil is inside the training distribution (centre vof in
-// [0.01, 0.99], all stencil values in [0, 1], |kappa dx| in [0.015, 0.55]);
-// the plain curvature already in `curv` stays otherwise.  Square cells.
+// [0.01, 0.99], all stencil values in [0, 1], |kappa dx| in [lo, hi]); the
+// plain curvature already in `curv` stays otherwise.  Square cells.
 __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__restrict__ params,
                                                       const double *__restrict__ vof, const double *__restrict__ dvof,
                                                       const int *__restrict__ list, const int *__restrict__ count,
-                                                      double *__restrict__ curv, int *__restrict__ used) {
+                                                      double *__restrict__ curv, int *__restrict__ used, float lo,
+                                                      float hi) {
   pdl_entry();
   extern __shared__ unsigned char smraw[];
   SmemW &w = *reinterpret_cast<SmemW *>(smraw);
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
     const float o = (lane & 8) ? ob : oa;
     if (lane < 16 && ok) {
       const float a = fabsf(o);
-      if (a >= 0.015f && a <= 0.55f) {
+      if (a >= lo && a <= hi) {
         const int rc = cell / g.nx, I = cell - rc * g.nx + 1;
         curv[(size_t)(rc + zr) * g.p1 + I] = (double)o * g.idx;
         ++nused;
@@ -492,15 +493,32 @@ size_t smem_infer() { return sizeof(SmemW) + sizeof(__nv_bfloat16) * 8 * 16 * NF
 // ---- entry points used by the solver (sbfs_api.cu)
 namespace sbfs {
 bool mlp_ready() { return g_params != nullptr; }
+// the closure's range in |kappa dx|: the curvatures of the training circles,
+// radii 2 .. 50 cells
+float g_kappa_lo = 0.02f, g_kappa_hi = 0.5f;
+void mlp_range(float *lo, float *hi) {
+  *lo = g_kappa_lo;
+  *hi = g_kappa_hi;
+}
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b) {
   launch_pdl(k_mlp_curv, dim3(max(2, (2 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, smem_infer(), s,
-      g, g_params, b.vof, b.dvof, b.ilist, b.icount, b.curv, g_used);
+      g, g_params, b.vof, b.dvof, b.ilist, b.icount, b.curv, g_used, g_kappa_lo, g_kappa_hi);
 }
 }  // namespace sbfs
 
 extern "C" {
 
 const char *sbfs_mlp_last_error(void) { return g_mlp_err; }
+
+int sbfs_mlp_set_range(double lo, double hi) {
+  if (!(lo >= 0. && hi > lo)) {
+    snprintf(g_mlp_err, sizeof(g_mlp_err), "bad closure range [%g, %g]", lo, hi);
+    return 1;
+  }
+  sbfs::g_kappa_lo = (float)lo;
+  sbfs::g_kappa_hi = (float)hi;
+  return 0;
+}
 
 int sbfs_mlp_nparams(void) { return NPARAM; }
 

@@ -448,6 +448,39 @@ def interface_stencils(vof_rows: np.ndarray, vofmin=1e-8):
     return st, rr, cc
 
 
+# the closure's default range in |kappa dx|: the training circles, radii 2 .. 50 cells
+KAPPA_RANGE = (0.02, 0.5)
+
+
+def static_drop_table(lib, ns=(64, 128, 256), steps=1000, params=None, log=None):
+    """the static-drop comparison of the plain curvature, the learned closure
+    (trained with train_default unless params are given) and the exact
+    curvature (a constant network output kappa dx = 4 / n, the closure's range
+    opened so that it applies everywhere); one row per (n, variant) with the
+    measures of evaluate_static_drop and the mean of 10 parasitic-velocity
+    samples over the run"""
+    if params is None:
+        _, params, _ = train_default(lib, log=log)
+    rows = []
+    for n in ns:
+        exact = np.zeros(NPARAM, dtype=np.float32)
+        exact[-1] = 4.0 / n
+        for name, model, p, rng in (("plain", 0, None, KAPPA_RANGE), ("learned", 1, params, KAPPA_RANGE),
+                                    ("exact", 1, exact, (0.0, 1.0))):
+            lib.mlp_set_range(*rng)
+            try:
+                r = evaluate_static_drop(lib, n=n, steps=steps, model=model, params=p, record_every=steps // 10)
+            finally:
+                lib.mlp_set_range(*KAPPA_RANGE)
+            r["variant"] = name
+            r["umax_mean"] = float(np.mean([u for _, _, u in r["umax_history"]]))
+            rows.append(r)
+            if log:
+                log(f"{n} {name}: kappa rms {r['kappa_rms_rel_err']:.3g} umax mean {r['umax_mean']:.3g} "
+                    f"dp err {r['dp_rel_err']:.3g}")
+    return rows
+
+
 def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_every=0):
     """Run the static drop (r = 0.25 in the unit box, density ratio 1e-3,
     La = 12000) for `steps` steps with curvature model 0 (-div n) or 1 (the
