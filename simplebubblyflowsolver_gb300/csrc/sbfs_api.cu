@@ -1483,12 +1483,17 @@ int sbfs_sync_to_host(const domain_t *d, fluid_t *f, interface_t *itf) {
 
 // host memory the GPU can address: any on a system whose GPU reads pageable
 // memory through the host page tables, else memory registered with CUDA
-int g_pageable = -1;
+int g_pageable = -1, g_pageable_dev = -1;  // the attribute of device g_pageable_dev
 bool host_addressable(void *p, double **dev) {
-  if (g_pageable < 0) {
-    int d = 0, v = 0;
-    g_pageable = cudaGetDevice(&d) == cudaSuccess &&
-                 cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, d) == cudaSuccess && v == 1;
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (d != g_pageable_dev) {
+    int v = 0;
+    g_pageable = cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, d) == cudaSuccess && v == 1;
+    g_pageable_dev = d;
     cudaGetLastError();
   }
   if (g_pageable && g_host_link == 1) {
