@@ -624,14 +624,25 @@ __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__res
       const double2 *xr = x + c * M;
       double2 *yr = y + c * M;
       const int kk = j & (Ns - 1);
-      double2 v0 = xr[j], v1 = xr[j + q4], v2 = xr[j + 2 * q4], v3 = xr[j + 3 * q4];
+      const double2 v0 = xr[j], v1 = xr[j + q4], v2 = xr[j + 2 * q4], v3 = xr[j + 3 * q4];
+      double2 a0, a1, a2, a3;
       if (Ns > 1) {
+        // a0 = v0 + w2 v2 and a2 = w1 v1 + w3 v3 with the products folded into
+        // FMAs, a1 = 2 v0 - a0 and a3 = 2 (w1 v1) - a2: 24 FP64 operations per
+        // butterfly instead of 28 (cmul, then add and subtract)
         const int e = kk * step;
-        v1 = cmul(v1, wm[e]);
-        v2 = cmul(v2, wm[2 * e]);
-        v3 = cmul(v3, wm[3 * e]);
+        const double2 w1 = wm[e], w2 = wm[2 * e], w3 = wm[3 * e];
+        a0 = make_double2(fma(w2.x, v2.x, fma(-w2.y, v2.y, v0.x)), fma(w2.x, v2.y, fma(w2.y, v2.x, v0.y)));
+        a1 = make_double2(fma(2., v0.x, -a0.x), fma(2., v0.y, -a0.y));
+        const double2 t1 = cmul(v1, w1);
+        a2 = make_double2(fma(w3.x, v3.x, fma(-w3.y, v3.y, t1.x)), fma(w3.x, v3.y, fma(w3.y, v3.x, t1.y)));
+        a3 = make_double2(fma(2., t1.x, -a2.x), fma(2., t1.y, -a2.y));
+      } else {
+        a0 = cadd(v0, v2);
+        a1 = csub(v0, v2);
+        a2 = cadd(v1, v3);
+        a3 = csub(v1, v3);
       }
-      const double2 a0 = cadd(v0, v2), a1 = csub(v0, v2), a2 = cadd(v1, v3), a3 = csub(v1, v3);
       // -i a3 (forward) or +i a3 (inverse)
       const double2 r3 = inverse ? make_double2(-a3.y, a3.x) : make_double2(a3.y, -a3.x);
       const int d = ((j - kk) << 2) + kk;
