@@ -779,10 +779,11 @@ __global__ void __launch_bounds__(512)
       const double2 zr = sp[(size_t)i * M1 + (p == 0 ? 0 : M - p)];
       const double2 E = make_double2(zm.x + zr.x, zm.y - zr.y);
       const double2 O = make_double2(zm.y + zr.y, zr.x - zm.x);  // -i (zm - conj zr)
-      xa = cadd(E, cmul(tw[p], O));
-      const double2 E2 = make_double2(zr.x + zm.x, zr.y - zm.y);
-      const double2 O2 = make_double2(zr.y + zm.y, zm.x - zr.x);
-      xb = cadd(E2, cmul(tw[M - p], O2));
+      // X_p = E + w^p O; X_{M-p} = conj E + w^{M-p} conj O (the pair's E and O
+      // with the signs of their imaginary parts flipped), products in FMAs
+      const double2 wa = tw[p], wb = tw[M - p];
+      xa = make_double2(fma(wa.x, O.x, fma(-wa.y, O.y, E.x)), fma(wa.x, O.y, fma(wa.y, O.x, E.y)));
+      xb = make_double2(fma(wb.x, O.x, fma(wb.y, O.y, E.x)), fma(wb.y, O.x, fma(-wb.x, O.y, -E.y)));
     }
     sm[(4 * q) * sys_len + at] = xa.x;
     sm[(4 * q + 1) * sys_len + at] = xa.y;
@@ -904,17 +905,17 @@ __global__ void __launch_bounds__(512)
     const int at = (i / L) * S + (i % L);
     const double2 Xa = make_double2(sm[(4 * q) * sys_len + at], sm[(4 * q + 1) * sys_len + at]);
     const double2 Xb = make_double2(sm[(4 * q + 2) * sys_len + at], sm[(4 * q + 3) * sys_len + at]);
-    {
-      const double2 E = make_double2(Xa.x + Xb.x, Xa.y - Xb.y);
-      const double2 D = make_double2(Xa.x - Xb.x, Xa.y + Xb.y);
-      const double2 O = cmul(D, make_double2(tw[p].x, -tw[p].y));
-      sp[(size_t)i * M1 + p] = make_double2(E.x - O.y, E.y + O.x);
-    }
+    // z_p = E + i D conj w^p and z_{M-p} = conj E - i conj D conj w^{M-p}, with
+    // E = X_p + conj X_{M-p}, D = X_p - conj X_{M-p}; products in FMAs
+    const double2 E = make_double2(Xa.x + Xb.x, Xa.y - Xb.y);
+    const double2 D = make_double2(Xa.x - Xb.x, Xa.y + Xb.y);
+    const double2 wa = tw[p];
+    sp[(size_t)i * M1 + p] =
+        make_double2(fma(D.x, wa.y, fma(-D.y, wa.x, E.x)), fma(D.y, wa.y, fma(D.x, wa.x, E.y)));
     if (p != 0 && 2 * p != M) {
-      const double2 E = make_double2(Xb.x + Xa.x, Xb.y - Xa.y);
-      const double2 D = make_double2(Xb.x - Xa.x, Xb.y + Xa.y);
-      const double2 O = cmul(D, make_double2(tw[M - p].x, -tw[M - p].y));
-      sp[(size_t)i * M1 + (M - p)] = make_double2(E.x - O.y, E.y + O.x);
+      const double2 wb = tw[M - p];
+      sp[(size_t)i * M1 + (M - p)] =
+          make_double2(fma(-D.y, wb.x, fma(-D.x, wb.y, E.x)), fma(D.y, wb.y, fma(-D.x, wb.x, -E.y)));
     }
   }
 }
