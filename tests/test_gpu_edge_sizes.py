@@ -1,9 +1,8 @@
 """Grid sizes at the edges of what the library accepts, against the oracle:
 ny at its minimum (8) and maximum (8192, one transform column per block),
 nx at its maximum (8192: the tridiagonal systems of a wavenumber pair exceed
-shared memory and are staged in global memory), nx that no block shape
-divides, and sizes where the tridiagonal systems are split over 2 or 4 warps
-with padded chunks."""
+shared memory and are staged in global memory; 4 warps per system), nx that no
+block shape divides, and chunked systems padded past nx (200 x 16)."""
 import pytest
 
 from simplebubblyflowsolver_gb300 import SYNC_STATE, ic
@@ -47,10 +46,10 @@ def bubble(nx, ny, We):
 # state is no parity case.  At nx = 8192 the floors grow by orders of
 # magnitude a step after the second, so that case runs two steps.
 CASES = [
-    (64, 8, bubble, 10.0, 5),            # min ny; 4 warps per system
+    (64, 8, bubble, 10.0, 5),            # min ny
     (8192, 8, bubble, 10.0, 2),          # max nx: global staging, 4 warps, 64 rows a lane
     (37, 64, bubble, 10.0, 5),           # odd nx, ragged blocks of every shape
-    (200, 16, bubble, 10.0, 5),          # 4 warps, 2 rows a lane, 56 padding rows
+    (200, 16, bubble, 10.0, 5),          # 7 rows a lane, 24 padding rows
     (256, 512, square_cells, 10.0, 5),   # a tall domain, 129 wavenumber pairs
     (32, 4096, square_cells, 100.0, 5),  # two transform columns per block
     (32, 8192, square_cells, 100.0, 5),  # max ny: one transform column per block

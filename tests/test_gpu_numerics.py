@@ -33,9 +33,9 @@ def test_poisson_manufactured_solution(nx, ny, bar):
     """the GPU Poisson solve (transforms along y, tridiagonal solves along x)
     against a known answer: u* = grad(phi) with a uniform density and psi_old
     = 0 gives psi = rho_ref / dt_new * phi up to a constant, phi = cos(pi x /
-    lx) cos(2 pi y / ly).  The grids cover 4 warps per system with padded
-    chunks (200 x 16), systems staged in global memory (8192 x 8) and 2 and 1
-    transform columns per block (ny = 4096, 8192)."""
+    lx) cos(2 pi y / ly).  The grids cover chunked systems padded past nx
+    (200 x 16), 4 warps per system staged in global memory (8192 x 8) and 2
+    and 1 transform columns per block (ny = 4096, 8192)."""
     from simplebubblyflowsolver_gb300 import ic, load_library
     from simplebubblyflowsolver_gb300.binding import state_from_fields
     from ._helpers import set_env
