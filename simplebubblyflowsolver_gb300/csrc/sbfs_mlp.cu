@@ -152,18 +152,21 @@ struct SmemTrain {
   __nv_bfloat16 h1[TILE][NH + 8];
   __nv_bfloat16 dz2[TILE][NH + 8];
   __nv_bfloat16 dz1[TILE][NH + 8];
-  float gsum[3][NH];  // block sums of gb1, gb2, gw3
-  float gb3;
-  double loss;
+  float gsum[WARPS][3][NH];  // per warp: its sums of gb1, gb2, gw3
+  float gb3[WARPS];
+  double loss[WARPS];
 };
 
 // gradients of the mean-square loss over a batch of `nbatch` rows, one
 // 128-row tile per block: rows idx[tile*128 + r] of X (bf16 [n][16]) with
-// targets y; accumulates into grad (FP32, atomic) and loss (FP64, atomic)
+// targets y.  Block b writes its gradient to gblk[b * NPARAM ..] and its
+// squared-error sum to lblk[b]; k_mlp_adam or k_mlp_reduce add the blocks in
+// order.  No atomics: every sum has a fixed order, so training is
+// reproducible bit for bit.
 __global__ void __launch_bounds__(TILE * 2) k_mlp_grad(const float *__restrict__ params,
                                                       const __nv_bfloat16 *__restrict__ X,
                                                       const float *__restrict__ Y, const int *__restrict__ idx,
-                                                      int nbatch, float *__restrict__ grad, double *__restrict__ loss) {
+                                                      int nbatch, float *__restrict__ gblk, double *__restrict__ lblk) {
   extern __shared__ unsigned char smraw[];
   SmemTrain &s = *reinterpret_cast<SmemTrain *>(smraw);
   load_weights(s.w, params);
@@ -172,11 +175,6 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_grad(const float *__restrict__
     const int r = i / NF, c = i % NF;
     const int row = base + r;
     s.x[r][c] = row < nbatch ? X[(size_t)idx[row] * NF + c] : __float2bfloat16_rn(0.f);
-  }
-  for (int i = threadIdx.x; i < 3 * NH; i += blockDim.x) (&s.gsum[0][0])[i] = 0.f;
-  if (threadIdx.x == 0) {
-    s.gb3 = 0.f;
-    s.loss = 0.;
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -191,9 +189,19 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_grad(const float *__restrict__
     const float ya = ra < nbatch ? Y[idx[ra]] : 0.f, yb = rb < nbatch ? Y[idx[rb]] : 0.f;
     const float ea = ra < nbatch ? f.out0 - ya : 0.f, eb = rb < nbatch ? f.out1 - yb : 0.f;
     const float da = ea * invn, db = eb * invn;  // d loss / d out
-    if (t == 0) {
-      atomicAdd(&s.loss, (double)ea * ea + (double)eb * eb);
-      atomicAdd(&s.gb3, da + db);
+    {
+      // the warp's sums over its 16 rows (the lanes t = 0 hold each row once)
+      double lw = t == 0 ? (double)ea * ea + (double)eb * eb : 0.;
+      float bw = t == 0 ? da + db : 0.f;
+#pragma unroll
+      for (int m = 1; m < 32; m <<= 1) {
+        lw += __shfl_xor_sync(0xffffffffu, lw, m);
+        bw += __shfl_xor_sync(0xffffffffu, bw, m);
+      }
+      if (lane == 0) {
+        s.loss[warp] = lw;
+        s.gb3[warp] = bw;
+      }
     }
     // gw3 (column sums of h2 * dout), gb2, dz2 and h1 to shared memory
 #pragma unroll
@@ -211,10 +219,10 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_grad(const float *__restrict__
         gb1 += __shfl_xor_sync(0xffffffffu, gb1, m);
       }
       if (g == 0) {
-        atomicAdd(&s.gsum[2][c0], gw0);
-        atomicAdd(&s.gsum[2][c0 + 1], gw1);
-        atomicAdd(&s.gsum[1][c0], gb0);
-        atomicAdd(&s.gsum[1][c0 + 1], gb1);
+        s.gsum[warp][2][c0] = gw0;
+        s.gsum[warp][2][c0 + 1] = gw1;
+        s.gsum[warp][1][c0] = gb0;
+        s.gsum[warp][1][c0 + 1] = gb1;
       }
       s.dz2[r0 + g][c0] = __float2bfloat16_rn(z0);
       s.dz2[r0 + g][c0 + 1] = __float2bfloat16_rn(z1);
@@ -256,8 +264,8 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_grad(const float *__restrict__
         gb1 += __shfl_xor_sync(0xffffffffu, gb1, m);
       }
       if (g == 0) {
-        atomicAdd(&s.gsum[0][c0], gb0);
-        atomicAdd(&s.gsum[0][c0 + 1], gb1);
+        s.gsum[warp][0][c0] = gb0;
+        s.gsum[warp][0][c0 + 1] = gb1;
       }
       s.dz1[r0 + g][c0] = __float2bfloat16_rn(z0);
       s.dz1[r0 + g][c0 + 1] = __float2bfloat16_rn(z1);
@@ -301,34 +309,67 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_grad(const float *__restrict__
         mma16816(d, a, b);
       }
       const int row = mt * 16 + g, col = nt * 8 + 2 * t;
-      float *G = grad + (l2 ? OFF_W2 : OFF_W1);
+      float *G = gblk + (size_t)blockIdx.x * NPARAM + (l2 ? OFF_W2 : OFF_W1);
       const int ld = l2 ? NH : NF;
-      atomicAdd(&G[row * ld + col], d[0]);
-      atomicAdd(&G[row * ld + col + 1], d[1]);
-      atomicAdd(&G[(row + 8) * ld + col], d[2]);
-      atomicAdd(&G[(row + 8) * ld + col + 1], d[3]);
+      G[row * ld + col] = d[0];
+      G[row * ld + col + 1] = d[1];
+      G[(row + 8) * ld + col] = d[2];
+      G[(row + 8) * ld + col + 1] = d[3];
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < NH; i += blockDim.x) {
-    atomicAdd(&grad[OFF_B1 + i], s.gsum[0][i]);
-    atomicAdd(&grad[OFF_B2 + i], s.gsum[1][i]);
-    atomicAdd(&grad[OFF_W3 + i], s.gsum[2][i]);
+  // the bias and last-layer sums of the warps, in warp order
+  float *G = gblk + (size_t)blockIdx.x * NPARAM;
+  for (int i = threadIdx.x; i < 3 * NH; i += blockDim.x) {
+    const int q = i / NH, c = i - q * NH;
+    float v = 0.f;
+    for (int w = 0; w < WARPS; ++w) v += s.gsum[w][q][c];
+    G[(q == 0 ? OFF_B1 : (q == 1 ? OFF_B2 : OFF_W3)) + c] = v;
   }
   if (threadIdx.x == 0) {
-    atomicAdd(&grad[OFF_B3], s.gb3);
-    atomicAdd(loss, s.loss);
+    float b = 0.f;
+    double l = 0.;
+    for (int w = 0; w < WARPS; ++w) {
+      b += s.gb3[w];
+      l += s.loss[w];
+    }
+    G[OFF_B3] = b;
+    lblk[blockIdx.x] = l;
   }
 }
 
-// Adam step on the master parameters; zeroes the gradient accumulators.
-// Padding columns 11..15 of W1 stay zero.
-__global__ void k_mlp_adam(float *__restrict__ p, float *__restrict__ grad, float *__restrict__ m1,
-                           float *__restrict__ m2, float lr, float b1, float b2, float eps, float c1, float c2) {
+// sum of the nb block gradients, in block order: grad[i] = sum_b gblk[b][i];
+// loss += sum_b lblk[b]
+__device__ __forceinline__ float block_sum(const float *__restrict__ gblk, int nb, int i) {
+  float v = 0.f;
+  for (int b = 0; b < nb; ++b) v += gblk[(size_t)b * NPARAM + i];
+  return v;
+}
+__device__ __forceinline__ void loss_sum(const double *__restrict__ lblk, int nb, double *__restrict__ loss) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double l = 0.;
+    for (int b = 0; b < nb; ++b) l += lblk[b];
+    *loss += l;
+  }
+}
+
+__global__ void k_mlp_reduce(const float *__restrict__ gblk, const double *__restrict__ lblk, int nb,
+                             float *__restrict__ grad, double *__restrict__ loss) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  loss_sum(lblk, nb, loss);
+  if (i < NPARAM) grad[i] = block_sum(gblk, nb, i);
+}
+
+// Adam step on the master parameters with the gradient summed over the nb
+// blocks of k_mlp_grad (in block order); the batch's squared error is added
+// to loss.  Padding columns 11..15 of W1 stay zero.
+__global__ void k_mlp_adam(float *__restrict__ p, const float *__restrict__ gblk, const double *__restrict__ lblk,
+                           int nb, double *__restrict__ loss, float *__restrict__ m1, float *__restrict__ m2, float lr,
+                           float b1, float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  loss_sum(lblk, nb, loss);
   if (i >= NPARAM) return;
-  const float gr = grad[i];
-  grad[i] = 0.f;
+  const float gr = block_sum(gblk, nb, i);
   if (i < OFF_B1 && (i % NF) >= 11) return;
   const float a = b1 * m1[i] + (1.f - b1) * gr;
   const float b = b2 * m2[i] + (1.f - b2) * gr * gr;
@@ -454,6 +495,10 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
 // ---- host side state of the closure
 float *g_params = nullptr, *g_grad = nullptr, *g_m1 = nullptr, *g_m2 = nullptr;
 double *g_loss = nullptr;
+// per-block gradients and squared errors of k_mlp_grad (g_nblk blocks)
+float *g_gblk = nullptr;
+double *g_lblk = nullptr;
+int g_nblk = 0;
 int *g_used = nullptr;
 int g_adam_t = 0;
 char g_mlp_err[256];
@@ -483,6 +528,19 @@ int ensure_alloc() {
   MCK(cudaMemset(g_m2, 0, sizeof(float) * NPARAM));
   MCK(cudaMemset(g_used, 0, sizeof(int)));
   MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemTrain)));
+  return 0;
+}
+
+int ensure_blocks(int nb) {
+  if (nb <= g_nblk) return 0;
+  if (g_gblk) cudaFree(g_gblk);
+  if (g_lblk) cudaFree(g_lblk);
+  g_gblk = nullptr;
+  g_lblk = nullptr;
+  g_nblk = 0;
+  MCK(cudaMalloc(&g_gblk, sizeof(float) * NPARAM * (size_t)nb));
+  MCK(cudaMalloc(&g_lblk, sizeof(double) * (size_t)nb));
+  g_nblk = nb;
   return 0;
 }
 
@@ -543,16 +601,17 @@ int sbfs_mlp_get_params(float *host, int n) {
 // returns it to host `grad_out` (NPARAM floats) and the loss
 int sbfs_mlp_gradient(const void *X, const float *Y, const int *idx, int n, float *grad_out, double *loss_out) {
   if (ensure_alloc()) return 1;
-  MCK(cudaMemset(g_grad, 0, sizeof(float) * NPARAM));
+  const int nb = (n + TILE - 1) / TILE;
+  if (ensure_blocks(nb)) return 1;
   MCK(cudaMemset(g_loss, 0, sizeof(double)));
-  k_mlp_grad<<<(n + TILE - 1) / TILE, TILE * 2, sizeof(SmemTrain)>>>(
-      g_params, static_cast<const __nv_bfloat16 *>(X), Y, idx, n, g_grad, g_loss);
+  k_mlp_grad<<<nb, TILE * 2, sizeof(SmemTrain)>>>(g_params, static_cast<const __nv_bfloat16 *>(X), Y, idx, n, g_gblk,
+                                                   g_lblk);
+  k_mlp_reduce<<<(NPARAM + 255) / 256, 256>>>(g_gblk, g_lblk, nb, g_grad, g_loss);
   MCK(cudaGetLastError());
   MCK(cudaMemcpy(grad_out, g_grad, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost));
   double l = 0.;
   MCK(cudaMemcpy(&l, g_loss, sizeof(double), cudaMemcpyDeviceToHost));
   *loss_out = l / n;
-  MCK(cudaMemset(g_grad, 0, sizeof(float) * NPARAM));
   return 0;
 }
 
@@ -561,14 +620,17 @@ int sbfs_mlp_gradient(const void *X, const float *Y, const int *idx, int n, floa
 int sbfs_mlp_train_epoch(const void *X, const float *Y, const int *idx, int n, int batch, float lr,
                          double *mean_loss) {
   if (ensure_alloc()) return 1;
+  const int nb = (batch + TILE - 1) / TILE;
+  if (ensure_blocks(nb)) return 1;
   MCK(cudaMemset(g_loss, 0, sizeof(double)));
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   for (int off = 0; off + batch <= n; off += batch) {
-    k_mlp_grad<<<(batch + TILE - 1) / TILE, TILE * 2, sizeof(SmemTrain)>>>(
-        g_params, static_cast<const __nv_bfloat16 *>(X), Y, idx + off, batch, g_grad, g_loss);
+    k_mlp_grad<<<nb, TILE * 2, sizeof(SmemTrain)>>>(g_params, static_cast<const __nv_bfloat16 *>(X), Y, idx + off,
+                                                     batch, g_gblk, g_lblk);
     ++g_adam_t;
     const float c1 = 1.f / (1.f - powf(b1, (float)g_adam_t)), c2 = 1.f / (1.f - powf(b2, (float)g_adam_t));
-    k_mlp_adam<<<(NPARAM + 255) / 256, 256>>>(g_params, g_grad, g_m1, g_m2, lr, b1, b2, eps, c1, c2);
+    k_mlp_adam<<<(NPARAM + 255) / 256, 256>>>(g_params, g_gblk, g_lblk, nb, g_loss, g_m1, g_m2, lr, b1, b2, eps, c1,
+                                              c2);
   }
   MCK(cudaGetLastError());
   double l = 0.;

@@ -520,9 +520,16 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
     p, vof = st.interior_rows("p")[:, 1:-1], st.interior_rows("vof")[:, 1:-1]
     xc = (np.arange(n) + 0.5) / n
     X, Y = np.meshgrid(xc, xc)
-    d = np.hypot(X - 0.5, Y - 0.5)
-    p_in = p[(vof > 1 - 1e-6) & (d < 0.15)].mean()
-    p_out = p[(vof < 1e-6) & (d > 0.35)].mean()
+    # around the drop's own centre (it may drift under parasitic currents):
+    # its vof centroid, y periodic (mean direction on the circle)
+    w = vof / vof.sum()
+    cx = float((w * X).sum())
+    ang = 2 * np.pi * Y
+    cy = float(np.arctan2((w * np.sin(ang)).sum(), (w * np.cos(ang)).sum()) / (2 * np.pi)) % 1.0
+    dy = np.abs(Y - cy)
+    d = np.hypot(X - cx, np.minimum(dy, 1.0 - dy))
+    p_in = p[(vof > 0.99) & (d < 0.15)].mean()
+    p_out = p[(vof < 0.01) & (d > 0.35)].mean()
     exact = 1.0 / (wl.We * 0.25)
     umax = max(float(np.abs(ux).max()), float(np.abs(uy).max()))
     st_i, _, _ = interface_stencils(st.interior_rows("vof"))
