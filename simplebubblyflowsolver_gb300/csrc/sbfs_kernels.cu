@@ -314,29 +314,45 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
       up |= !neg(uy[ix(g, rp, I)]) ? 8u : 0u;
     }
   }
-  // warp-aggregated appends (a warp is 32 consecutive threads of the block,
-  // whatever its shape)
-  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+  // block-aggregated appends: per warp (32 consecutive threads of the block,
+  // whatever its shape) the ballots of its cells and faces, per block one
+  // atomic per list; the order of the entries is free (each is processed on
+  // its own)
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = (blockDim.x * blockDim.y + 31) >> 5;
   const int cell = (J - 1) * g.nx + (I - 1);
+  const unsigned below = (1u << lane) - 1u;
   const unsigned mask = __ballot_sync(0xffffffffu, itf);
-  if (mask) {
-    const int leader = __ffs(mask) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(count, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (itf) list[base + __popc(mask & ((1u << lane) - 1u))] = cell;
+  unsigned fm[4];
+  int nfw = 0;
 #pragma unroll
-    for (int f = 0; f < 4; ++f) {
-      const bool has = (up >> f) & 1u;
-      const unsigned fm = __ballot_sync(0xffffffffu, has);
-      if (fm) {
-        const int fl = __ffs(fm) - 1;
-        int fb = 0;
-        if (lane == fl) fb = atomicAdd(fcount, __popc(fm));
-        fb = __shfl_sync(0xffffffffu, fb, fl);
-        if (has) flist[fb + __popc(fm & ((1u << lane) - 1u))] = 4 * cell + f;
-      }
+  for (int f = 0; f < 4; ++f) {
+    fm[f] = __ballot_sync(0xffffffffu, (up >> f) & 1u);
+    nfw += __popc(fm[f]);
+  }
+  __shared__ int wofs[2][BX * BY / 32];  // per warp: its cell / face count, then its offset in the block
+  __shared__ int bbase[2];
+  if (lane == 0) {
+    wofs[0][warp] = __popc(mask);
+    wofs[1][warp] = nfw;
+  }
+  __syncthreads();
+  if (tid < 2) {
+    int run = 0;
+    for (int w = 0; w < nwarp; ++w) {
+      const int c = wofs[tid][w];
+      wofs[tid][w] = run;
+      run += c;
     }
+    bbase[tid] = run ? atomicAdd(tid == 0 ? count : fcount, run) : 0;
+  }
+  __syncthreads();
+  if (itf) list[bbase[0] + wofs[0][warp] + __popc(mask & below)] = cell;
+  int fo = bbase[1] + wofs[1][warp];
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    if ((up >> f) & 1u) flist[fo + __popc(fm[f] & below)] = 4 * cell + f;
+    fo += __popc(fm[f]);
   }
 }
 
