@@ -1380,10 +1380,10 @@ size_t tdm_stage_doubles(int nx, int ny, int nc, int G) {
 int tdm_group_index(int G) { return G == 4 ? 2 : (G == 2 ? 1 : 0); }
 // warps per tridiagonal system for a grid of nc cases: the fewest (1, 2, 4)
 // that put about 2048 warps in flight (13 per SM), as long as every lane
-// keeps at least 16 rows (with fewer, the cross-warp combine costs more than
-// the shorter recurrences save: the 256 x 128 bubble ran 4% faster with 1 or
-// 2 warps per system than with 4).  A rule of the grid, not a tuned choice:
-// it sets how the chunk maps are combined, and so the rounding of the solve.
+// keeps at least 4 rows (with 2, the cross-warp combine costs more than the
+// shorter recurrences save; 4 rows a lane beat 8 and 16 on every grid from
+// 256 x 128 to 1024 x 512).  A rule of the grid, not a tuned choice: it sets
+// how the chunk maps are combined, and so the rounding of the solve.
 int tdm_modes_per_block(const Tiles &t, int nx) {
   const int G = t.tdm_g > 0 ? t.tdm_g : 1;
   const int mb = t.tdm_mb > 0 ? t.tdm_mb : poisson_tdm_modes(nx);
@@ -1392,7 +1392,7 @@ int tdm_modes_per_block(const Tiles &t, int nx) {
 int tdm_warps_for(int nx, int ny, int nc) {
   const long systems = 4L * (ny / 4 + 1) * nc;
   int G = 1;
-  while (G < 4 && systems * G < 2048 && tdm_chunk(nx, 2 * G) >= 16) G *= 2;
+  while (G < 4 && systems * G < 2048 && tdm_chunk(nx, 2 * G) >= 4) G *= 2;
   return G;
 }
 

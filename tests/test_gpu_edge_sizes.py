@@ -49,7 +49,7 @@ CASES = [
     (64, 8, bubble, 10.0, 5),            # min ny
     (8192, 8, bubble, 10.0, 2),          # max nx: global staging, 4 warps, 64 rows a lane
     (37, 64, bubble, 10.0, 5),           # odd nx, ragged blocks of every shape
-    (200, 16, bubble, 10.0, 5),          # 7 rows a lane, 24 padding rows
+    (200, 16, bubble, 10.0, 5),          # 2 warps, 4 rows a lane, 56 padding rows
     (256, 512, square_cells, 10.0, 5),   # a tall domain, 129 wavenumber pairs
     (32, 4096, square_cells, 100.0, 5),  # two transform columns per block
     (32, 8192, square_cells, 100.0, 5),  # max ny: one transform column per block
