@@ -811,8 +811,9 @@ void enqueue_step(Ctx &c) {
 // columns per block of the Poisson transforms, wavenumbers per block of the
 // tridiagonal solves).  On the first step of a context it times each
 // candidate on the context's own state (saved before and put back after
-// every trial), two eager steps per candidate with CUDA events around every
-// launch, and keeps the fastest per kernel class.  Results do not depend on
+// every trial): the block shapes by two eager steps per candidate with CUDA
+// events around every launch, keeping the fastest per kernel class; then the
+// two Poisson choices by the time of whole steps.  Results do not depend on
 // the shapes.
 int g_autotune = 0;
 
@@ -834,7 +835,12 @@ int autotune(Ctx &c) {
       CK(cudaMemcpyAsync(live[q], save[q], n * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
     return 0;
   };
-  const unsigned short shapes[][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {32, 2}, {64, 2}, {16, 16}, {256, 1}};
+  // 256-thread blocks (whose warps are 32 x 1 cells, 16 x 2, 8 x 4 or 4 x 8)
+  // and smaller ones; an FP64 instruction costs a warp its issue slot however
+  // few lanes take it, so where a branch follows the interface, warps of
+  // compact patches are more often all in or all out of it
+  const unsigned short shapes[][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {32, 2}, {64, 2},
+                                      {16, 16}, {256, 1}, {8, 32}, {4, 64}};
   const int nshape = sizeof(shapes) / sizeof(shapes[0]);
   std::vector<int> fws;
   std::vector<std::pair<int, int>> tdms;  // (wavenumbers per block, warps per system)
@@ -848,7 +854,7 @@ int autotune(Ctx &c) {
   const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT,
                                -1, -1, -1, TK_CORRECT, -1, -1};
   Tiles best = c.b.tiles;
-  float best_ms[TK_COUNT], best_fft = 1e30f, best_tdm = 1e30f;
+  float best_ms[TK_COUNT];
   for (int k = 0; k < TK_COUNT; ++k) best_ms[k] = 1e30f;
   const Tiles keep = c.b.tiles;
   int rc = 0;
@@ -858,9 +864,6 @@ int autotune(Ctx &c) {
       cand.bx[k] = shapes[t][0];
       cand.by[k] = shapes[t][1];
     }
-    cand.fft_w = fws[t % fws.size()];
-    cand.tdm_mb = tdms[t % tdms.size()].first;
-    cand.tdm_g = tdms[t % tdms.size()].second;
     c.b.tiles = cand;
     if (restore()) {
       rc = 1;
@@ -890,16 +893,53 @@ int autotune(Ctx &c) {
         best.by[tk] = cand.by[tk];
       }
     }
-    const float fft = ms[KC_POISSON_FWD] + ms[KC_POISSON_INV];
-    if (fft < best_fft) {
-      best_fft = fft;
-      best.fft_w = cand.fft_w;
+  }
+  // second pass, on the chosen block shapes: the transform columns per block
+  // and the wavenumber pairs per tridiagonal block set how many blocks a
+  // Poisson launch has and so how its last wave fills the SMs, which events
+  // around every launch misjudge (they also stop the launches overlapping);
+  // each candidate is timed as three whole steps launched as a step runs
+  if (!rc) {
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) rc = 1;
+    auto step_ms = [&](const Tiles &cand, float *out) -> int {
+      c.b.tiles = cand;
+      if (restore()) return 1;
+      enqueue_step(c);  // warm-up
+      cudaEventRecord(t0, c.s);
+      for (int r = 0; r < 3; ++r) enqueue_step(c);
+      cudaEventRecord(t1, c.s);
+      if (sync(c)) return 1;
+      return cudaEventElapsedTime(out, t0, t1) == cudaSuccess ? 0 : 1;
+    };
+    float bms = 1e30f;
+    Tiles pick = best;
+    for (size_t i = 0; i < fws.size() && !rc; ++i) {
+      Tiles cand = best;
+      cand.fft_w = fws[i];
+      float ms = 0.f;
+      if (step_ms(cand, &ms)) rc = 1;
+      else if (ms < bms) {
+        bms = ms;
+        pick = cand;
+      }
     }
-    if (ms[KC_POISSON_TDM] < best_tdm) {
-      best_tdm = ms[KC_POISSON_TDM];
-      best.tdm_mb = cand.tdm_mb;
-      best.tdm_g = cand.tdm_g;
+    best = pick;
+    bms = 1e30f;
+    for (size_t i = 0; i < tdms.size() && !rc && tdms.size() > 1; ++i) {
+      Tiles cand = best;
+      cand.tdm_mb = tdms[i].first;
+      cand.tdm_g = tdms[i].second;
+      float ms = 0.f;
+      if (step_ms(cand, &ms)) rc = 1;
+      else if (ms < bms) {
+        bms = ms;
+        pick = cand;
+      }
     }
+    best = pick;
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
   }
   c.b.tiles = rc ? keep : best;
   const int rr = restore();

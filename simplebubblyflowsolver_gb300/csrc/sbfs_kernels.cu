@@ -1279,7 +1279,10 @@ __global__ void k_nr_check(const double *__restrict__ x, double *__restrict__ rc
   rsq[i] = rsqrt_nr(x[i]);
 }
 
-constexpr int kFftCols = 4;
+// columns per transform block before tuning: with 2, 256 threads and 32 KB
+// at ny = 1024, five blocks share an SM (40 warps); with 4, three (24 warps).
+// The 2048 x 1024 swarm stepped 3% faster and 1024 x 512 11% faster.
+constexpr int kFftCols = 2;
 // dynamic shared memory of k_poisson_tdm<false> (its static xch lies beside)
 constexpr size_t kTdmSmemMax = 227 * 1024 - 4096;
 
