@@ -64,39 +64,71 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, c
   const Phys ph = zphys(g, ph0);
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (I > g.nx + 1 || J > g.ny) return;
+  const bool in = I <= g.nx + 1 && J <= g.ny;
+  if (!GRAD && !in) return;  // with GRAD every thread meets the barriers below
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
-  const double v = vof[ix(g, r, I)];
-  if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.dm1, v, 1.), ph.den_lo, ph.den_hi);
-  if (VIS) {
-    // 1 + (visr - 1) 0.5 (a + b) = 1 + c2 (a + b), c2 = (visr - 1) / 2
-    const double c = ph.vm1, c2 = ph.hvm1;
-    if (I >= 1) {
-      double vis;
-      if (I == 1) vis = fma(c, vof[ix(g, r, 0)], 1.);
-      else if (I == g.nx + 1) vis = fma(c, v, 1.);
-      else vis = fma(c2, vof[ix(g, r, I - 1)] + v, 1.);
-      visux[ix(g, r, I - 1)] = clip_pos(vis, ph.vis_lo, ph.vis_hi);
+  const size_t q = g.p2 / 2;
+  bool need = false;  // the corner gradient is not identically zero
+  if (in) {
+    const double v = vof[ix(g, r, I)];
+    if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.dm1, v, 1.), ph.den_lo, ph.den_hi);
+    if (VIS) {
+      // 1 + (visr - 1) 0.5 (a + b) = 1 + c2 (a + b), c2 = (visr - 1) / 2
+      const double c = ph.vm1, c2 = ph.hvm1;
+      if (I >= 1) {
+        double vis;
+        if (I == 1) vis = fma(c, vof[ix(g, r, 0)], 1.);
+        else if (I == g.nx + 1) vis = fma(c, v, 1.);
+        else vis = fma(c2, vof[ix(g, r, I - 1)] + v, 1.);
+        visux[ix(g, r, I - 1)] = clip_pos(vis, ph.vis_lo, ph.vis_hi);
+      }
+      visuy[ix(g, r, I)] = clip_pos(fma(c2, vof[ix(g, rm, I)] + v, 1.), ph.vis_lo, ph.vis_hi);
     }
-    visuy[ix(g, r, I)] = clip_pos(fma(c2, vof[ix(g, rm, I)] + v, 1.), ph.vis_lo, ph.vis_hi);
+    if (GRAD && I >= 1) {
+      // corner at x face I between rows J-1 and J: zero where the four
+      // values are bitwise equal (single-phase bulk)
+      const double a = vof[ix(g, rm, I - 1)], b = vof[ix(g, rm, I)], c = vof[ix(g, r, I - 1)];
+      need = !(same(a, b) && same(b, c) && same(c, v));
+      if (!need) reinterpret_cast<double2 *>(dvof)[(size_t)r * q + (I - 1)] = make_double2(0., 0.);
+    }
   }
-  if (GRAD && I >= 1) {
-    // corner at x face I between rows J-1 and J
-    const double a = vof[ix(g, rm, I - 1)], b = vof[ix(g, rm, I)];
-    const double c = vof[ix(g, r, I - 1)], d = v;
-    double2 out = make_double2(0., 0.);
-    if (!(same(a, b) && same(b, c) && same(c, d))) {
+  if (GRAD) {
+    // the other corners are compacted to the block's first threads, so that
+    // their ~16 FP64 operations fill whole warps: an FP64 instruction costs
+    // a warp its issue slot however few of its lanes run it, and the corners
+    // with a gradient lie along the interface and its THINC tails
+    __shared__ int cnt[BX * BY / 32];
+    __shared__ int list[BX * BY];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = (blockDim.x * blockDim.y + 31) >> 5;
+    const unsigned mask = __ballot_sync(0xffffffffu, need);
+    if (lane == 0) cnt[warp] = __popc(mask);
+    __syncthreads();
+    int off = 0, n = 0;
+    for (int w = 0; w < nwarp; ++w) {
+      const int c = cnt[w];
+      off += w < warp ? c : 0;
+      n += c;
+    }
+    if (need) list[off + __popc(mask & ((1u << lane) - 1u))] = tid;
+    __syncthreads();
+    if (tid < n) {
+      const int src = list[tid];
+      const int sy = src / blockDim.x, sx = src - sy * blockDim.x;
+      const int Ic = blockIdx.x * blockDim.x + sx, Jc = blockIdx.y * blockDim.y + sy + 1;
+      const int rc = Jc - 1 + zr, rmc = wrap(Jc - 1, g.ny) + zr;
+      const double a = vof[ix(g, rmc, Ic - 1)], b = vof[ix(g, rmc, Ic)];
+      const double c = vof[ix(g, rc, Ic - 1)], d = vof[ix(g, rc, Ic)];
       // the reference's summation order, kept on purpose: in the THINC
       // tails the four values differ by ~1e-16 and the reference's sum is
       // rounding noise that the normalisation below (by max(|g|, eps))
       // scales up to O(1); another order gives O(1) different corner normals
-      const double gx = m.ihxxf[I] * (((-a + b) - c) + d);
+      const double gx = m.ihxxf[Ic] * (((-a + b) - c) + d);
       const double gy = g.ihy * (((-a - b) + c) + d);
       const double inv = inv_norm(fma(gx, gx, gy * gy));
-      out = make_double2(gx * inv, gy * inv);
+      reinterpret_cast<double2 *>(dvof)[(size_t)rc * q + (Ic - 1)] = make_double2(gx * inv, gy * inv);
     }
-    reinterpret_cast<double2 *>(dvof)[(size_t)r * (g.p2 / 2) + (I - 1)] = out;
   }
 }
 
