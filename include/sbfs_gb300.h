@@ -101,6 +101,12 @@ int sbfs_set_use_graphs(int on);
  * finishes, and wait on the GPU for its results.  Same results either way. */
 int sbfs_set_pdl(int on);
 
+/* interface-branch compaction (the corner-gradient and curvature work handed
+ * to the first threads of each block, so that it fills whole warps): -1 (the
+ * default) as the autotuner chose, else 0 off or 1 on for every context.
+ * Same results either way, bit for bit. */
+int sbfs_set_compaction(int mode);
+
 /* In SBFS_SYNC_STATE mode, let the step copy the state itself (default 1):
  * when the GPU can address the caller's arrays (pageable host memory on a
  * system with host page-table access, such as Grace-Blackwell, or arrays
@@ -235,8 +241,9 @@ int sbfs_set_autotune(int on);
 /* shapes in use (group -1: the single-case context): bx[7], by[7] for
  * props, curvature list, flux/force, vof advance, stress, predict,
  * correct; the Poisson transform width, wavenumbers per tridiagonal block
- * and warps per tridiagonal system */
-int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps);
+ * and warps per tridiagonal system; compact (may be NULL): 1 when the
+ * corner-gradient and curvature work is compacted within blocks */
+int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps, int *compact);
 /* number of grid groups and cases per group of the current batch */
 int sbfs_batch_groups(int *ngroups, int *cases_per_group);
 int sbfs_batch_release(void);

@@ -81,6 +81,10 @@ class GpuLibrary(ReferenceAPI):
         """launch the step's kernels with programmatic dependent launch"""
         self._ext("sbfs_set_pdl", 1 if on else 0)
 
+    def set_compaction(self, mode: int):
+        """interface-branch compaction: -1 as tuned (default), 0 off, 1 on"""
+        self._ext("sbfs_set_compaction", int(mode))
+
     def set_host_link(self, on):
         """strict-mode steps copy the state in and out themselves, overlapped
         with their kernels, when the GPU can address the host arrays (True or
@@ -231,14 +235,16 @@ class GpuLibrary(ReferenceAPI):
         fw = C.c_int(0)
         mb = C.c_int(0)
         gw = C.c_int(0)
+        cm = C.c_int(0)
         self.lib.sbfs_tiles.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                        C.POINTER(C.c_int), C.POINTER(C.c_int)]
-        self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb), C.byref(gw))
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb), C.byref(gw), C.byref(cm))
         names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_stress", "k_predict", "k_correct"]
         out = {n: f"{bx[k]}x{by[k]}" for k, n in enumerate(names)}
         out["fft_cols"] = fw.value
         out["tdm_modes"] = mb.value
         out["tdm_warps"] = gw.value
+        out["compact"] = cm.value
         return out
 
     def batch_groups(self):

@@ -898,16 +898,21 @@ int autotune(Ctx &c) {
   // and the wavenumber pairs per tridiagonal block set how many blocks a
   // Poisson launch has and so how its last wave fills the SMs, which events
   // around every launch misjudge (they also stop the launches overlapping);
-  // each candidate is timed as three whole steps launched as a step runs
+  // the interface-branch compaction saves FP64 issue slots on large grids
+  // but lengthens the kernels' critical path, which small grids feel.  Each
+  // candidate is timed as whole steps launched as a step runs: three, or as
+  // many as take about 8 M cell-steps on small grids (up to 40)
   if (!rc) {
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) rc = 1;
+    const double cells = (double)c.nx * c.ny * c.nc;
+    const int nsteps = (int)std::min(40., std::max(3., std::ceil(8e6 / cells)));
     auto step_ms = [&](const Tiles &cand, float *out) -> int {
       c.b.tiles = cand;
       if (restore()) return 1;
       enqueue_step(c);  // warm-up
       cudaEventRecord(t0, c.s);
-      for (int r = 0; r < 3; ++r) enqueue_step(c);
+      for (int r = 0; r < nsteps; ++r) enqueue_step(c);
       cudaEventRecord(t1, c.s);
       if (sync(c)) return 1;
       return cudaEventElapsedTime(out, t0, t1) == cudaSuccess ? 0 : 1;
@@ -938,6 +943,18 @@ int autotune(Ctx &c) {
       }
     }
     best = pick;
+    bms = 1e30f;
+    for (int cm = 1; cm >= 0 && !rc; --cm) {
+      Tiles cand = best;
+      cand.compact = cm;
+      float ms = 0.f;
+      if (step_ms(cand, &ms)) rc = 1;
+      else if (ms < bms) {
+        bms = ms;
+        pick = cand;
+      }
+    }
+    best = pick;
     if (t0) cudaEventDestroy(t0);
     if (t1) cudaEventDestroy(t1);
   }
@@ -955,7 +972,7 @@ int autotune(Ctx &c) {
 
 int role_key(const Ctx &c) {
   return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
-         (g_pdl << 6);
+         (g_pdl << 6) | ((g_compact + 1) << 7);
 }
 
 int launch_step(Ctx &c) {
@@ -1255,6 +1272,12 @@ const char *sbfs_last_error(void) { return g_err.c_str(); }
 
 int sbfs_set_pdl(int on) {
   g_pdl = on ? 1 : 0;
+  return 0;
+}
+
+int sbfs_set_compaction(int mode) {
+  if (mode < -1 || mode > 1) return fail("bad compaction mode %d", mode);
+  g_compact = mode;
   return 0;
 }
 
@@ -1704,7 +1727,7 @@ int sbfs_set_autotune(int on) {
 }
 
 // launch shapes in use: group -1 = the single-case context, else batch group
-int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps) {
+int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps, int *compact) {
   Ctx *c = nullptr;
   if (group < 0)
     c = g_ctx.get();
@@ -1718,6 +1741,7 @@ int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_wa
   *fft_w = c->b.tiles.fft_w;
   *tdm_mb = tdm_modes_per_block(c->b.tiles, c->nx);
   *tdm_warps = c->b.tiles.tdm_g > 0 ? c->b.tiles.tdm_g : 1;
+  if (compact) *compact = c->b.tiles.compact;
   return 0;
 }
 

@@ -28,6 +28,7 @@
 namespace sbfs {
 
 int g_pdl = 1;  // step kernels launched with programmatic stream serialisation
+int g_compact = -1;
 
 namespace {
 
@@ -41,6 +42,31 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+// Interface-branch compaction.  An FP64 instruction costs its warp an issue
+// slot however few of its lanes run it (measured: eight FMA chains on 1 to
+// 32 lanes of every warp all took the same time), and the cells that need
+// the FP64 work of an interface branch lie along the interface and its THINC
+// tails, often a few to a warp.  block_compact lists the block's threads
+// whose flag is set in list[0 .. n) in thread order (a ballot per warp, a
+// prefix over the warp counts in shared memory) and returns n, so that
+// threads 0 .. n-1 can each take one listed cell and fill whole warps.
+// Every thread of the block must call it (two barriers).
+__device__ __forceinline__ int block_compact(bool flag, int tid, int *cnt, int *list) {
+  const int lane = tid & 31, warp = tid >> 5, nwarp = (blockDim.x * blockDim.y + 31) >> 5;
+  const unsigned mask = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) cnt[warp] = __popc(mask);
+  __syncthreads();
+  int off = 0, n = 0;
+  for (int w = 0; w < nwarp; ++w) {
+    const int c = cnt[w];
+    off += w < warp ? c : 0;
+    n += c;
+  }
+  if (flag) list[off + __popc(mask & ((1u << lane) - 1u))] = tid;
+  __syncthreads();
+  return n;
+}
 
 dim3 grid2d(int ni, int nj, int nz = 1) { return dim3((ni + BX - 1) / BX, (nj + BY - 1) / BY, nz); }
 // grid of the block shape of kernel k
@@ -56,19 +82,40 @@ dim3 tile_grid(const Tiles &t, int k, int ni, int nj, int nz) {
 //   dvof:  src/interface/curvature_tensor.c:16-49
 // thread (I, J): I = 0..nx+1
 // ---------------------------------------------------------------------------
+// unit normal of the vof gradient at the corner between columns I-1, I and
+// rows J-1, J of a case (curvature_tensor.c:16-49)
+__device__ __forceinline__ void corner_normal(const Grid &g, const Metrics &m, const double *__restrict__ vof,
+                                              double *__restrict__ dvof, int zr, int I, int J) {
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
+  const double a = vof[ix(g, rm, I - 1)], b = vof[ix(g, rm, I)];
+  const double c = vof[ix(g, r, I - 1)], d = vof[ix(g, r, I)];
+  // the reference's summation order, kept on purpose: in the THINC tails the
+  // four values differ by ~1e-16 and the reference's sum is rounding noise
+  // that the normalisation below (by max(|g|, eps)) scales up to O(1);
+  // another order gives O(1) different corner normals
+  const double gx = m.ihxxf[I] * (((-a + b) - c) + d);
+  const double gy = g.ihy * (((-a - b) + c) + d);
+  const double inv = inv_norm(fma(gx, gx, gy * gy));
+  reinterpret_cast<double2 *>(dvof)[(size_t)r * (g.p2 / 2) + (I - 1)] = make_double2(gx * inv, gy * inv);
+}
+
+// compact: the corners with a gradient are handed to the block's first
+// threads (see the interface-branch compaction below); otherwise each thread
+// does its own.  The same arithmetic either way.
 template <bool DEN, bool VIS, bool GRAD>
 __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, const double *__restrict__ vof,
                                                   double *__restrict__ den, double *__restrict__ visux,
-                                                  double *__restrict__ visuy, double *__restrict__ dvof) {
+                                                  double *__restrict__ visuy, double *__restrict__ dvof,
+                                                  int compact) {
   pdl_entry();
   const Phys ph = zphys(g, ph0);
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const bool in = I <= g.nx + 1 && J <= g.ny;
-  if (!GRAD && !in) return;  // with GRAD every thread meets the barriers below
+  const bool cmp = GRAD && compact;  // uniform over the block
+  if (!cmp && !in) return;  // when compacting, every thread meets the barriers below
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
-  const size_t q = g.p2 / 2;
   bool need = false;  // the corner gradient is not identically zero
   if (in) {
     const double v = vof[ix(g, r, I)];
@@ -86,48 +133,21 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, c
       visuy[ix(g, r, I)] = clip_pos(fma(c2, vof[ix(g, rm, I)] + v, 1.), ph.vis_lo, ph.vis_hi);
     }
     if (GRAD && I >= 1) {
-      // corner at x face I between rows J-1 and J: zero where the four
-      // values are bitwise equal (single-phase bulk)
+      // zero where the four values are bitwise equal (single-phase bulk)
       const double a = vof[ix(g, rm, I - 1)], b = vof[ix(g, rm, I)], c = vof[ix(g, r, I - 1)];
       need = !(same(a, b) && same(b, c) && same(c, v));
-      if (!need) reinterpret_cast<double2 *>(dvof)[(size_t)r * q + (I - 1)] = make_double2(0., 0.);
+      if (!need) reinterpret_cast<double2 *>(dvof)[(size_t)r * (g.p2 / 2) + (I - 1)] = make_double2(0., 0.);
+      else if (!cmp) corner_normal(g, m, vof, dvof, zr, I, J);
     }
   }
-  if (GRAD) {
-    // the other corners are compacted to the block's first threads, so that
-    // their ~16 FP64 operations fill whole warps: an FP64 instruction costs
-    // a warp its issue slot however few of its lanes run it, and the corners
-    // with a gradient lie along the interface and its THINC tails
+  if (cmp) {
     __shared__ int cnt[BX * BY / 32];
     __shared__ int list[BX * BY];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5, nwarp = (blockDim.x * blockDim.y + 31) >> 5;
-    const unsigned mask = __ballot_sync(0xffffffffu, need);
-    if (lane == 0) cnt[warp] = __popc(mask);
-    __syncthreads();
-    int off = 0, n = 0;
-    for (int w = 0; w < nwarp; ++w) {
-      const int c = cnt[w];
-      off += w < warp ? c : 0;
-      n += c;
-    }
-    if (need) list[off + __popc(mask & ((1u << lane) - 1u))] = tid;
-    __syncthreads();
+    const int n = block_compact(need, tid, cnt, list);
     if (tid < n) {
-      const int src = list[tid];
-      const int sy = src / blockDim.x, sx = src - sy * blockDim.x;
-      const int Ic = blockIdx.x * blockDim.x + sx, Jc = blockIdx.y * blockDim.y + sy + 1;
-      const int rc = Jc - 1 + zr, rmc = wrap(Jc - 1, g.ny) + zr;
-      const double a = vof[ix(g, rmc, Ic - 1)], b = vof[ix(g, rmc, Ic)];
-      const double c = vof[ix(g, rc, Ic - 1)], d = vof[ix(g, rc, Ic)];
-      // the reference's summation order, kept on purpose: in the THINC
-      // tails the four values differ by ~1e-16 and the reference's sum is
-      // rounding noise that the normalisation below (by max(|g|, eps))
-      // scales up to O(1); another order gives O(1) different corner normals
-      const double gx = m.ihxxf[Ic] * (((-a + b) - c) + d);
-      const double gy = g.ihy * (((-a - b) + c) + d);
-      const double inv = inv_norm(fma(gx, gx, gy * gy));
-      reinterpret_cast<double2 *>(dvof)[(size_t)rc * q + (Ic - 1)] = make_double2(gx * inv, gy * inv);
+      const int sy = list[tid] / blockDim.x, sx = list[tid] - sy * blockDim.x;
+      corner_normal(g, m, vof, dvof, zr, blockIdx.x * blockDim.x + sx, blockIdx.y * blockDim.y + sy + 1);
     }
   }
 }
@@ -306,11 +326,27 @@ __global__ void __launch_bounds__(BX *BY)
 // Each face is written by exactly one of them: the upwind choice and the
 // vofmin test are the same integer tests in both.
 // ---------------------------------------------------------------------------
+// kappa = -div n of cell (I, J) of a case from its four corner normals
+// (curvature_tensor.c:100-135)
+__device__ __forceinline__ void cell_curv(const Grid &g, const Metrics &m, const double2 *__restrict__ dv,
+                                          double *__restrict__ curv, int zr, int I, int J) {
+  const size_t q = g.p2 / 2;
+  const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
+  const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
+  const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
+  const double ddx = (d10.x + d11.x) - (d00.x + d01.x);
+  const double ddy = (d01.y + d11.y) - (d00.y + d10.y);
+  curv[ix(g, r, I)] = -fma(m.hihxxc[I], ddx, g.hihy * ddy);
+}
+
+// compact: the cells with a corner normal hand their curvature to the
+// block's first threads (interface-branch compaction); otherwise each thread
+// computes its own.  The same arithmetic either way.
 __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const double *__restrict__ vof,
                                                       const double *__restrict__ dvof, const double *__restrict__ ux,
                                                       const double *__restrict__ uy, double *__restrict__ curv,
                                                       int *__restrict__ list, int *__restrict__ count,
-                                                      int *__restrict__ flist, int *__restrict__ fcount) {
+                                                      int *__restrict__ flist, int *__restrict__ fcount, int compact) {
   pdl_entry();
   list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
   count += (size_t)blockIdx.z * (1);
@@ -319,24 +355,20 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const bool in = I <= g.nx && J <= g.ny;
-  bool itf = false;
+  const int zr = blockIdx.z * g.ny;
+  const double2 *dv = reinterpret_cast<const double2 *>(dvof);
+  const size_t q = g.p2 / 2;
+  bool itf = false, kap = false;  // kap: some corner normal of the cell is not +-0
   unsigned up = 0u;  // faces this cell is upwind of: bit 0 left, 1 right, 2 bottom, 3 top
   if (in) {
-    const int zr = blockIdx.z * g.ny;
     const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
-    const double2 *dv = reinterpret_cast<const double2 *>(dvof);
-    const size_t q = g.p2 / 2;
     const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
     const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
     const long long any = dbits(d00.x) | dbits(d00.y) | dbits(d10.x) | dbits(d10.y) | dbits(d01.x) | dbits(d01.y) |
                           dbits(d11.x) | dbits(d11.y);
-    double k = -0.;
-    if ((any << 1) != 0) {
-      const double ddx = (d10.x + d11.x) - (d00.x + d01.x);
-      const double ddy = (d01.y + d11.y) - (d00.y + d10.y);
-      k = -fma(m.hihxxc[I], ddx, g.hihy * ddy);
-    }
-    curv[ix(g, r, I)] = k;
+    kap = (any << 1) != 0;
+    if (!kap) curv[ix(g, r, I)] = -0.;
+    else if (!compact) cell_curv(g, m, dv, curv, zr, I, J);
     itf = !single_phase(vof[ix(g, r, I)]);
     if (itf) {
       // upwind tests of update/fluxx.c, fluxy.c; the wall faces belong to k_flux_force
@@ -354,6 +386,7 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
   const int lane = tid & 31, warp = tid >> 5, nwarp = (blockDim.x * blockDim.y + 31) >> 5;
   const int cell = (J - 1) * g.nx + (I - 1);
   const unsigned below = (1u << lane) - 1u;
+  const unsigned kmask = __ballot_sync(0xffffffffu, kap);
   const unsigned mask = __ballot_sync(0xffffffffu, itf);
   unsigned fm[4];
   int nfw = 0;
@@ -362,21 +395,25 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
     fm[f] = __ballot_sync(0xffffffffu, (up >> f) & 1u);
     nfw += __popc(fm[f]);
   }
-  __shared__ int wofs[2][BX * BY / 32];  // per warp: its cell / face count, then its offset in the block
-  __shared__ int bbase[2];
+  // per warp: its interface cell / face / curvature cell count, then its
+  // offset in the block (lists) or among the block's curvature cells
+  __shared__ int wofs[3][BX * BY / 32];
+  __shared__ int bbase[3];
+  __shared__ int klist[BX * BY];
   if (lane == 0) {
     wofs[0][warp] = __popc(mask);
     wofs[1][warp] = nfw;
+    wofs[2][warp] = __popc(kmask);
   }
   __syncthreads();
-  if (tid < 2) {
+  if (tid < 3) {
     int run = 0;
     for (int w = 0; w < nwarp; ++w) {
       const int c = wofs[tid][w];
       wofs[tid][w] = run;
       run += c;
     }
-    bbase[tid] = run ? atomicAdd(tid == 0 ? count : fcount, run) : 0;
+    bbase[tid] = tid == 2 ? run : (run ? atomicAdd(tid == 0 ? count : fcount, run) : 0);
   }
   __syncthreads();
   if (itf) list[bbase[0] + wofs[0][warp] + __popc(mask & below)] = cell;
@@ -385,6 +422,16 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
   for (int f = 0; f < 4; ++f) {
     if ((up >> f) & 1u) flist[fo + __popc(fm[f] & below)] = 4 * cell + f;
     fo += __popc(fm[f]);
+  }
+  // compacted curvature: the cells with a corner normal lie in the THINC
+  // tails, often a few to a warp (the prefix of their counts came with the
+  // lists' above)
+  if (!compact) return;  // uniform over the block
+  if (kap) klist[wofs[2][warp] + __popc(kmask & below)] = tid;
+  __syncthreads();
+  if (tid < bbase[2]) {
+    const int sy = klist[tid] / blockDim.x, sx = klist[tid] - sy * blockDim.x;
+    cell_curv(g, m, dv, curv, zr, blockIdx.x * blockDim.x + sx + 1, blockIdx.y * blockDim.y + sy + 1);
   }
 }
 
@@ -1386,6 +1433,8 @@ int poisson_fft_cols(int ny) {
 size_t poisson_fft_smem(int ny, int w) { return sizeof(double2) * 2 * w * (size_t)(ny / 2); }
 bool fft_w_fits(int ny, int w) { return poisson_fft_smem(ny, w) <= 227 * 1024; }
 
+int compaction(const Tiles &t) { return g_compact >= 0 ? g_compact : t.compact; }
+
 Tiles default_tiles(int ny) {
   Tiles t{};
   for (int k = 0; k < TK_COUNT; ++k) {
@@ -1395,6 +1444,7 @@ Tiles default_tiles(int ny) {
   t.fft_w = poisson_fft_cols(ny);
   t.tdm_mb = 0;
   t.tdm_g = 1;
+  t.compact = 1;
   return t;
 }
 int tdm_chunk(int nx, int G) { return (nx + 32 * G - 1) / (32 * G); }
@@ -1458,15 +1508,20 @@ void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &p
                   bool grad, double *den_out) {
   const dim3 gr = tile_grid(b.tiles, TK_PROPS, g.nx + 2, g.ny, g.nc), bl = tile_block(b.tiles, TK_PROPS);
   if (den && vis && grad)
-    launch_pdl(k_props<true, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<true, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
+               compaction(b.tiles));
   else if (vis && grad)
-    launch_pdl(k_props<false, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<false, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
+               compaction(b.tiles));
   else if (den)
-    launch_pdl(k_props<true, false, false>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<true, false, false>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
+               compaction(b.tiles));
   else if (vis)
-    launch_pdl(k_props<false, true, false>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<false, true, false>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
+               compaction(b.tiles));
   else if (grad)
-    launch_pdl(k_props<false, false, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof);
+    launch_pdl(k_props<false, false, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
+               compaction(b.tiles));
 }
 
 void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv,
@@ -1505,7 +1560,7 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
   if (stage == 0) {
     cudaMemsetAsync(b.icount, 0, sizeof(int) * 2 * g.nc, s);  // cell and face counts
     launch_pdl(k_curv_list, tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s,
-        g, m, b.vof, b.dvof, ux, uy, b.curv, b.ilist, b.icount, b.flist, b.fcount);
+        g, m, b.vof, b.dvof, ux, uy, b.curv, b.ilist, b.icount, b.flist, b.fcount, compaction(b.tiles));
   } else if (stage == 1) {
     launch_pdl(k_interface_cells, dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s,
         g, m, ux, uy, b.vof, b.dvof, b.flist, b.fcount, b.fluxx, b.fluxy);

@@ -17,6 +17,8 @@ struct Tiles {
   int tdm_mb;  // wavenumbers per block of the tridiagonal solves (0: by size)
   int tdm_g;   // warps per tridiagonal system: 1, 2 or 4 (tdm_g * tdm_mb <= 4), set by
                // tdm_warps_for from the grid (it changes the rounding, so it is not tuned)
+  int compact;  // 1: the FP64 work of the corner-gradient and curvature branches is
+                // compacted to the first threads of each block; 0: done in place
 };
 Tiles default_tiles(int ny);
 
@@ -108,6 +110,7 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
 // kernel begins with pdl_entry, which waits for it); g_pdl = 0 launches
 // them plainly
 extern int g_pdl;
+extern int g_compact;  // -1: per context (Tiles::compact), else 0 / 1 for all
 template <typename... P, typename... A>
 void launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A &&...a) {
   cudaLaunchAttribute at[1];

@@ -180,6 +180,29 @@ def test_graphs_follow_physics_changes(libs):
     assert max(errs.values()) <= 1e-10, errs
 
 
+@pytest.mark.parametrize("name", ["single_bubble", "swarm"])
+def test_compaction_gives_identical_steps(libs, name):
+    """the interface-branch compaction hands the corner-gradient and
+    curvature work to other threads of the block, with the same arithmetic:
+    the steps stay bit for bit"""
+    gpu, orc = libs
+    wl = ic.single_bubble(256, 128) if name == "single_bubble" else ic.bubble_swarm(512, 256, nbubbles=12, seed=3)
+    st0 = prepare(libs, wl)
+    runs = {}
+    try:
+        for mode in (0, 1):
+            gpu.release()
+            gpu.set_compaction(mode)
+            st = clone(st0)
+            runs[mode] = ([gpu.integrate(st) for _ in range(4)], st)
+    finally:
+        gpu.set_compaction(-1)
+        gpu.release()
+    assert runs[0][0] == runs[1][0]
+    for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+        assert np.array_equal(runs[0][1].field(s), runs[1][1].field(s)), s
+
+
 def test_autotuned_shapes_give_identical_steps(libs):
     """the autotuner changes launch shapes only: the steps stay bit for bit"""
     gpu, orc = libs
