@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(BX *BY)
 // warps wait on a few lanes.  So:
 //   k_curv_list       curvature of every cell (curvature_tensor.c:100-135),
 //                     a list of the interface cells and a list of the faces
-//                     they are upwind of (warp-aggregated appends)
+//                     they are upwind of (block-aggregated appends)
 //   k_interface_cells one thread per listed face: the cell's normal and
 //                     K = 1/phi - 1 (curvature_tensor.c:51-97), then the THINC
 //                     flux of that face (update/fluxx.c, fluxy.c); a cell
