@@ -407,10 +407,24 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_predict(const float *__restric
   }
 }
 
+// 0 <= v <= 1 and lo <= v <= hi (0 < lo < hi) as integer tests on the bit
+// pattern, the same answers as the FP64 comparisons (-0 counts as 0, NaN as
+// out of range) without their FP64 instructions
+__device__ __forceinline__ bool in_unit(double v) {
+  const long long b = __double_as_longlong(v);
+  return (b >= 0 && b <= 0x3FF0000000000000LL) || b == (long long)0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool in_pos_range(double v, double lo, double hi) {
+  const long long b = __double_as_longlong(v);
+  return b >= __double_as_longlong(lo) && b <= __double_as_longlong(hi);
+}
+
 // In the fused step: curvature of the listed interface cells from the
 // network when the stencil is inside the training distribution (centre vof in
 // [0.01, 0.99], all stencil values in [0, 1], |kappa dx| in [lo, hi]); the
-// plain curvature already in `curv` stays otherwise.  Square cells.
+// plain curvature already in `curv` stays otherwise.  Square cells.  Every
+// lane of a warp builds one feature row (32 rows, two 16-row MMA tiles), so
+// the FP64 work of the gather fills whole warps.
 __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__restrict__ params,
                                                       const double *__restrict__ vof, const double *__restrict__ dvof,
                                                       const int *__restrict__ list, const int *__restrict__ count,
@@ -419,7 +433,7 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
   pdl_entry();
   extern __shared__ unsigned char smraw[];
   SmemW &w = *reinterpret_cast<SmemW *>(smraw);
-  __nv_bfloat16(*xs)[16][NF] = reinterpret_cast<__nv_bfloat16(*)[16][NF]>(smraw + sizeof(SmemW));
+  __nv_bfloat16(*xs)[32][NF] = reinterpret_cast<__nv_bfloat16(*)[32][NF]>(smraw + sizeof(SmemW));
   load_weights(w, params);
   __syncthreads();
   // batches: case blockIdx.z has its own list and rows z ny .. z ny + ny - 1
@@ -432,11 +446,10 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
   const size_t q = g.p2 / 2;
   int nused = 0;
-  for (int e0 = (blockIdx.x * nwarps + warp) * 16; e0 < n; e0 += gridDim.x * nwarps * 16) {
-    // lanes 0..15 build one feature row each
+  for (int e0 = (blockIdx.x * nwarps + warp) * 32; e0 < n; e0 += gridDim.x * nwarps * 32) {
     bool ok = false;
     int cell = -1;
-    if (lane < 16) {
+    {
       const int e = e0 + lane;
       float fr[NF];
       for (int c = 0; c < NF; ++c) fr[c] = 0.f;
@@ -449,12 +462,11 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
           const int rr = wrap(J + dy, g.ny) + zr;
           for (int dx = -1; dx <= 1; ++dx) {
             const double v = vof[(size_t)rr * g.p1 + I + dx];
-            ok = ok && v >= 0. && v <= 1.;
+            ok = ok && in_unit(v);
             fr[(dy + 1) * 3 + (dx + 1)] = (float)v;
           }
         }
-        const double phi = vof[(size_t)r * g.p1 + I];
-        ok = ok && phi >= 0.01 && phi <= 0.99;
+        ok = ok && in_pos_range(vof[(size_t)r * g.p1 + I], 0.01, 0.99);
         // the solver's cell normal: sum of the four unit corner normals, normalised
         const int rp = wrap(J + 1, g.ny) + zr;
         const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
@@ -467,15 +479,20 @@ __global__ void __launch_bounds__(TILE * 2) k_mlp_curv(Grid g, const float *__re
       for (int c = 0; c < NF; ++c) xs[warp][lane][c] = __float2bfloat16_rn(fr[c]);
     }
     __syncwarp();
-    uint32_t xa[4];
-    load_x_frag(&xs[warp][0][0], xa);
-    Fwd f;
-    forward16(w, xa, f);
-    // rows gq and gq + 8 come out in lanes 4 gq .. 4 gq + 3; lane L < 16 takes row L
-    const float oa = __shfl_sync(0xffffffffu, f.out0, (lane & 7) * 4);
-    const float ob = __shfl_sync(0xffffffffu, f.out1, (lane & 7) * 4);
-    const float o = (lane & 8) ? ob : oa;
-    if (lane < 16 && ok) {
+    // tile h holds rows 16 h .. 16 h + 15; their outputs come out in lanes
+    // 4 gq .. 4 gq + 3 (rows gq and gq + 8); lane L takes row L
+    float o = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint32_t xa[4];
+      load_x_frag(&xs[warp][16 * h][0], xa);
+      Fwd f;
+      forward16(w, xa, f);
+      const float oa = __shfl_sync(0xffffffffu, f.out0, (lane & 7) * 4);
+      const float ob = __shfl_sync(0xffffffffu, f.out1, (lane & 7) * 4);
+      if ((lane >> 4) == h) o = (lane & 8) ? ob : oa;
+    }
+    if (ok) {
       const float a = fabsf(o);
       if (a >= lo && a <= hi) {
         const int rc = cell / g.nx, I = cell - rc * g.nx + 1;
@@ -544,7 +561,8 @@ int ensure_blocks(int nb) {
   return 0;
 }
 
-size_t smem_infer() { return sizeof(SmemW) + sizeof(__nv_bfloat16) * 8 * 16 * NF; }
+// weights and per warp (8 warps) up to 32 feature rows
+size_t smem_infer() { return sizeof(SmemW) + sizeof(__nv_bfloat16) * 8 * 32 * NF; }
 
 }  // namespace
 
