@@ -177,3 +177,26 @@ def test_autotuned_batch_equals_default(libs):
     for k, (x, y) in enumerate(zip(a, b)):
         for s in ("ux", "uy", "p", "vof"):
             assert np.array_equal(x.field(s), y.field(s)), (k, s)
+
+
+@pytest.mark.gpu
+def test_batch_compaction_gives_identical_steps(libs):
+    """interface-branch compaction on and off over a batch (the case index
+    in blockIdx.z): the steps stay bit for bit"""
+    gpu, orc = libs
+    wls = ic.ensemble(9, seed=11, grids=SMALL_GRIDS)
+    st0 = prepare(gpu, orc, wls)
+    runs = {}
+    try:
+        for mode in (0, 1):
+            gpu.batch_release()
+            gpu.set_compaction(mode)
+            sts = [clone(s) for s in st0]
+            runs[mode] = ([gpu.integrate_batch(sts) for _ in range(3)], sts)
+    finally:
+        gpu.set_compaction(-1)
+        gpu.batch_release()
+    assert [list(d) for d in runs[0][0]] == [list(d) for d in runs[1][0]]
+    for k, (x, y) in enumerate(zip(runs[0][1], runs[1][1])):
+        for s in SLOTS:
+            assert np.array_equal(x.field(s), y.field(s)), (k, s)
