@@ -811,8 +811,9 @@ void enqueue_step(Ctx &c) {
 // columns per block of the Poisson transforms, wavenumbers per block of the
 // tridiagonal solves).  On the first step of a context it times each
 // candidate on the context's own state (saved before and put back after
-// every trial): the block shapes by two eager steps per candidate with CUDA
-// events around every launch, keeping the fastest per kernel class; then the
+// every trial): the block shapes by two eager steps per candidate (up to
+// eight on small grids) with CUDA events around every launch, keeping the
+// fastest per kernel class; then the
 // two Poisson choices by the time of whole steps.  Results do not depend on
 // the shapes.
 int g_autotune = 0;
@@ -857,6 +858,9 @@ int autotune(Ctx &c) {
   float best_ms[TK_COUNT];
   for (int k = 0; k < TK_COUNT; ++k) best_ms[k] = 1e30f;
   const Tiles keep = c.b.tiles;
+  // profiled steps per shape: 2, or up to 8 on grids below a million cells,
+  // whose kernels last a few microseconds each
+  const int nprof = (int)std::min(8., std::max(2., std::ceil(1e6 / ((double)c.nx * c.ny * c.nc))));
   int rc = 0;
   for (int t = 0; t < nshape && !rc; ++t) {
     Tiles cand = keep;
@@ -873,7 +877,7 @@ int autotune(Ctx &c) {
     g_prof.on = true;
     g_prof.used = 0;
     g_prof.marks.clear();
-    for (int r = 0; r < 2; ++r) enqueue_step(c);
+    for (int r = 0; r < nprof; ++r) enqueue_step(c);
     g_prof.on = false;
     if (sync(c)) {
       rc = 1;
