@@ -123,3 +123,18 @@ def test_init_errors(lib, tmp_path):
     os.remove(d / "xf.npy")
     rc, _ = _init(lib, str(d), env)
     assert rc != 0
+
+
+def test_switches_reject_bad_modes(lib):
+    """the run-mode switches check their argument on the host, before any
+    CUDA call, and report through sbfs_last_error"""
+    lib.sbfs_last_error.restype = C.c_char_p
+    for bad in (-2, 2):
+        assert lib.sbfs_set_compaction(bad) != 0
+        assert "compaction" in lib.sbfs_last_error().decode()
+    for mode in (0, 1, -1):  # ends on the default
+        assert lib.sbfs_set_compaction(mode) == 0
+    for bad in (-1, 3):
+        assert lib.sbfs_set_host_link(bad) != 0
+        assert "host-link" in lib.sbfs_last_error().decode()
+    assert lib.sbfs_set_host_link(1) == 0  # the default
