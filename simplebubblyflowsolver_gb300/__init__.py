@@ -239,7 +239,7 @@ class GpuLibrary(ReferenceAPI):
         self.lib.sbfs_tiles.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb), C.byref(gw), C.byref(cm))
-        names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_stress", "k_predict", "k_correct"]
+        names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_momflux", "k_predict_mf", "k_correct"]
         out = {n: f"{bx[k]}x{by[k]}" for k, n in enumerate(names)}
         out["fft_cols"] = fw.value
         out["tdm_modes"] = mb.value

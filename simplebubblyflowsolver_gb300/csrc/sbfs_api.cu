@@ -97,10 +97,11 @@ struct Ctx {
   // safety factor); graphs are dropped when any of them changes
   std::vector<double> graph_sig;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  // side stream of the step: decide_dt beside k_props, k_stress beside the
-  // interface kernels (fork / join events)
+  // side stream of the step: decide_dt beside k_props and the interface
+  // kernels, the next substage's k_props beside the predictor, the Poisson
+  // solve and the correction (fork / join events)
   cudaStream_t s2 = nullptr;
-  cudaEvent_t evf = nullptr, evd = nullptr, evs = nullptr, evp = nullptr;
+  cudaEvent_t evf = nullptr, evd = nullptr, evp = nullptr;
   bool props_ahead = false;  // the next substage's k_props is already on the side stream
   // host-linked step (strict sync mode, host arrays the GPU can address): the
   // step copies the state in and out itself, on the copy stream s3, each
@@ -127,7 +128,6 @@ struct Ctx {
     if (e1) cudaEventDestroy(e1);
     if (evf) cudaEventDestroy(evf);
     if (evd) cudaEventDestroy(evd);
-    if (evs) cudaEventDestroy(evs);
     if (evp) cudaEventDestroy(evp);
     for (cudaEvent_t e : evh)
       if (e) cudaEventDestroy(e);
@@ -236,13 +236,13 @@ int check_domain(const domain_t *d) {
 }
 
 // per-column coefficients (see Metrics)
-// (batches: one block of 6 columns per case, Re[k] per case; the kernels
-// offset only nuf, the one column that depends on the case)
+// (batches: one block of NCOL columns per case, Re[k] per case; the kernels
+// offset the columns that depend on the case: nuf, nuc, c4nuc, c2nuf)
 int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   const int nx = c.nx, n = nx + 3;
   const double hy = d->hy;
   const double dx = d->hxxc[0];
-  constexpr int NCOL = 10;
+  constexpr int NCOL = 13;
   std::vector<double> h(NCOL * (size_t)n * c.nc, 0.);
   for (int k = 0; k < c.nc; ++k) {
     const double nu = 1. / Re[k];
@@ -255,6 +255,8 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
       A(4, I) = nu / hf;
       A(5, I) = hf;
       A(8, I) = 0.5 * (1. / hf);
+      A(10, I) = dx / hf;
+      A(12, I) = 2. * (nu / hf);
     }
     for (int I = 1; I <= nx; ++I) {
       const double ihc = 1. / d->hxxc[I - 1];
@@ -262,6 +264,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
       A(6, I) = nu * ihc;
       A(7, I) = 0.25 * ihc;
       A(9, I) = 0.5 * ihc;
+      A(11, I) = 4. * (nu * ihc);
     }
   }
   c.g.cm = c.nc > 1 ? NCOL * n : 0;
@@ -281,6 +284,9 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   c.m.q4c = b + 7 * n;
   c.m.hihxxf = b + 8 * n;
   c.m.hihxxc = b + 9 * n;
+  c.m.rq = b + 10 * n;
+  c.m.c4nuc = b + 11 * n;
+  c.m.c2nuf = b + 12 * n;
   c.Re = Re[0];
   return 0;
 }
@@ -307,10 +313,17 @@ Phys phys_of(const fluid_t *f, const interface_t *itf) {
   return p;
 }
 
+// the constants of a case that depend on the grid
+void finish_phys(Phys &p, const Grid &g) {
+  p.nuy = p.nu * g.ihy;
+  p.qfy = p.qf * g.ihy;
+  p.nuy2 = 2. * p.nuy;
+  p.nuy4 = 4. * p.nuy;
+}
+
 void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
   c.ph = phys_of(f, itf);
-  c.ph.nuy = c.ph.nu * c.g.ihy;
-  c.ph.qfy = c.ph.qf * c.g.ihy;
+  finish_phys(c.ph, c.g);
 }
 
 double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
@@ -427,7 +440,6 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   CK(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&c->evf, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
-  CK(cudaEventCreateWithFlags(&c->evs, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
   CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
   for (cudaEvent_t &e : c->evh) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -464,7 +476,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
-                     &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.irhox, &b.irhoy};
+                     &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.egx, &b.egy, &b.pxx, &b.pyy, &b.pxy, &b.pyx};
   for (double **p : scal)
     if (dalloc(*c, p, n1 * nc)) return 1;
   if (dalloc(*c, &b.dvof, n2 * nc)) return 1;
@@ -610,11 +622,11 @@ struct Prof {
 } g_prof;
 
 enum KernelClass {
-  KC_PROPS, KC_CURV_LIST, KC_INTERFACE, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_STRESS, KC_PREDICT,
+  KC_PROPS, KC_CURV_LIST, KC_INTERFACE, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_MOMFLUX, KC_PREDICT,
   KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_MLP_CURV, KC_COUNT
 };
-const char *kKernelNames[KC_COUNT] = {"k_props", "k_curv_list", "k_interface_cells", "k_flux_force", "k_vof_advance", "k_stress",
-                                      "k_predict", "k_poisson_fwd", "k_poisson_tdm", "k_poisson_inv", "k_correct",
+const char *kKernelNames[KC_COUNT] = {"k_props", "k_curv_list", "k_interface_cells", "k_flux_force", "k_vof_advance", "k_momflux",
+                                      "k_predict_mf", "k_poisson_fwd", "k_poisson_tdm", "k_poisson_inv", "k_correct",
                                       "k_decide_dt", "k_mlp_curv"};
 
 // curvature model of the fused step: 0 = the reference's kappa = -div n,
@@ -709,10 +721,11 @@ void link_out(Ctx &c, int slot, const Layout &l, double *dev) {
   link_side(c, false, slot, l, dev);
 }
 
-// par: run decide_dt (already on the side stream, joined before the first
-// use of its scalars, when wait_dt) and k_stress on the side stream.  Both
-// only read what the main stream has finished when they are forked, and the
-// main stream waits for them before anything reads what they write.
+// par: decide_dt runs on the side stream (forked by enqueue_step, joined
+// before the first use of its scalars when wait_dt), and so does the next
+// substage's k_props once this substage's last reader of the viscosities and
+// corner normals (k_momflux) is enqueued.  The main stream waits for them
+// before anything reads what they write.
 void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   Bufs &b = c.b;
   if (k != 0) c.isrc ^= 1;  // stash the previous stage's sources (pointer swap)
@@ -729,13 +742,6 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   } else {
     timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
   }
-  if (par) {
-    // txx, txy, tyy need the velocity and the viscosities just computed
-    cudaEventRecord(c.evf, c.s);
-    cudaStreamWaitEvent(c.s2, c.evf, 0);
-    launch_stress(c.s2, c.g, c.m, b, ux, uy);
-    cudaEventRecord(c.evs, c.s2);
-  }
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
   const bool learned = g_curv_model != 0;
@@ -746,6 +752,11 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   if (c.link && k == 2) link_out(c, HL_VOF_OUT, L_VOF, b.vof);  // vof is final
+  // the last substage leaves txy at the walls for the wall-stress log (all of
+  // txx, txy, tyy when every array is synchronised), as the reference's
+  // fluid_t holds the stress of its last predictor
+  const int stress = k < 2 ? 0 : (g_sync_mode == SBFS_SYNC_ALL ? 2 : 1);
+  timed(c, KC_MOMFLUX, [&] { launch_momflux(c.s, c.g, c.m, c.ph, b, ux, uy, stress); });
   if (par && k < 2) {
     // the next substage's viscosities and corner normals need only the new
     // vof: they run beside this substage's predictor, Poisson solve and
@@ -756,22 +767,17 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     cudaEventRecord(c.evp, c.s2);
     c.props_ahead = true;
   }
-  if (par)
-    cudaStreamWaitEvent(c.s, c.evs, 0);
-  else
-    timed(c, KC_STRESS, [&] { launch_stress(c.s, c.g, c.m, b, ux, uy); });
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[2], 0);  // p is in
-  timed(c, KC_PREDICT, [&] {
-    launch_predict(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, b.mfluxx, b.mfluxy, den0, den1, sxa, sxb,
-                   nullptr, sya, syb, nullptr);
-  });
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[3], 0);  // psi is in
-  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, b, sc, k, uxs, uys, psio); });
+  timed(c, KC_PREDICT, [&] {
+    launch_predict_mf(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, den0, den1, psio, sxa, sxb, sya, syb);
+  });
+  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, b, sc, k, uxs, uys); });
   timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
   timed(c, KC_POISSON_INV, [&] { launch_poisson_inv(c.s, c.g, b, psin); });
   // psi of substages 2 and 3 are final: the caller's psi[1] and psi[0] after the step
   if (c.link && k >= 1) link_out(c, k == 1 ? HL_PSI1_OUT : HL_PSI0_OUT, L_P, psin);
-  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, b, sc, k, uxs, uys, psin, psio, true); });
+  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, b, sc, k, uxs, uys, psin, true); });
   c.iu ^= 1;
   c.ipsi ^= 1;
   c.iden ^= 1;
@@ -852,7 +858,7 @@ int autotune(Ctx &c) {
   for (int mb : {1, 2, 4})
     if (G * mb <= 4 && poisson_tdm_smem(c.nx, mb, G) <= 200 * 1024) tdms.push_back({mb, G});
   if (tdms.empty()) tdms.push_back({1, G});  // one pair per block (staged in global memory above ~6900 rows)
-  const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT,
+  const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_MOMFLUX, TK_PREDICT,
                                -1, -1, -1, TK_CORRECT, -1, -1};
   Tiles best = c.b.tiles;
   float best_ms[TK_COUNT];
@@ -976,7 +982,7 @@ int autotune(Ctx &c) {
 
 int role_key(const Ctx &c) {
   return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
-         (g_pdl << 6) | ((g_compact + 1) << 7);
+         (g_pdl << 6) | ((g_compact + 1) << 7) | ((g_sync_mode == SBFS_SYNC_ALL) << 9);
 }
 
 int launch_step(Ctx &c) {
@@ -1181,8 +1187,7 @@ Batch *prepare_batch(int n, const domain_t *const *d, fluid_t *const *f, interfa
       if (b->group_of[i] != (int)q) continue;
       const int k = b->slot_of[i];
       ph[k] = phys_of(f[i], itf[i]);
-      ph[k].nuy = ph[k].nu * c.g.ihy;
-      ph[k].qfy = ph[k].qf * c.g.ihy;
+      finish_phys(ph[k], c.g);
       ph[k].dtfix = fixed_dt(c, d[i], f[i], itf[i]);
       re[k] = f[i]->Re;
       re_changed = re_changed || !(b->res[i] == f[i]->Re);
@@ -1924,8 +1929,8 @@ int fluid_compute_potential(const domain_t *d, const double dt_old, const double
       h2d(*c, f->den[1], L_DEN, b.den1))
     return 1;
   if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
-  launch_face_factor(c->s, c->g, c->ph, b.den1, b.irhox, b.irhoy);
-  launch_poisson(c->s, c->g, b, b.scalars, 0, b.ux, b.uy, b.psi0, b.psi1);
+  launch_face_factor(c->s, c->g, c->ph, b, b.den1, b.psi0);
+  launch_poisson(c->s, c->g, b, b.scalars, 0, b.ux, b.uy, b.psi1);
   if (d2h(*c, f->psi[1], L_P, b.psi1)) return 1;
   return sync(*c);
 }
@@ -1940,8 +1945,8 @@ int fluid_correct_velocity(const domain_t *d, const double dt_old, const double 
       h2d(*c, f->psi[1], L_P, b.psi1) || h2d(*c, f->den[1], L_DEN, b.den1))
     return 1;
   if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
-  launch_face_factor(c->s, c->g, c->ph, b.den1, b.irhox, b.irhoy);
-  launch_correct(c->s, c->g, c->m, b, b.scalars, 0, b.ux, b.uy, b.psi1, b.psi0, false);
+  launch_face_factor(c->s, c->g, c->ph, b, b.den1, b.psi0);
+  launch_correct(c->s, c->g, c->m, b, b.scalars, 0, b.ux, b.uy, b.psi1, false);
   if (d2h(*c, f->ux, L_UX, b.ux) || d2h(*c, f->uy, L_UY, b.uy)) return 1;
   return sync(*c);
 }

@@ -35,6 +35,10 @@ struct Metrics {
   const double *q4c;    // 0.25 / HXXC(I)       (uy advection in x)
   const double *hihxxf; // 0.5 / HXXF(I)        (txy)
   const double *hihxxc; // 0.5 / HXXC(I)        (curvature)
+  // momentum fluxes of the fused step (k_momflux)
+  const double *rq;     // HXXC / HXXF(I)       (metric ratio of the ux advection along y)
+  const double *c4nuc;  // 4 (1 / Re) / HXXC(I) (4 nu txx)
+  const double *c2nuf;  // 2 (1 / Re) / HXXF(I) (4 nu txy)
 };
 
 struct Grid {
@@ -71,6 +75,7 @@ struct Phys {
   double rref2;       // 2 refden
   double nuy;         // nu / hy
   double qf, qfy;     // force_coef / 4, force_coef / 4 / hy
+  double nuy2, nuy4;  // 2 nu / hy, 4 nu / hy (k_momflux)
 };
 
 // x / 2 for a positive normal x (x >= 2^-1021), exactly: the exponent field

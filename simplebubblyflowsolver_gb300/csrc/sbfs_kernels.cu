@@ -578,8 +578,11 @@ __global__ void __launch_bounds__(BX *BY)
 //   adv_y = 0.25 HXXC / (HXXF(i) hy) [(G_j+1 sums)(u_j + u_j+1) - (G_j sums)(u_j-1 + u_j)]
 //   dif_x = nu / HXXF(i) (txx_i - txx_i-1),  dif_y = nu / hy (txy_j+1 - txy_j)
 // and the uy terms likewise with HXXC in place of HXXF.
+// This is the fine-grained entry point's form (fluid_predict_field returns
+// txx, txy, tyy and the sources); the fused step uses k_momflux and
+// k_predict_mf below, the same terms with every flux formed once.
 // thread (I, J): I = 1..nx handles the ux face I (I >= 2) and the uy face
-// (I, J - 1/2); also stores e = rho_ref / rho^{k+1} - 1 at both faces
+// (I, J - 1/2)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(BX *BY)
     k_predict(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, const double *__restrict__ ux,
@@ -589,7 +592,7 @@ __global__ void __launch_bounds__(BX *BY)
               const double *__restrict__ ifrcx, const double *__restrict__ ifrcy, const double *__restrict__ den0,
               const double *__restrict__ den1, double *__restrict__ sxa, const double *__restrict__ sxb,
               double *__restrict__ sxg, double *__restrict__ sya, const double *__restrict__ syb,
-              double *__restrict__ syg, double *__restrict__ ex, double *__restrict__ ey) {
+              double *__restrict__ syg) {
   pdl_entry();
   const Phys ph = zphys(g, ph0);
   const double *__restrict__ nuf = m.nuf + (size_t)blockIdx.z * g.cm;
@@ -603,7 +606,6 @@ __global__ void __launch_bounds__(BX *BY)
   // the update is carried as 2u with 2 alpha dt, ... and 1 / (2 rho_face):
   // powers of two, so every rounding is the one of the plain form
   const double adt2 = sc[sc_adt2(k)], bdt2 = sc[sc_bdt2(k)], gdt2 = sc[sc_gdt2(k)];
-  const double rref2 = ph.rref2;
   const double nuy = ph.nuy;
   // ---- ux at face I
   if (I >= 2) {
@@ -629,7 +631,6 @@ __global__ void __launch_bounds__(BX *BY)
     ux_out[ix(g, r, I - 1)] = u * ir2;
     sxa[ix(g, r, I - 2)] = a;
     if (sxg) sxg[ix(g, r, I - 2)] = gs;
-    ex[ix(g, r, I - 1)] = fma(rref2, ir2, -1.);
   }
   // ---- uy at face (I, J - 1/2)
   {
@@ -654,18 +655,172 @@ __global__ void __launch_bounds__(BX *BY)
     uy_out[ix(g, r, I)] = u * ir2;
     sya[ix(g, r, I - 1)] = a;
     if (syg) syg[ix(g, r, I - 1)] = gs;
-    ey[ix(g, r, I)] = fma(rref2, ir2, -1.);
   }
-  // walls: impermeable, no-slip; wall-face factors for the Poisson operator
+  // walls: impermeable, no-slip
   if (I == 1) {
     ux_out[ix(g, r, 0)] = 0.;
     uy_out[ix(g, r, 0)] = 0.;
-    ex[ix(g, r, 0)] = fma(rref2, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -1.);
   }
   if (I == g.nx) {
     ux_out[ix(g, r, g.nx)] = 0.;
     uy_out[ix(g, r, g.nx + 1)] = 0.;
-    ex[ix(g, r, g.nx)] = fma(rref2, rcp_nr(den1[ix(g, r, g.nx)] + den1[ix(g, r, g.nx + 1)]), -1.);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// momentum fluxes of the fused step, one per centre and corner
+//   src/fluid/predict/ux.c:29-144, uy.c:29-130 (advective and diffusive
+//   terms), txx.c:11-40, txy.c:13-50, tyy.c:10-38 (the stress components)
+// The reference's advective term of ux at face i is a difference of products
+// at the two neighbouring cell centres (along x) and corners (along y), and
+// its diffusive term a difference of txx and txy at the same points; k_predict
+// forms each product twice, once for each face it borders.  Here each point
+// gets its flux once, scaled by 4 so that the 1/4 of the face averages
+// moves into the face coefficient:
+//   centre (I, J):     Pxx = 4 nu txx - (mfx_I + mfx_I+1) (ux_I + ux_I+1)
+//                      Pyy = 4 nu tyy - (mfy_J-1/2 + mfy_J+1/2) (uy_J-1/2 + uy_J+1/2)
+//   corner (I, J-1/2): Pxy = 4 nu txy - r_I (mfy_I-1 + mfy_I) (ux_J-1 + ux_J)
+//                      Pyx = 4 nu txy - (mfx_J-1 + mfx_J) (uy_I-1 + uy_I)
+// (mfx, mfy the mass fluxes, r_I = HXXC / HXXF(I) the metric ratio of the
+// reference's y advection of ux).  k_predict_mf then adds, with nu / H =
+// 4 nu (0.25 / H), the reference's diffusion minus advection
+//   ux face I:    0.25 / HXXF(I) (Pxx_I - Pxx_I-1) + 0.25 / hy (Pxy_J+1/2 - Pxy_J-1/2)
+//   uy face J-1/2: 0.25 / HXXC(I) (Pyx_I+1 - Pyx_I) + 0.25 / hy (Pyy_J - Pyy_J-1)
+// FP64 operations per cell: 29 here and 39 in k_predict_mf (with the
+// Poisson face fluxes below) against 16 + 61 for k_stress + k_predict.
+// STRESS 1: also txy at the wall columns I = 1, nx + 1 (what the wall-stress
+// log reads, src/logging/stress.c); 2: the whole of txx, txy, tyy, in the
+// reference's form
+// thread (I, J): I = 1..nx+1 handles the corner (I, J - 1/2) and, for I <= nx,
+// the centre (I, J)
+// ---------------------------------------------------------------------------
+template <int STRESS>
+__global__ void __launch_bounds__(BX *BY)
+    k_momflux(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
+              const double *__restrict__ visux, const double *__restrict__ visuy, const double *__restrict__ mfx,
+              const double *__restrict__ mfy, double *__restrict__ pxx, double *__restrict__ pyy,
+              double *__restrict__ pxy, double *__restrict__ pyx, double *__restrict__ txx, double *__restrict__ txy,
+              double *__restrict__ tyy) {
+  pdl_entry();
+  const Phys ph = zphys(g, ph0);
+  const double *__restrict__ c4nuc = m.c4nuc + (size_t)blockIdx.z * g.cm;
+  const double *__restrict__ c2nuf = m.c2nuf + (size_t)blockIdx.z * g.cm;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (I > g.nx + 1 || J > g.ny) return;
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
+  const double u0 = ux[ix(g, r, I - 1)];    // ux at face I, row J
+  const double vx0 = visux[ix(g, r, I - 1)];
+  const double w0 = uy[ix(g, r, I)];        // uy of cell I at J - 1/2
+  const double vy0 = visuy[ix(g, r, I)];
+  {
+    // corner (I, J - 1/2): txy = 0.5 (mu_s + mu_n) du/dy + 0.5 (mu_w + mu_e) dv/dx
+    const double us = ux[ix(g, rm, I - 1)], ww = uy[ix(g, r, I - 1)];
+    const double sx = visux[ix(g, rm, I - 1)] + vx0;
+    const double sy = visuy[ix(g, r, I - 1)] + vy0;
+    const double du = u0 - us, dw = w0 - ww;
+    const double t4 = fma(sx, du * ph.nuy2, sy * (dw * c2nuf[I]));  // 4 nu txy
+    const double fy = mfy[ix(g, r, I - 1)] + mfy[ix(g, r, I)];
+    const double fx = mfx[ix(g, rm, I - 1)] + mfx[ix(g, r, I - 1)];
+    pxy[ix(g, r, I - 1)] = fma(-(m.rq[I] * fy), us + u0, t4);
+    pyx[ix(g, r, I - 1)] = fma(-fx, ww + w0, t4);
+    if (STRESS == 2 || (STRESS == 1 && (I == 1 || I == g.nx + 1)))
+      txy[ix(g, r, I - 1)] = fma(sx, du * g.hihy, sy * (dw * m.hihxxf[I]));
+  }
+  if (I <= g.nx) {
+    // centre (I, J): txx = (mu_l + mu_r) du/dx, tyy = (mu_s + mu_n) dv/dy
+    const double u1 = ux[ix(g, r, I)], w1 = uy[ix(g, rp, I)];
+    const double sx = vx0 + visux[ix(g, r, I)], sy = vy0 + visuy[ix(g, rp, I)];
+    const double du = u1 - u0, dw = w1 - w0;
+    pxx[ix(g, r, I - 1)] = fma(-(mfx[ix(g, r, I - 1)] + mfx[ix(g, r, I)]), u0 + u1, sx * (du * c4nuc[I]));
+    pyy[ix(g, r, I - 1)] = fma(-(mfy[ix(g, r, I)] + mfy[ix(g, rp, I)]), w0 + w1, sy * (dw * ph.nuy4));
+    if (STRESS == 2) {
+      txx[ix(g, r, I - 1)] = sx * (du * m.ihxxc[I]);
+      tyy[ix(g, r, I - 1)] = sy * (dw * g.ihy);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// momentum right-hand sides and the RK predictor of the fused step, from the
+// fluxes of k_momflux (the terms of k_predict, same discretisation)
+//   src/fluid/predict/ux.c:146-273, uy.c:132-251, main.c:9-80
+// Also stores, at both faces, e grad psi_old with e = rho_ref / rho^{k+1} - 1
+// and psi_old the potential of the previous substage: the variable-density
+// term of the Poisson right-hand side (src/fluid/compute_potential.c:
+// 285-363) and of the velocity correction (src/fluid/correct_velocity/ux.c:
+// 18-66, uy.c:17-64) is the same face quantity, so both read it from here.
+// thread (I, J): I = 1..nx handles the ux face I (I >= 2) and the uy face
+// (I, J - 1/2)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BX *BY)
+    k_predict_mf(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, const double *__restrict__ ux,
+                 const double *__restrict__ uy, double *__restrict__ ux_out, double *__restrict__ uy_out,
+                 const double *__restrict__ pxx, const double *__restrict__ pyy, const double *__restrict__ pxy,
+                 const double *__restrict__ pyx, const double *__restrict__ p, const double *__restrict__ ifrcx,
+                 const double *__restrict__ ifrcy, const double *__restrict__ den0, const double *__restrict__ den1,
+                 const double *__restrict__ psio, double *__restrict__ sxa, const double *__restrict__ sxb,
+                 double *__restrict__ sya, const double *__restrict__ syb, double *__restrict__ egx,
+                 double *__restrict__ egy) {
+  pdl_entry();
+  const Phys ph = zphys(g, ph0);
+  sc += (size_t)blockIdx.z * (kScalars);
+  const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (I > g.nx || J > g.ny) return;
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
+  // the update is carried as 2u with 2 alpha dt, ... and 1 / (2 rho_face):
+  // powers of two, so every rounding is the one of the plain form
+  const double adt2 = sc[sc_adt2(k)], bdt2 = sc[sc_bdt2(k)], gdt2 = sc[sc_gdt2(k)];
+  const double rref2 = ph.rref2;
+  const double ps0 = psio[ix(g, r, I)];
+  // ---- ux at face I
+  if (I >= 2) {
+    const double u0 = ux[ix(g, r, I - 1)];
+    double a = ifrcx[ix(g, r, I - 2)];
+    const double rho0 = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];  // 2 rho^k
+    a = fma(ph.hgrav, rho0, a);
+    a = fma(m.q4f[I], pxx[ix(g, r, I - 1)] - pxx[ix(g, r, I - 2)], a);
+    a = fma(g.q4y, pxy[ix(g, rp, I - 1)] - pxy[ix(g, r, I - 1)], a);
+    const double gs = (p[ix(g, r, I - 1)] - p[ix(g, r, I)]) * m.ihxxf[I];
+    const double ir2 = rcp_nr(den1[ix(g, r, I - 1)] + den1[ix(g, r, I)]);  // 1 / (2 rho^{k+1})
+    double u = fma(adt2, a, rho0 * u0);
+    if (k != 0) u = fma(bdt2, sxb[ix(g, r, I - 2)], u);
+    u = fma(gdt2, gs, u);
+    ux_out[ix(g, r, I - 1)] = u * ir2;
+    sxa[ix(g, r, I - 2)] = a;
+    egx[ix(g, r, I - 1)] = fma(rref2, ir2, -1.) * (ps0 - psio[ix(g, r, I - 1)]);
+  }
+  // ---- uy at face (I, J - 1/2)
+  {
+    const double w0 = uy[ix(g, r, I)];
+    double a = ifrcy[ix(g, r, I - 1)];
+    a = fma(m.q4c[I], pyx[ix(g, r, I)] - pyx[ix(g, r, I - 1)], a);
+    a = fma(g.q4y, pyy[ix(g, r, I - 1)] - pyy[ix(g, rm, I - 1)], a);
+    const double gs = (p[ix(g, rm, I)] - p[ix(g, r, I)]) * g.ihy;
+    const double rho0 = den0[ix(g, rm, I)] + den0[ix(g, r, I)];  // 2 rho^k
+    const double ir2 = rcp_nr(den1[ix(g, rm, I)] + den1[ix(g, r, I)]);
+    double u = fma(adt2, a, rho0 * w0);
+    if (k != 0) u = fma(bdt2, syb[ix(g, r, I - 1)], u);
+    u = fma(gdt2, gs, u);
+    uy_out[ix(g, r, I)] = u * ir2;
+    sya[ix(g, r, I - 1)] = a;
+    egy[ix(g, r, I)] = fma(rref2, ir2, -1.) * (ps0 - psio[ix(g, rm, I)]);
+  }
+  // walls: impermeable, no-slip; the wall faces' e grad psi_old (zero for a
+  // Neumann psi_old, computed as the reference does)
+  if (I == 1) {
+    ux_out[ix(g, r, 0)] = 0.;
+    uy_out[ix(g, r, 0)] = 0.;
+    egx[ix(g, r, 0)] = fma(rref2, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -1.) * (ps0 - psio[ix(g, r, 0)]);
+  }
+  if (I == g.nx) {
+    ux_out[ix(g, r, g.nx)] = 0.;
+    uy_out[ix(g, r, g.nx + 1)] = 0.;
+    egx[ix(g, r, g.nx)] =
+        fma(rref2, rcp_nr(den1[ix(g, r, g.nx)] + den1[ix(g, r, g.nx + 1)]), -1.) * (psio[ix(g, r, g.nx + 1)] - ps0);
   }
 }
 
@@ -680,6 +835,7 @@ __global__ void __launch_bounds__(BX *BY)
 //   1. k_poisson_fwd: right-hand side of src/fluid/compute_potential.c:
 //      285-363 for a tile of W columns,
 //        rhs = rho_ref/dt_new div u* - dt_old/dt_new div((rho_ref/rho - 1) grad psi_old)
+//      (the face values of (rho_ref/rho - 1) grad psi_old come from k_predict_mf)
 //      with div and the face differences in the JD = H hy form, packed two
 //      reals per complex, a mixed radix-4/2 Stockham FFT of length ny/2 in
 //      shared memory and the real-to-complex split; spectrum [I][m]
@@ -757,8 +913,8 @@ __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__res
 template <int W>
 __global__ void __launch_bounds__(256)
     k_poisson_fwd(Grid g, const double *__restrict__ sc, int k, const double *__restrict__ ux,
-                  const double *__restrict__ uy, const double *__restrict__ psi, const double *__restrict__ ex,
-                  const double *__restrict__ ey, const double2 *__restrict__ tw, double2 *__restrict__ spec) {
+                  const double *__restrict__ uy, const double *__restrict__ egx, const double *__restrict__ egy,
+                  const double2 *__restrict__ tw, double2 *__restrict__ spec) {
   pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   spec += (size_t)blockIdx.z * (g.css);
@@ -775,11 +931,11 @@ __global__ void __launch_bounds__(256)
     if (I <= g.nx) {
       // global rows of this case (the case's rows follow each other)
       const int zr = blockIdx.z * ny;
-      const int rg = r + zr, rm = (r == 0 ? ny - 1 : r - 1) + zr, rp = (r == ny - 1 ? 0 : r + 1) + zr;
-      const double ps = psi[ix(g, rg, I)];
-      // (e dpsi) differences across the cell; the wall faces have dpsi = 0
-      const double X = fma(ex[ix(g, rg, I)], psi[ix(g, rg, I + 1)] - ps, -ex[ix(g, rg, I - 1)] * (ps - psi[ix(g, rg, I - 1)]));
-      const double Y = fma(ey[ix(g, rp, I)], psi[ix(g, rp, I)] - ps, -ey[ix(g, rg, I)] * (ps - psi[ix(g, rm, I)]));
+      const int rg = r + zr, rp = (r == ny - 1 ? 0 : r + 1) + zr;
+      // differences of e grad psi_old across the cell (its faces' values
+      // written by k_predict_mf or k_face_factor)
+      const double X = egx[ix(g, rg, I)] - egx[ix(g, rg, I - 1)];
+      const double Y = egy[ix(g, rp, I)] - egy[ix(g, rg, I)];
       const double dux = ux[ix(g, rg, I)] - ux[ix(g, rg, I - 1)];
       const double duy = uy[ix(g, rp, I)] - uy[ix(g, rg, I)];
       val = fma(pdx, dux, fma(pdy, duy, fma(pax, X, pay * Y)));
@@ -1020,14 +1176,15 @@ __global__ void __launch_bounds__(512)
 //   src/fluid/correct_velocity/ux.c:18-66, uy.c:17-64
 //   src/fluid/update_pressure.c:7-53
 //   u -= dt_new / rho_ref dpsi_new / h;  u += -dt_old (1/rho - 1/rho_ref) dpsi_old / h
-//   with 1/rho - 1/rho_ref = e / rho_ref
+//   with 1/rho - 1/rho_ref = e / rho_ref; e dpsi_old at the faces is egx, egy
+//   (k_predict_mf or k_face_factor)
 // thread (I, J): I = 1..nx
 // ---------------------------------------------------------------------------
 template <bool PRES>
 __global__ void __launch_bounds__(BX *BY)
     k_correct(Grid g, Metrics m, const double *__restrict__ sc, int k, double *__restrict__ ux,
-              double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ psio,
-              const double *__restrict__ ex, const double *__restrict__ ey, double *__restrict__ p) {
+              double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ egx,
+              const double *__restrict__ egy, double *__restrict__ p) {
   pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -1037,18 +1194,18 @@ __global__ void __launch_bounds__(BX *BY)
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
   const double cnew = sc[sc_cnew(k)], cold = sc[sc_cold(k)];
   const double cnewy = sc[sc_cnewy(k)], coldy = sc[sc_coldy(k)];
-  const double pn0 = psin[ix(g, r, I)], po0 = psio[ix(g, r, I)];
+  const double pn0 = psin[ix(g, r, I)];
   if (I >= 2) {
     const double ih = m.ihxxf[I];
     double u = ux[ix(g, r, I - 1)];
     u = fma(-(cnew * ih), pn0 - psin[ix(g, r, I - 1)], u);
-    u = fma((cold * ih) * ex[ix(g, r, I - 1)], po0 - psio[ix(g, r, I - 1)], u);
+    u = fma(cold * ih, egx[ix(g, r, I - 1)], u);
     ux[ix(g, r, I - 1)] = u;
   }
   {
     double u = uy[ix(g, r, I)];
     u = fma(-cnewy, pn0 - psin[ix(g, rm, I)], u);
-    u = fma(coldy * ey[ix(g, r, I)], po0 - psio[ix(g, rm, I)], u);
+    u = fma(coldy, egy[ix(g, r, I)], u);
     uy[ix(g, r, I)] = u;
   }
   if (I == 1) {
@@ -1201,17 +1358,23 @@ __global__ void __launch_bounds__(BX *BY)
   for (int i = tid; i <= g.nx + 3; i += BX * BY) acc[i] = 0ULL;
 }
 
-// e = rho_ref / rho - 1 at ux faces (I = 1..nx+1) and uy faces (I = 1..nx)
-// from a density field, as k_predict stores it (fine-grained entry points)
-__global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, double *__restrict__ ex,
-                              double *__restrict__ ey) {
+// e grad psi_old, e = rho_ref / rho - 1, at ux faces (I = 1..nx+1) and uy
+// faces (I = 1..nx) from a density field and psi_old, as k_predict_mf stores
+// it (fine-grained entry points)
+__global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, const double *__restrict__ psio,
+                              double *__restrict__ egx, double *__restrict__ egy) {
   pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int r = J - 1, rm = wrap(J - 1, g.ny);
-  ex[ix(g, r, I - 1)] = fma(ph.refden, rcp_nr(half_sum(den[ix(g, r, I - 1)], den[ix(g, r, I)])), -1.);
-  if (I <= g.nx) ey[ix(g, r, I)] = fma(ph.refden, rcp_nr(half_sum(den[ix(g, rm, I)], den[ix(g, r, I)])), -1.);
+  const double ps = psio[ix(g, r, I)];
+  const double ex = fma(ph.rref2, rcp_nr(den[ix(g, r, I - 1)] + den[ix(g, r, I)]), -1.);
+  egx[ix(g, r, I - 1)] = ex * (ps - psio[ix(g, r, I - 1)]);
+  if (I <= g.nx) {
+    const double ey = fma(ph.rref2, rcp_nr(den[ix(g, rm, I)] + den[ix(g, r, I)]), -1.);
+    egy[ix(g, r, I)] = ey * (ps - psio[ix(g, rm, I)]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1592,7 +1755,25 @@ void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, con
 
 void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *ux,
                    const double *uy) {
-  launch_pdl(k_stress, tile_grid(b.tiles, TK_STRESS, g.nx + 1, g.ny, g.nc), tile_block(b.tiles, TK_STRESS), 0, s, g, m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
+  launch_pdl(k_stress, tile_grid(b.tiles, TK_MOMFLUX, g.nx + 1, g.ny, g.nc), tile_block(b.tiles, TK_MOMFLUX), 0, s, g,
+             m, ux, uy, b.visux, b.visuy, b.txx, b.txy, b.tyy);
+}
+
+void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                    const double *ux, const double *uy, int stress) {
+  const dim3 gr = tile_grid(b.tiles, TK_MOMFLUX, g.nx + 1, g.ny, g.nc), bl = tile_block(b.tiles, TK_MOMFLUX);
+  auto k = stress == 2 ? k_momflux<2> : (stress == 1 ? k_momflux<1> : k_momflux<0>);
+  launch_pdl(k, gr, bl, 0, s, g, m, ph, ux, uy, b.visux, b.visuy, b.mfluxx, b.mfluxy, b.pxx, b.pyy, b.pxy, b.pyx,
+             b.txx, b.txy, b.tyy);
+}
+
+void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                       const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
+                       const double *den0, const double *den1, const double *psi_old, double *srcux_a,
+                       const double *srcux_b, double *srcuy_a, const double *srcuy_b) {
+  launch_pdl(k_predict_mf, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g,
+             m, ph, sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, b.ifrcx, b.ifrcy, den0, den1,
+             psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -1602,28 +1783,27 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                     double *srcuy_g) {
   launch_pdl(k_predict, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g, m, ph, sc, k, ux, uy, ux_out, uy_out, mfx, mfy, b.txx,
                                                         b.txy, b.tyy, b.p, b.ifrcx, b.ifrcy, den0, den1, srcux_a,
-                                                        srcux_b, srcux_g, srcuy_a, srcuy_b, srcuy_g, b.irhox,
-                                                        b.irhoy);
+                                                        srcux_b, srcux_g, srcuy_a, srcuy_b, srcuy_g);
 }
 
 template <int W>
 void poisson_fwd_w(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
-                   const double *uy, const double *psi_old) {
+                   const double *uy) {
   const int nb = (g.nx + W - 1) / W;
-  launch_pdl(k_poisson_fwd<W>, dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s, g, sc, k, ux, uy, psi_old, b.irhox,
-                                                                           b.irhoy, b.twiddle, b.spec);
+  launch_pdl(k_poisson_fwd<W>, dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s, g, sc, k, ux, uy, b.egx, b.egy,
+             b.twiddle, b.spec);
 }
 
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
-                        const double *uy, const double *psi_old) {
+                        const double *uy) {
   if (b.tiles.fft_w == 1)
-    poisson_fwd_w<1>(s, g, b, sc, k, ux, uy, psi_old);
+    poisson_fwd_w<1>(s, g, b, sc, k, ux, uy);
   else if (b.tiles.fft_w == 2)
-    poisson_fwd_w<2>(s, g, b, sc, k, ux, uy, psi_old);
+    poisson_fwd_w<2>(s, g, b, sc, k, ux, uy);
   else if (b.tiles.fft_w == 8)
-    poisson_fwd_w<8>(s, g, b, sc, k, ux, uy, psi_old);
+    poisson_fwd_w<8>(s, g, b, sc, k, ux, uy);
   else
-    poisson_fwd_w<4>(s, g, b, sc, k, ux, uy, psi_old);
+    poisson_fwd_w<4>(s, g, b, sc, k, ux, uy);
 }
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
@@ -1658,19 +1838,19 @@ void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *ps
 }
 
 void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
-                    const double *uy, const double *psi_old, double *psi_new) {
-  launch_poisson_fwd(s, g, b, sc, k, ux, uy, psi_old);
+                    const double *uy, double *psi_new) {
+  launch_poisson_fwd(s, g, b, sc, k, ux, uy);
   launch_poisson_tdm(s, g, b);
   launch_poisson_inv(s, g, b, psi_new);
 }
 
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
-                    double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure) {
+                    double *ux, double *uy, const double *psi_new, bool pressure) {
   const dim3 gr = tile_grid(b.tiles, TK_CORRECT, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_CORRECT);
   if (pressure)
-    launch_pdl(k_correct<true>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
+    launch_pdl(k_correct<true>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, b.egx, b.egy, b.p);
   else
-    launch_pdl(k_correct<false>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, psi_old, b.irhox, b.irhoy, b.p);
+    launch_pdl(k_correct<false>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, b.egx, b.egy, b.p);
 }
 
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new) {
@@ -1686,8 +1866,9 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
                                                     coef_adv);
 }
 
-void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey) {
-  launch_pdl(k_face_factor, grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s, g, ph, den, ex, ey);
+void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *den,
+                        const double *psi_old) {
+  launch_pdl(k_face_factor, grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s, g, ph, den, psi_old, b.egx, b.egy);
 }
 
 int diag_partial_blocks(const Grid &g) {

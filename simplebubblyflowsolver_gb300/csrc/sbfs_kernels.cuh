@@ -10,7 +10,7 @@ namespace sbfs {
 // launch shapes of the fused step, picked by the autotuner (sbfs_api.cu) or
 // the defaults below; results do not depend on them (every cell, column
 // and mode is computed independently of its block)
-enum TileKernel { TK_PROPS, TK_CURV_LIST, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_STRESS, TK_PREDICT, TK_CORRECT, TK_COUNT };
+enum TileKernel { TK_PROPS, TK_CURV_LIST, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_MOMFLUX, TK_PREDICT, TK_CORRECT, TK_COUNT };
 struct Tiles {
   unsigned short bx[TK_COUNT], by[TK_COUNT];  // block shape (bx * by <= 256)
   int fft_w;   // columns per block of the Poisson transforms: 1, 2, 4 or 8
@@ -34,8 +34,12 @@ struct Bufs {
   double *fluxx, *fluxy, *mfluxx, *mfluxy;
   // RK sources
   double *srcux[3], *srcuy[3], *srcvof[2];
-  // face factors e = rho_ref / rho^{k+1} - 1 at ux and uy faces
-  double *irhox, *irhoy;
+  // momentum fluxes of the fused step (k_momflux): 4 nu txx - C and 4 nu tyy - E
+  // at cell centres, the ux and uy fluxes 4 nu txy - r D at the corners
+  double *pxx, *pyy, *pxy, *pyx;
+  // e grad psi_old at the ux and uy faces, e = rho_ref / rho^{k+1} - 1: the
+  // variable-density part of the Poisson right-hand side and of the correction
+  double *egx, *egy;
   // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
   double2 *spec;
   double2 *tdm_fac[3];  // (w, v, P, Q) per row for 1, 2, 4 warps per system, see k_poisson_tdm
@@ -73,25 +77,44 @@ void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const P
                         const double *ux, const double *uy, double *den1);
 void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b,
                               const double *ux, const double *uy);
+// the reference's txx, txy, tyy (fine-grained entry point)
 void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *ux, const double *uy);
+// the reference's momentum right-hand sides and predictor from txx, txy, tyy
+// and the mass fluxes (fine-grained entry point)
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                     const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
                     const double *mfx, const double *mfy, const double *den0, const double *den1,
                     double *srcux_a, const double *srcux_b, double *srcux_g,
                     double *srcuy_a, const double *srcuy_b, double *srcuy_g);
+// fused step: the momentum fluxes of every centre and corner (b.pxx, b.pyy,
+// b.pxy, b.pyx) from the velocity, the viscosities and the mass fluxes;
+// stress = 1 also writes txy at the two wall columns (the wall-stress log
+// reads it), 2 the whole of txx, txy, tyy
+void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                    const double *ux, const double *uy, int stress);
+// fused step: the predictor from those fluxes; also writes e grad psi_old at
+// the faces (b.egx, b.egy) for the Poisson right-hand side and the correction
+void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                       const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
+                       const double *den0, const double *den1, const double *psi_old, double *srcux_a,
+                       const double *srcux_b, double *srcuy_a, const double *srcuy_b);
+// the Poisson solve; the right-hand side reads b.egx, b.egy
 void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
-                    const double *uy, const double *psi_old, double *psi_new);
+                    const double *uy, double *psi_new);
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
-                        const double *uy, const double *psi_old);
+                        const double *uy);
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b);
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new);
+// velocity correction (+ pressure); reads b.egx, b.egy
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
-                    double *ux, double *uy, const double *psi_new, const double *psi_old, bool pressure);
+                    double *ux, double *uy, const double *psi_new, bool pressure);
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new);
 void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                       const double *ux, const double *uy, double dt_fixed, double coef_adv);
-// e = rho_ref / rho - 1 at the faces from a density field (as k_predict stores it)
-void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const double *den, double *ex, double *ey);
+// e grad psi_old at the faces (b.egx, b.egy) from a density field and psi_old,
+// as k_predict_mf stores it (fine-grained entry points)
+void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *den,
+                        const double *psi_old);
 // logging diagnostics (16 doubles, see k_diag_partial) and statistics sums
 int diag_partial_blocks(const Grid &g);
 void launch_diagnostics(cudaStream_t s, const Grid &g, const Metrics &m, const double *ux, const double *uy,

@@ -14,6 +14,16 @@
 // per GPU that loads the library and stays there until the process exits.
 // Every call uses the same array: calls that overlap on the GPU (issued on
 // streams without an order between them) race on it and give wrong results.
+//
+// Set-up: the first call on each GPU is where the CUDA runtime loads this
+// file's device code onto that GPU (with the default lazy module loading);
+// loading places the code and the scratch array in device memory and may
+// synchronise.  A caller that must not see that mid-run makes one warm-up
+// call per GPU while it initialises, before any stream capture.  Every call
+// looks the array's device address up again (a host-side lookup that
+// allocates nothing once the code is loaded), so an address never outlives
+// the context it belongs to (after cudaDeviceReset the code is loaded anew,
+// possibly elsewhere).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -30,10 +40,9 @@ namespace {
 constexpr int kScratchWords = SBFS_NOALLOC_MAX_NX + 8;
 static __device__ __align__(256) unsigned long long g_dt_scratch[kScratchWords];
 
-// device address of g_dt_scratch per device, resolved once per device
-constexpr int kMaxDevices = 64;
-unsigned long long *g_scratch_addr[kMaxDevices];
-char g_last_error[256];
+// message of this thread's last failure (threads driving different GPUs do
+// not overwrite each other's)
+thread_local char g_last_error[256];
 
 int report(const char *msg, cudaError_t e) {
   snprintf(g_last_error, sizeof(g_last_error), "%s%s%s", msg, e == cudaSuccess ? "" : ": ",
@@ -57,21 +66,16 @@ extern "C" int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, cons
   if (pitch < nx + 2) return report("sbfs_decide_dt_noalloc: pitch must be at least nx + 2 doubles", cudaSuccess);
   if (!ux || !uy || !hxxf || !scalars || !status)
     return report("sbfs_decide_dt_noalloc: null device pointer", cudaSuccess);
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return report("sbfs_decide_dt_noalloc: cudaGetDevice", e);
-  if (dev < 0 || dev >= kMaxDevices) return report("sbfs_decide_dt_noalloc: device index out of range", cudaSuccess);
-  if (!g_scratch_addr[dev]) {
-    // host code may not use g_dt_scratch as an address: ask the runtime for
-    // the device address of this device's copy (first call on each device)
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_dt_scratch);
-    if (e != cudaSuccess) return report("sbfs_decide_dt_noalloc: cudaGetSymbolAddress", e);
-    g_scratch_addr[dev] = static_cast<unsigned long long *>(p);
-  }
+  // host code may not use g_dt_scratch as an address: the runtime gives the
+  // device address of the current GPU's copy (on the first call on a GPU this
+  // also loads the module, see above)
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_dt_scratch);
+  if (e != cudaSuccess) return report("sbfs_decide_dt_noalloc: cudaGetSymbolAddress", e);
+  unsigned long long *scratch = static_cast<unsigned long long *>(p);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the kernel needs zeroed accumulators; the array keeps the last call's words
-  e = cudaMemsetAsync(g_scratch_addr[dev], 0, sizeof(unsigned long long) * (nx + 4), s);
+  e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (nx + 4), s);
   if (e != cudaSuccess) return report("sbfs_decide_dt_noalloc: clearing the scratch", e);
   Grid g{};
   g.nc = 1;
@@ -99,7 +103,7 @@ extern "C" int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, cons
   for (int d = 0; d < 2; ++d) cap = fmin(cap, sqrt(1. / (1. / We) / 4. / pi * pow(h[d], 3.)));
   dt_fixed = fmin(dt_fixed, cap * coef_int);
   Bufs b{};
-  b.dt_acc = g_scratch_addr[dev];
+  b.dt_acc = scratch;
   b.scalars = scalars;
   b.status = status;
   launch_decide_dt(s, g, m, ph, b, ux, uy, dt_fixed, coef_adv);
