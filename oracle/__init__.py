@@ -87,12 +87,39 @@ def ref_available() -> bool:
 
 class RefShim(ReferenceAPI):
     """The reference's own sources (one grid per process: they keep
-    function-static solver state)."""
+    function-static solver state; its statistics accumulate across cases)."""
 
     def __init__(self):
         lib = C.CDLL(REF_SO)
         super().__init__(lib, prefix="", name="reference")
         lib.sbfs_refshim_info.restype = C.c_void_p
+        P = C.c_void_p
+        lib.sbfs_refshim_log.argtypes = [P, C.c_size_t, C.c_double, C.c_double, C.c_double, P, P]
+        lib.sbfs_refshim_stats_init.argtypes = [P, C.c_double]
+        lib.sbfs_refshim_stats_collect.argtypes = [P, P, P]
+        lib.sbfs_refshim_stats_output.argtypes = [P, C.c_size_t]
+        for fn in ("domain_init", "domain_save"):
+            getattr(lib, fn).argtypes = [C.c_char_p, P]
+        for fn in ("fluid_init", "fluid_save", "interface_init", "interface_save"):
+            getattr(lib, fn).argtypes = [C.c_char_p, P, P]
 
     def info(self):
         return self.lib.sbfs_refshim_info()
+
+    # the reference's logging and statistics (src/logging/, src/statistics.c);
+    # they write under output/ of the current directory, as the reference does
+    def log(self, st, step, time, dt, wtime):
+        d, f, i = self._ptrs(st)
+        self.lib.sbfs_refshim_log(d, step, time, dt, wtime, f, i)
+
+    def stats_init(self, st, time):
+        if self.lib.sbfs_refshim_stats_init(C.addressof(st.domain), time):
+            raise RuntimeError("reference statistics.init failed (stat_rate / stat_after unset?)")
+
+    def stats_collect(self, st):
+        d, f, i = self._ptrs(st)
+        self.lib.sbfs_refshim_stats_collect(d, f, i)
+
+    def stats_output(self, st, step):
+        if self.lib.sbfs_refshim_stats_output(C.addressof(st.domain), step):
+            raise RuntimeError("reference statistics.output failed")

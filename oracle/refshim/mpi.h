@@ -56,4 +56,28 @@ int MPI_Sendrecv(const void *sendbuf, int sendcount, MPI_Datatype sendtype, int 
                  MPI_Comm comm, MPI_Status *status);
 double MPI_Wtime(void);
 
+/* MPI-IO on one rank (src/fileio.c): a file handle is a stdio stream; a
+ * subarray file type must cover its whole array (one rank owns everything),
+ * so a file view is the data offset after the NPY header and the collective
+ * read / write are fread / fwrite of count elements of the given extent */
+typedef struct sbfs_mpi_file_s *MPI_File;
+typedef long MPI_Offset;
+typedef int MPI_Info;
+#define MPI_INFO_NULL ((MPI_Info)0)
+#define MPI_MODE_CREATE 1
+#define MPI_MODE_RDONLY 2
+#define MPI_MODE_WRONLY 4
+#define MPI_MODE_RDWR 8
+#define MPI_ORDER_C 56
+#define MPI_ERR_OTHER 15
+int MPI_File_open(MPI_Comm comm, const char *filename, int amode, MPI_Info info, MPI_File *fh);
+int MPI_File_close(MPI_File *fh);
+int MPI_File_set_view(MPI_File fh, MPI_Offset disp, MPI_Datatype etype, MPI_Datatype filetype, const char *datarep,
+                      MPI_Info info);
+int MPI_File_read_all(MPI_File fh, void *buf, int count, MPI_Datatype type, MPI_Status *status);
+int MPI_File_write_all(MPI_File fh, const void *buf, int count, MPI_Datatype type, MPI_Status *status);
+int MPI_Type_create_subarray(int ndims, const int sizes[], const int subsizes[], const int starts[], int order,
+                             MPI_Datatype oldtype, MPI_Datatype *newtype);
+int MPI_Error_string(int errorcode, char *string, int *resultlen);
+
 #endif

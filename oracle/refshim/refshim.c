@@ -1,4 +1,3 @@
-#define _POSIX_C_SOURCE 199309L
 /*
  * Implementations behind the single-rank MPI, SimpleDecomp and FFTW stand-ins
  * (see mpi.h, sdecomp.h, fftw3.h in this directory), plus a few helpers that

@@ -32,7 +32,13 @@ def make_workload(name, nx, ny, seed=0, nbubbles=64):
     raise ValueError(name)
 
 
-def run(backend_name, wl, steps):
+LOG_FILES = ("progress.dat", "divergence.dat", "momentum.dat", "extrema.dat", "energy.dat", "stress.dat", "vof.dat")
+
+
+def run(backend_name, wl, steps, monitor=None):
+    """monitor (reference backend only): a directory in which the reference's
+    own logging writes its seven monitor files after every step and its
+    statistics collect every step's state and are written after the last"""
     for k, v in wl.env().items():
         os.environ[k] = v
     import oracle
@@ -47,10 +53,37 @@ def run(backend_name, wl, steps):
                            visr=wl.visr, info=info)
     be.apply_initial_boundaries(st)
     dts = []
-    for _ in range(steps):
-        dts.append(be.integrate(st))
+    here = os.getcwd()
+    if monitor:
+        os.makedirs(os.path.join(monitor, "output", "log"), exist_ok=True)
+        os.makedirs(os.path.join(monitor, "output", "stat"), exist_ok=True)
+        os.environ.setdefault("stat_rate", "1.0")
+        os.environ.setdefault("stat_after", "0.0")
+        os.chdir(monitor)
+        be.stats_init(st, 0.0)
+    try:
+        t = 0.0
+        for step in range(1, steps + 1):
+            dts.append(be.integrate(st))
+            t += dts[-1]
+            if monitor:
+                be.log(st, step, t, dts[-1], 0.0)
+                be.stats_collect(st)
+        if monitor:
+            be.stats_output(st, steps)
+    finally:
+        os.chdir(here)
     out = {s: st.interior_rows(s).copy() for s in STATE_SLOTS}
     out["dt"] = np.array(dts)
+    if monitor:
+        # the stress the last predictor left (the wall-stress log reads it)
+        out["txy"] = st.interior_rows("txy").copy()
+        for name in LOG_FILES:
+            with open(os.path.join(monitor, "output", "log", name)) as fh:
+                out["log_" + name.split(".")[0]] = np.array(fh.read())
+        sdir = os.path.join(monitor, "output", "stat", f"step{steps:010d}")
+        for name in ("num", "ux1", "uy1", "vof1"):
+            out["stat_" + name] = np.load(os.path.join(sdir, name + ".npy"))
     return out
 
 
@@ -64,9 +97,10 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--out", required=True)
+    ap.add_argument("--monitor", default=None, help="directory for the reference's logging and statistics output")
     a = ap.parse_args()
     wl = make_workload(a.workload, a.nx, a.ny, a.seed, a.nbubbles)
-    out = run(a.backend, wl, a.steps)
+    out = run(a.backend, wl, a.steps, a.monitor)
     np.savez(a.out, **out)
 
 

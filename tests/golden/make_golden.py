@@ -6,9 +6,13 @@ reference keeps function-static solver state.
     python tests/golden/make_golden.py
 
 Fixture content: the state after N steps of integrate() (ux, uy, p, psi, vof
-interior rows with x ghosts, i.e. the reference's .npy layout) and the dt of
-every step.  Inputs are regenerated by simplebubblyflowsolver_gb300.ic with
-the case parameters stored alongside.
+interior rows with x ghosts, i.e. the reference's .npy layout), the dt of
+every step, and what the reference's own monitoring wrote over the run: its
+seven log files after every step (log_*, the text of src/logging/*.c) with
+the txy the last predictor left (the wall-stress log reads it), and its
+statistics sums over the N steps (stat_num, stat_ux1, stat_uy1, stat_vof1,
+the arrays src/statistics.c writes).  Inputs are regenerated by
+simplebubblyflowsolver_gb300.ic with the case parameters stored alongside.
 """
 from __future__ import annotations
 
@@ -41,14 +45,15 @@ def main():
         with tempfile.TemporaryDirectory() as td:
             out = os.path.join(td, "out.npz")
             cmd = [sys.executable, "-m", "oracle.run_case", "--backend", "ref", "--workload", wl,
-                   "--nx", str(nx), "--ny", str(ny), "--steps", str(steps), "--out", out]
+                   "--nx", str(nx), "--ny", str(ny), "--steps", str(steps), "--out", out, "--monitor", td]
             for k, v in extra.items():
                 cmd += [f"--{k}", str(v)]
             subprocess.run(cmd, check=True, cwd=ROOT, stdout=subprocess.DEVNULL)
             data = dict(np.load(out))
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
         manifest[name] = {"workload": wl, "nx": nx, "ny": ny, "steps": steps, **extra,
-                          "source": "reference time-step sources + single-rank stand-ins (oracle/_ref)"}
+                          "source": "reference time-step, logging, statistics and file-layer sources + "
+                                    "single-rank stand-ins (oracle/_ref)"}
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
 
