@@ -200,11 +200,14 @@ int sbfs_statistics_output(const char dirname[], const domain_t *domain);
  *   scalars device array of SBFS_STEP_SCALARS doubles; [0] receives dt
  *   status  device int; bit 0 is set when a velocity is not finite
  *   stream  the cudaStream_t to run on (NULL: the legacy default stream)
- * The result is ready when the stream reaches it.  The first call on each
- * GPU resolves the address of that GPU's scratch array (make it before any
- * stream capture).  Every call shares the one array: calls that overlap on
- * the GPU race and give wrong results.  nx > SBFS_NOALLOC_MAX_NX is rejected.
- * Message of the last failure: sbfs_noalloc_last_error(). */
+ * The result is ready when the stream reaches it.  Set-up: the first call on
+ * each GPU is where the CUDA runtime loads the library's device code there
+ * (lazy module loading), which places the code and the scratch array in
+ * device memory and may synchronise; make one warm-up call per GPU while
+ * initialising, before any stream capture.  Later calls allocate nothing.
+ * Every call shares the one array: calls that overlap on the GPU race and
+ * give wrong results.  nx > SBFS_NOALLOC_MAX_NX is rejected.  Message of the
+ * calling thread's last failure: sbfs_noalloc_last_error(). */
 #define SBFS_NOALLOC_MAX_NX 8192
 #define SBFS_STEP_SCALARS 64
 int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, const double *ux, const double *uy, int pitch,
