@@ -9,21 +9,34 @@ Bo = We = 5, Fr = 1, CFL 0.4.  A step is one full integrate(): decide_dt plus
 the three RK substages.  Metric: Mcell-steps/s = nx * ny * steps / s / 1e6.
 
 value : device-resident steps (state already in HBM), CUDA events on the
-        library's stream around K graph-launched steps; the ~0.5 GB working
+        library's stream around K graph-launched steps; the ~0.6 GB working
         set is larger than L2, so no flush is needed between steps.
-e2e   : the same metric through the drop-in C ABI, integrate() with host
-        (page-locked) buffers: every step uploads the state and writes it
-        back, as a reference caller sees it.
-roofline : the dominant kernel (largest share of a profiled step), its
-        algorithmic bytes per launch over its average duration, measured live
-        with CUDA events around each launch on the library's stream.
-cpu_baseline : the CPU port of the reference time step (oracle/, OpenMP over
-        all host cores) on a bounded sample of the same workload.
+e2e   : the same metric through the drop-in C ABI, integrate() on the
+        caller's own pageable host buffers, as a reference caller has them
+        (calloc): every step reads the state from the host and writes it
+        back.  The same with page-locked buffers is reported beside it.
+roofline : the dominant kernel (largest share of a profiled step) against
+        the FP64 pipe, which bounds this solver on GB300: its FP64 operations
+        per launch (ncu counts on this workload, profiles/kernel_traffic.txt)
+        over its average duration (CUDA events around each launch on the
+        library's stream), against the FP64 FMA rate measured live; its HBM
+        fraction (algorithmic bytes) beside it; step-wide figures too.
+cpu_baseline : the reference's own time-step sources (oracle/_ref, built on
+        this machine) as one single-thread process per host core, each
+        stepping the workload (the reference parallelises with MPI ranks
+        only, and there is no MPI here), on a bounded sample; the oracle's
+        OpenMP port and a single reference process are reported beside it.
+metric_arms : the metric's second form, FP64 plain against learned curvature
+        + batching, on the ensemble of 256 independent cases (three grids):
+        plain batched, learned + batched (the closure trained on the GPU
+        first) and plain one case at a time, with the static-drop curvature
+        error and parasitic velocity of plain and learned curvature.
 
---impl reference times that CPU implementation alone (rank 0; other ranks
-exit without work).  Multi-GPU (--gpus N under torchrun): independent
-replicas of the workload, one per GPU (the path has no exchange step on one
-GPU per case); value = all ranks' cell-steps / the slowest rank's time.
+--impl reference times the reference's own sources alone, as above (rank 0;
+other ranks exit without work).  Multi-GPU (--gpus N under torchrun):
+independent replicas of the workload, one per GPU (the path has no exchange
+step on one GPU per case); value = all ranks' cell-steps / the slowest
+rank's time.
 """
 from __future__ import annotations
 
@@ -46,7 +59,7 @@ TRAFFIC_FILE = os.path.join(ROOT, "profiles", "kernel_traffic.txt")
 HBM_FALLBACK_GBS = 6800.0
 
 # algorithmic bytes per cell and launch: every field a kernel reads or
-# writes counted once per cell (8 bytes per double); see the design doc
+# writes counted once per cell (8 bytes per double)
 ALG_DOUBLES_PER_CELL = {
     "k_props": 1 + 4,          # vof -> visux, visuy, dvof(2)
     "k_curv_list": 3 + 1,      # vof, dvof(2) -> curv (+ list of interface cells)
@@ -84,6 +97,9 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--curvature", choices=("plain", "learned"), default="plain",
                     help="learned: train the closure on the GPU first, then time the step with it")
+    ap.add_argument("--no-arms", action="store_true", help="skip the metric's learned + batched arm")
+    ap.add_argument("--ref-seconds", type=float, default=30.0,
+                    help="timed seconds per process of the reference arm")
     return ap.parse_args()
 
 
@@ -209,28 +225,52 @@ def make_state(wl, backend):
     return st
 
 
-def cpu_run(wl, steps, seconds_cap, warmup=1):
-    """the CPU port of the reference (oracle/) with all host cores: `warmup`
-    untimed steps (first touch, caches), then up to `steps` timed ones within
-    seconds_cap; returns (Mcell-steps/s, threads, steps done, seconds)"""
+def time_cpu(backend, workload, procs, seconds, steps, warmup, threads=1, nx=2048, ny=1024, nbubbles=64,
+             cases=256):
+    """one run of oracle.time_ref in its own process tree (the reference keeps
+    per-grid static state, so it never runs in this process); returns its
+    JSON result"""
+    cmd = [sys.executable, "-m", "oracle.time_ref", "--backend", backend, "--workload", workload,
+           "--nx", str(nx), "--ny", str(ny), "--nbubbles", str(nbubbles), "--cases", str(cases),
+           "--steps", str(steps), "--warmup", str(warmup), "--seconds", str(seconds),
+           "--threads", str(threads), "--procs", str(procs)]
+    r = subprocess.run(cmd, cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle.time_ref failed ({r.returncode}): {' '.join(cmd)}")
+    for line in reversed(r.stdout.splitlines()):
+        if line.startswith("{"):
+            return json.loads(line)
+    raise RuntimeError("oracle.time_ref printed no result")
+
+
+def cpu_baseline(args, seconds, steps, warmup):
+    """the reference's own sources on every host core (one single-thread
+    process per core), beside one reference process and the OpenMP port;
+    the port alone when the reference could not be built here"""
     import oracle
-    orc = oracle.Oracle()
-    orc.set_threads(os.cpu_count() or 1)
-    orc.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
-    st = make_state(wl, orc)
-    t0 = time.perf_counter()
-    for _ in range(max(1, warmup)):
-        orc.integrate(st)
-        if time.perf_counter() - t0 > seconds_cap / 4:
-            break
-    done, t0 = 0, time.perf_counter()
-    while done < steps:
-        orc.integrate(st)
-        done += 1
-        if time.perf_counter() - t0 > seconds_cap:
-            break
-    el = time.perf_counter() - t0
-    return wl.cells * done / el / 1e6, orc.threads(), done, el
+    wname = args.workload if args.workload != "swarm" else "swarm"
+    kw = dict(nx=args.nx if args.workload != "static_drop" else args.n, ny=args.ny, nbubbles=args.bubbles,
+              cases=args.cases)
+    cores = os.cpu_count() or 1
+    port = time_cpu("oracle", wname, 1, seconds / 2, steps, warmup, threads=cores, **kw)
+    side = {"port_openmp": {"value": round(port["value"], 4), "threads": port["threads"],
+                            "sample": f"{port['steps']} steps, {port['seconds']:.1f} s"}}
+    if not oracle.ref_available():
+        return {"value": round(port["value"], 4), "unit": METRIC, "cores": port["threads"], "kind": "port",
+                "sample": f"{port['steps']} steps of the workload, {port['seconds']:.1f} s (OpenMP over every "
+                          f"core; the reference's own sources were not built on this machine)"}, side
+    many = time_cpu("ref", wname, cores, seconds, steps, warmup, **kw)
+    one = time_cpu("ref", wname, 1, seconds, steps, warmup, **kw)
+    side["reference_one_process"] = {"value": round(one["value"], 4), "cores": 1,
+                                     "sample": f"{one['steps']} steps, {one['seconds']:.1f} s"}
+    what = ("one case each (cases spread over the ensemble)" if wname == "ensemble" else
+            "each stepping the whole workload")
+    base = {"value": round(many["value"], 4), "unit": METRIC, "cores": cores, "kind": "reference",
+            "sample": f"{cores} independent single-thread processes of the reference's own time-step sources "
+                      f"(oracle/_ref built here; no MPI on this machine), {what}: at least {many['steps']} "
+                      f"timed steps each after {warmup} untimed, {many['seconds']:.1f} s; aggregate cell-steps "
+                      f"over the slowest process's time"}
+    return base, side
 
 
 def load_traffic():
@@ -252,53 +292,23 @@ def ensemble_config(wls, ws):
             "l2": "working set (~4 GB) larger than L2, no flush"}
 
 
-def cpu_ensemble(wls, seconds_cap):
-    """the CPU port on every 8th case (one warm step, then timed steps until
-    the cap); returns (Mcell-steps/s, threads, case-steps, seconds)"""
-    import oracle
-    orc = oracle.Oracle()
-    orc.set_threads(os.cpu_count() or 1)
-    orc.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
-    sample = wls[::8]
-    sts = [make_state(w, orc) for w in sample]
-    for st in sts:
-        orc.integrate(st)
-    cells, done, t0 = 0, 0, time.perf_counter()
-    while time.perf_counter() - t0 < seconds_cap:
-        for w, st in zip(sample, sts):
-            orc.integrate(st)
-            cells += w.cells
-            done += 1
-    el = time.perf_counter() - t0
-    return cells / el / 1e6, orc.threads(), done, el
-
-
 def reference_arm(args, ws, rank):
+    """--impl reference: the reference's own sources on every host core"""
     if rank != 0:
         return
+    # W untimed steps (at most two: the reference takes about a second a step
+    # on the swarm), then up to K timed steps within --ref-seconds per process
+    base, side = cpu_baseline(args, args.ref_seconds, args.steps, min(args.warmup, 2))
     if args.workload == "ensemble":
         from simplebubblyflowsolver_gb300 import ic
-        wls = ic.ensemble(args.cases, seed=0)
-        val, threads, done, el = cpu_ensemble(wls, seconds_cap=60.0)
-        line = {"metric": METRIC, "value": round(val, 4), "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
-                "steps": done, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": ensemble_config(wls, 1),
-                "cpu_baseline": {"value": round(val, 4), "unit": METRIC, "cores": threads, "kind": "port",
-                                 "sample": f"{done} case-steps over every 8th case, {el:.1f} s"},
-                "e2e": {"value": round(val, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
-    wl = workload(args)
-    # W untimed steps, then K timed steps, capped so the run stays within minutes
-    val, threads, done, el = cpu_run(wl, args.steps, seconds_cap=180.0, warmup=args.warmup)
-    line = {"metric": METRIC, "value": round(val, 4), "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
-            "steps": done, "warmup": args.warmup, "ms_per_step": round(1e3 * el / done, 3), "higher_is_better": True,
+        cfg = ensemble_config(ic.ensemble(args.cases, seed=0), 1)
+    else:
+        cfg = config_of(workload(args), args, 1)
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_of(wl, args, 1),
-            "cpu_baseline": {"value": round(val, 4), "unit": METRIC, "cores": threads, "kind": "port",
-                             "sample": f"{done} timed full steps of the workload after {args.warmup} untimed "
-                                       f"(timed part capped at 180 s)"},
-            "e2e": {"value": round(val, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": dict(cfg, curvature=args.curvature), "cpu_baseline": base, "cpu_other": side,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -346,67 +356,162 @@ def main():
 
     # ---- per-kernel shares and the dominant kernel (eager launches, events)
     prof = lib.profile_steps(st, args.profile_steps)
-    total = sum(v[0] for v in prof.values())
-    dom = max(prof, key=lambda k: prof[k][0])
-    dom_ms, dom_n = prof[dom]
-    dom_avg_s = dom_ms / dom_n / 1e3
-    alg_bytes = ALG_DOUBLES_PER_CELL[dom] * 8 * cells
-    achieved = alg_bytes / dom_avg_s / 1e9
-    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
-    hbm_peak = peaks.get("hbm_gbs", HBM_FALLBACK_GBS)
-    tr = load_traffic().get((dom, f"{wl.nx}x{wl.ny}"))
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(achieved / hbm_peak, 4), "traffic": tr["traffic"] if tr else None,
-                "peak_source": "measured" if peaks else "fallback",
-                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": round(dom_avg_s * 1e3, 4),
-                "share": round(dom_ms / total, 4),
-                "shares": {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
-    fp64_peak = lib.measure_fp64_peak()
-    roofline["fp64_peak_gflops"] = round(fp64_peak, 1)
-    if tr and tr.get("fp64_flop"):
-        ach = tr["fp64_flop"] / dom_avg_s / 1e9
-        roofline["fp64"] = {"achieved": round(ach, 1), "peak": round(fp64_peak, 1), "unit": "GFLOP/s",
-                            "frac": round(ach / fp64_peak, 4),
-                            "peak_source": "measured live: FMA loop (sbfs_measure_fp64_peak)",
-                            "flop_source": "ncu sass FP64 instruction counts (profiles/kernel_traffic.txt)"}
+    roofline = roofline_of(prof, lib, cells, f"{wl.nx}x{wl.ny}", t_max * 1e3 / args.steps)
 
-    # ---- end to end through integrate() with page-locked host buffers
+    # ---- end to end through integrate(): the caller's own pageable buffers
+    # (as the reference's calloc leaves them), then page-locked ones
     lib.set_sync_mode(SYNC_STATE)
-    lib.pin_host_state(st)
-    for _ in range(2):
-        lib.integrate(st)
     ne = min(args.e2e_steps, args.steps)
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(ne):
-        lib.integrate(st)
-    t_e2e = dist.max(time.perf_counter() - t0)
+    t_pageable = e2e_time(lib, st, ne, dist)
+    lib.pin_host_state(st)
+    t_pinned = e2e_time(lib, st, ne, dist)
     lib.unpin_host_state(st)
     state_bytes = sum(st.interior_rows(s).nbytes for s in ("ux", "uy", "p", "psi0", "vof"))
     h2d = state_bytes
     d2h = state_bytes + st.interior_rows("psi1").nbytes + 8 * 33
-    e2e = {"value": round(ws * cells * ne / t_e2e / 1e6, 4), "unit": METRIC, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "steps": ne}
+    e2e = {"value": round(ws * cells * ne / t_pageable / 1e6, 4), "unit": METRIC, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "steps": ne, "host_buffers": "pageable (the caller's own)",
+           "pinned": round(ws * cells * ne / t_pinned / 1e6, 4)}
 
-    # ---- CPU baseline (rank 0, N = 1 only)
-    cpu = None
+    # ---- CPU baseline (rank 0, N = 1 only), the GPU idle meanwhile
+    cpu, cpu_other = None, None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        per_step = cells / 15e6  # rough seconds per step to size the sample
-        n = max(2, int(args.cpu_sample_s / per_step))
-        val, threads, done, el = cpu_run(wl, n, seconds_cap=2 * args.cpu_sample_s)
-        cpu = {"value": round(val, 4), "unit": METRIC, "cores": threads, "kind": "port",
-               "sample": f"{done} full steps of the same workload, {el:.1f} s"}
+        cpu, cpu_other = cpu_baseline(args, args.cpu_sample_s, max(args.steps, 2), 1)
+
+    # ---- the metric's second form (rank 0, N = 1 only)
+    arms = None
+    if rank == 0 and ws == 1 and not args.no_arms and args.workload == "swarm":
+        arms = metric_arms(args, lib)
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(config_of(wl, args, ws), curvature=args.curvature), "e2e": e2e, "roofline": roofline,
-                "cpu_baseline": cpu, "learned_curvature": learned, "tiles": lib.tiles(),
-                "clocks": clocks, "gpu_launches": lib.kernels_per_step() * args.steps,
+                "cpu_baseline": cpu, "cpu_other": cpu_other, "metric_arms": arms, "learned_curvature": learned,
+                "tiles": lib.tiles(), "clocks": clocks, "gpu_launches": lib.kernels_per_step() * args.steps,
                 "dt_last": dt_last}
         print(json.dumps(line), flush=True)
     dist.close()
+
+
+def e2e_time(lib, st, n, dist):
+    """seconds of n integrate() calls on the host state, after two untimed"""
+    for _ in range(2):
+        lib.integrate(st)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        lib.integrate(st)
+    return dist.max(time.perf_counter() - t0)
+
+
+def roofline_of(prof, lib, cells, grid, step_ms):
+    """roofline of the dominant kernel against the FP64 pipe (what bounds this
+    solver on GB300) with its HBM fraction beside it, and step-wide figures.
+    prof: {kernel: (ms, launches)} of profiled eager steps.  FP64 operations
+    and DRAM bytes per launch are ncu counts on this grid
+    (profiles/kernel_traffic.txt); the FP64 rate is measured live."""
+    total = sum(v[0] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    dom_avg_s = dom_ms / dom_n / 1e3
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    hbm_peak = peaks.get("hbm_gbs", HBM_FALLBACK_GBS)
+    fp64_peak = lib.measure_fp64_peak()
+    traffic = {k: v for (k, g), v in load_traffic().items() if g == grid}
+    tr = traffic.get(dom)
+    alg_bytes = ALG_DOUBLES_PER_CELL[dom] * 8 * cells
+    hbm = {"achieved": round(alg_bytes / dom_avg_s / 1e9, 1), "peak": hbm_peak, "unit": "GB/s",
+           "frac": round(alg_bytes / dom_avg_s / 1e9 / hbm_peak, 4), "alg_bytes_per_launch": alg_bytes,
+           "peak_source": "measured" if peaks else "fallback"}
+    out = {"bound": "fp64", "kernel": dom, "achieved": None, "peak": round(fp64_peak, 1), "unit": "GFLOP/s",
+           "frac": None, "traffic": tr["traffic"] if tr else None, "fp64_flop_per_launch": None,
+           "peak_source": "measured live: FP64 FMA loop on this GPU (sbfs_measure_fp64_peak), of measured",
+           "flop_source": "ncu DADD + DMUL + 2 DFMA thread instructions on this grid (profiles/kernel_traffic.txt)",
+           "avg_launch_ms": round(dom_avg_s * 1e3, 4), "share": round(dom_ms / total, 4), "hbm": hbm,
+           "shares": {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+    if tr:
+        ach = tr["fp64_flop"] / dom_avg_s / 1e9
+        out.update(achieved=round(ach, 1), frac=round(ach / fp64_peak, 4), fp64_flop_per_launch=tr["fp64_flop"])
+    # step-wide: every launch class of a step (decide_dt once, the rest three times)
+    if traffic and all(k in traffic for k, v in prof.items() if v[1] > 0):
+        per = {k: v[1] / max(1, prof["k_decide_dt"][1]) for k, v in prof.items() if v[1] > 0}
+        flop = sum(traffic[k]["fp64_flop"] * n for k, n in per.items())
+        out["step"] = {"fp64_flop_per_cell_step": round(flop / cells, 1),
+                       "fp64_frac": round(flop / (step_ms / 1e3) / 1e9 / fp64_peak, 4),
+                       "fused_hbm_frac": round(720.0 * cells / (step_ms / 1e3) / 1e9 / hbm_peak, 4),
+                       "dram_bytes_per_cell_step": round(sum(traffic[k]["traffic"] * n for k, n in per.items())
+                                                         / cells, 1),
+                       "note": "fp64_frac: the step's FP64 operations (ncu) over its device time and the live FMA "
+                               "rate; fused_hbm_frac: 720 B per cell-step (the fused-minimum dataflow) over the "
+                               "measured HBM bandwidth"}
+    return out
+
+
+def metric_arms(args, lib):
+    """FP64 plain against learned curvature + batching on the ensemble of 256
+    independent cases (three grids, random physics), and what the closure
+    does to the static drop's curvature error and parasitic currents"""
+    from simplebubblyflowsolver_gb300 import SYNC_NONE, ic
+    from simplebubblyflowsolver_gb300 import learned_curvature as L
+    wls = ic.ensemble(args.cases, seed=0)
+    cells = sum(w.cells for w in wls)
+    lib.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
+    lib.set_sync_mode(SYNC_NONE)
+    steps, warm = max(args.steps, 10), max(args.warmup, 3)
+
+    def batched(model):
+        # (training and the static drops set their own dt factors and modes)
+        lib.set_dt_coefs(wls[0].coef_dt_adv, wls[0].coef_dt_dif, wls[0].coef_dt_int)
+        lib.set_sync_mode(SYNC_NONE)
+        lib.set_curvature_model(model)
+        sts = [make_state(w, lib) for w in wls]
+        lib.integrate_batch(sts)
+        lib.run_batch_steps_timed(warm)
+        ms = lib.run_batch_steps_timed(steps)
+        lib.batch_release()
+        return cells * steps / (ms / 1e3) / 1e6
+
+    plain = batched(0)
+    # one case at a time: the step time of four cases of each grid alone,
+    # scaled to the ensemble's case count per grid
+    per_grid = {}
+    for w in wls:
+        key = (w.nx, w.ny)
+        if len(per_grid.setdefault(key, [])) < 4:
+            st = make_state(w, lib)
+            lib.invalidate_device()
+            lib.run_steps_timed(st, warm)
+            ms, _ = lib.run_steps_timed(st, steps)
+            per_grid[key].append(ms / steps)
+    one_ms = sum(sum(per_grid[(w.nx, w.ny)]) / len(per_grid[(w.nx, w.ny)]) for w in wls)
+    t0 = time.perf_counter()
+    _, params, hist = L.train_default(lib, seed=0)
+    train_s = time.perf_counter() - t0
+    lib.mlp_set_params(params)
+    learned = batched(1)
+    lib.set_curvature_model(0)
+    drop = {}
+    nsteps = 500
+    for name, model in (("plain", 0), ("learned", 1)):
+        r = L.evaluate_static_drop(lib, n=64, steps=nsteps, model=model, params=params if model else None,
+                                   record_every=50)
+        drop[name] = {"kappa_rms_rel_err": round(r["kappa_rms_rel_err"], 4),
+                      "umax_mean": float(np.mean([h[2] for h in r["umax_history"]])),
+                      "laplace_dp_rel_err": round(r["dp_rel_err"], 4)}
+    lib.set_sync_mode(SYNC_NONE)
+    return {"workload": f"ensemble_{len(wls)} (grids ny x nx 64x128, 128x256, 256x512; seed 0)",
+            "plain_batched": round(plain, 3), "learned_batched": round(learned, 3),
+            "plain_one_at_a_time": round(cells / one_ms * 1e3 / 1e6, 3),
+            "learned_batched_over_plain_one_at_a_time": round(learned / (cells / one_ms * 1e3 / 1e6), 3),
+            "learned_batched_over_plain_batched": round(learned / plain, 4),
+            "steps": steps, "train_s": round(train_s, 1), "train_final_loss": hist[-1],
+            "static_drop_64": dict(drop, steps=nsteps, note="kappa: rms relative error of the curvature the "
+                                   "last substage used in the interface cells (exact 1/r = 4); umax_mean: "
+                                   "max |u| sampled every 50 steps, averaged (parasitic currents)"),
+            "one_at_a_time_note": "device-resident steps of four cases of each grid alone (CUDA events), "
+                                  "their mean step time times the ensemble's cases on that grid"}
 
 
 def run_ensemble(args, lib, dist, ws, rank, local, learned=None):
@@ -441,38 +546,47 @@ def run_ensemble(args, lib, dist, ws, rank, local, learned=None):
     achieved = alg_total / (dom_ms / 1e3) / 1e9
     peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
     hbm_peak = peaks.get("hbm_gbs", HBM_FALLBACK_GBS)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(achieved / hbm_peak, 4), "traffic": None,
-                "peak_source": "measured" if peaks else "fallback",
-                "alg_bytes_per_launch": round(alg_total / dom_n),
+    # the FP64 pipe bounds the step; ncu FP64 counts exist for the swarm
+    # grid only, so this line carries the dominant class's HBM fraction
+    roofline = {"bound": "fp64", "kernel": dom, "achieved": None, "peak": round(lib.measure_fp64_peak(), 1),
+                "unit": "GFLOP/s", "frac": None, "traffic": None,
+                "peak_source": "measured live: FP64 FMA loop on this GPU, of measured",
                 "avg_launch_ms": round(dom_ms / dom_n, 4), "share": round(dom_ms / total, 4),
-                "shares": {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
-                "note": "all cases of the dominant kernel class per step / summed event time of its launches"}
-    roofline["fp64_peak_gflops"] = round(lib.measure_fp64_peak(), 1)
+                "hbm": {"achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                        "frac": round(achieved / hbm_peak, 4), "alg_bytes_per_launch": round(alg_total / dom_n),
+                        "peak_source": "measured" if peaks else "fallback",
+                        "note": "all cases of the dominant kernel class per step / summed event time of its "
+                                "launches"},
+                "shares": {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
 
-    # end to end: sbfs_integrate_batch with page-locked host state of every case
+    # end to end: sbfs_integrate_batch on the cases' own pageable host state,
+    # then page-locked
     lib.set_sync_mode(SYNC_STATE)
+    ne = max(2, min(args.e2e_steps, args.steps) // 10)
+
+    def batch_e2e():
+        lib.integrate_batch(sts)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            lib.integrate_batch(sts)
+        return dist.max(time.perf_counter() - t0)
+
+    t_e2e = batch_e2e()
     for st in sts:
         lib.pin_host_state(st)
-    lib.integrate_batch(sts)
-    ne = max(2, min(args.e2e_steps, args.steps) // 10)
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(ne):
-        lib.integrate_batch(sts)
-    t_e2e = dist.max(time.perf_counter() - t0)
+    t_pinned = batch_e2e()
     for st in sts:
         lib.unpin_host_state(st)
     h2d = sum(sum(st.interior_rows(s).nbytes for s in ("ux", "uy", "p", "psi0", "vof")) for st in sts)
     d2h = h2d + sum(st.interior_rows("psi1").nbytes for st in sts) + len(sts) * 8 * 65
     e2e = {"value": round(ws * cells * ne / t_e2e / 1e6, 4), "unit": METRIC, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "steps": ne}
+           "d2h_bytes_per_step": d2h, "steps": ne, "host_buffers": "pageable (the caller's own)",
+           "pinned": round(ws * cells * ne / t_pinned / 1e6, 4)}
 
-    cpu = None
+    cpu, cpu_other = None, None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        val, threads, done, el = cpu_ensemble(wls, seconds_cap=args.cpu_sample_s)
-        cpu = {"value": round(val, 4), "unit": METRIC, "cores": threads, "kind": "port",
-               "sample": f"{done} case-steps over every 8th case, {el:.1f} s"}
+        cpu, cpu_other = cpu_baseline(args, args.cpu_sample_s, max(args.steps, 2), 1)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 4), "higher_is_better": True,
@@ -480,7 +594,7 @@ def run_ensemble(args, lib, dist, ws, rank, local, learned=None):
                 "config": dict(ensemble_config(wls, ws), groups=groups, curvature=args.curvature),
                 "e2e": e2e, "roofline": roofline, "learned_curvature": learned,
                 "tiles": [lib.tiles(q) for q in range(len(groups))],
-                "cpu_baseline": cpu, "clocks": clocks,
+                "cpu_baseline": cpu, "cpu_other": cpu_other, "clocks": clocks,
                 "gpu_launches": lib.kernels_per_step() * len(groups) * args.steps}
         print(json.dumps(line), flush=True)
     lib.batch_release()

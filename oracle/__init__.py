@@ -23,12 +23,23 @@ ORACLE_FMA_SO = os.path.join(HERE, "liboracle_fma.so")
 REF_SO = os.path.join(HERE, "_ref", "libsbfs_ref.so")
 
 
+STAGED = os.path.join(HERE, "_ref", "src")
+
+
 def build(ref_dir: str | None = None, quiet: bool = True) -> None:
-    """compile liboracle.so, and _ref/libsbfs_ref.so when ref_dir exists"""
+    """compile liboracle.so, and _ref/libsbfs_ref.so: from ref_dir when it
+    holds the reference checkout (whose sources are then also staged into
+    _ref/src, git-ignored, so that a machine without the checkout can build
+    the same library), else from a staged copy when there is one"""
     out = subprocess.DEVNULL if quiet else None
+    err = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "liboracle.so", "liboracle_fma.so"], check=True, stdout=out)
     if ref_dir and os.path.isdir(os.path.join(ref_dir, "src")):
-        subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_dir}"], check=True, stdout=out)
+        ref_dir = os.path.abspath(ref_dir)
+        subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_dir}"], check=True, stdout=out, stderr=err)
+        subprocess.run(["make", "-C", HERE, "stage", f"REF={ref_dir}"], check=True, stdout=out, stderr=err)
+    elif os.path.isdir(os.path.join(STAGED, "src")):
+        subprocess.run(["make", "-C", HERE, "ref", f"REF={STAGED}"], check=True, stdout=out, stderr=err)
 
 
 class Oracle(ReferenceAPI):

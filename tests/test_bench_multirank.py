@@ -64,5 +64,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1, r.stdout
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
-    assert line["cpu_baseline"]["kind"] == "port"
+    # the reference's own sources where they were built here, else the port
+    assert line["cpu_baseline"]["kind"] == ("reference" if oracle.ref_available() else "port")
+    assert line["config"]["curvature"] == "plain"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
