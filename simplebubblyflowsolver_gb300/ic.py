@@ -228,3 +228,76 @@ def save_ic(dirname: str, fields: dict):
 def load_ic(dirname: str) -> dict:
     names = ("step", "time", "xf", "xc", "glsizes", "lengths", "vof", "ux", "uy", "p", "psi")
     return {k: np.load(os.path.join(dirname, f"{k}.npy")) for k in names}
+
+
+def reference_bubble(nx, ny, lx=4.0, ly=2.0) -> Workload:
+    """The reference generator's case (initial_condition/main.py:27-45): one
+    bubble of diameter 1 centred at (1, 1), here as exact cell area fractions
+    instead of the reference's tanh profile; physics of exec/main.sh
+    (Re 35, We 10, Fr 1, density ratio 0.0013, viscosity ratio 0.018, CFL
+    0.2)."""
+    return Workload("reference_bubble", nx, ny, lx, ly, [(1.0, 1.0, 0.5)], Re=35.0, We=10.0, Fr=1.0,
+                    denr=0.0013, visr=0.018, coef_dt_adv=0.2)
+
+
+def main(argv=None):
+    """Command-line generator, the counterpart of the reference's
+    initial_condition/main.sh + main.py: writes step, time, xf, xc, glsizes,
+    lengths, vof, ux, uy, p and psi into DIR (the reference's schema, which
+    its domain_init / fluid_init / interface_init and this library's read)
+    and prints the environment the solver reads for the case's physics
+    (Re, We, Fr, denr, visr and the dt safety factors), as export lines.
+
+        python -m simplebubblyflowsolver_gb300.ic DIR
+            the reference's case on the grid of the environment variables
+            lx, ly, glisize, gljsize (those initial_condition/main.sh sets)
+        python -m simplebubblyflowsolver_gb300.ic DIR --workload swarm --nx 2048 --ny 1024 --bubbles 64 --seed 0
+        python -m simplebubblyflowsolver_gb300.ic DIR --workload single_bubble --nx 256 --ny 128
+        python -m simplebubblyflowsolver_gb300.ic DIR --workload static_drop --nx 64
+        python -m simplebubblyflowsolver_gb300.ic DIR --workload ensemble_case --case 17 --seed 0
+    """
+    import argparse
+    ap = argparse.ArgumentParser(prog="python -m simplebubblyflowsolver_gb300.ic",
+                                 description="initial condition in the reference's .npy schema")
+    ap.add_argument("dirname")
+    ap.add_argument("--workload", default="reference",
+                    choices=("reference", "single_bubble", "swarm", "static_drop", "ensemble_case"))
+    ap.add_argument("--nx", type=int, default=None)
+    ap.add_argument("--ny", type=int, default=None)
+    ap.add_argument("--bubbles", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--case", type=int, default=0, help="ensemble_case: which of the ensemble's cases")
+    ap.add_argument("--cases", type=int, default=256)
+    ap.add_argument("--env-file", default=None, help="also write the export lines to this file")
+    a = ap.parse_args(argv)
+    if a.workload == "reference":
+        try:
+            lx, ly = float(os.environ["lx"]), float(os.environ["ly"])
+            nx = int(os.environ["glisize"]) if a.nx is None else a.nx
+            ny = int(os.environ["gljsize"]) if a.ny is None else a.ny
+        except KeyError as e:
+            ap.error(f"environment variable {e.args[0]} not set (initial_condition/main.sh sets lx, ly, "
+                     "glisize, gljsize)")
+        wl = reference_bubble(nx, ny, lx, ly)
+    elif a.workload == "single_bubble":
+        wl = single_bubble(a.nx or 256, a.ny or 128)
+    elif a.workload == "swarm":
+        wl = bubble_swarm(a.nx or 2048, a.ny or 1024, nbubbles=a.bubbles, seed=a.seed)
+    elif a.workload == "static_drop":
+        wl = static_drop(a.nx or 64)
+    else:
+        cases = ensemble(a.cases, seed=a.seed)
+        if not 0 <= a.case < len(cases):
+            ap.error(f"--case must be in 0..{len(cases) - 1}")
+        wl = cases[a.case]
+    save_ic(a.dirname, wl.fields())
+    lines = [f"export {k}={v}" for k, v in wl.env().items()]
+    if a.env_file:
+        with open(a.env_file, "w") as fh:
+            fh.write("\n".join(lines) + "\n")
+    print("\n".join(lines))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -160,3 +160,35 @@ def test_oracle_logging_reductions_match_the_reference_logs():
         assert abs(got["vof_integral"] / got["volume"] - vmean) <= 1e-14 * abs(vmean)
         assert abs(got["interface_area"] - area) <= 1e-14 * abs(area)
         assert float(f"{got['divmax']:.1e}") == last["divergence"][0], (name, got["divmax"], last["divergence"])
+
+
+def test_command_line_generator_writes_what_the_reference_reads(libs, tmp_path):
+    """python -m simplebubblyflowsolver_gb300.ic, driven like the reference's
+    initial_condition/main.sh (lx, ly, glisize, gljsize in the environment):
+    the directory holds the reference's schema, step and time included, and
+    the reference's init and the library's load it to the same arrays"""
+    import subprocess
+    import sys
+    ours, ref = libs
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    d = tmp_path / "ic"
+    env = dict(os.environ, lx="4.0", ly="2.0", glisize="64", gljsize="32", PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-m", "simplebubblyflowsolver_gb300.ic", str(d)], env=env, cwd=str(tmp_path),
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    exports = dict(line[len("export "):].split("=", 1) for line in r.stdout.splitlines())
+    assert sorted(exports) == sorted(["Re", "We", "Fr", "denr", "visr", "coef_dt_adv", "coef_dt_dif", "coef_dt_int"])
+    assert np.load(d / "step.npy").dtype == np.uint64 and int(np.load(d / "step.npy")) == 0
+    assert np.load(d / "time.npy").dtype == np.float64 and float(np.load(d / "time.npy")) == 0.0
+    vof = np.load(d / "vof.npy")
+    assert vof.shape == (32, 66) and abs(vof.sum() * (4.0 / 64) * (2.0 / 32) - np.pi / 4) < 1e-12
+    for k, v in exports.items():
+        os.environ[k] = v
+    a, b = arrays(load(ours, str(d))), arrays(load(ref, str(d)))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    # a missing environment key is reported, as the reference's script needs them
+    env.pop("glisize")
+    r = subprocess.run([sys.executable, "-m", "simplebubblyflowsolver_gb300.ic", str(tmp_path / "x")], env=env,
+                       cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode != 0 and "glisize" in r.stderr
