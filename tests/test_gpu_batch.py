@@ -200,3 +200,80 @@ def test_batch_compaction_gives_identical_steps(libs):
     for k, (x, y) in enumerate(zip(runs[0][1], runs[1][1])):
         for s in SLOTS:
             assert np.array_equal(x.field(s), y.field(s)), (k, s)
+
+
+def ensemble_extremes():
+    """from the benchmarked ensemble (256 cases, seed 0), on each of its three
+    grids: the case with the lowest density ratio (down to 1e-3), the one
+    with the highest We and the one with the lowest We (strongest surface
+    tension)"""
+    wls = ic.ensemble(256, seed=0)
+    out = []
+    for g in ic.ENSEMBLE_GRIDS:
+        on = [w for w in wls if (w.nx, w.ny) == g]
+        picks = [min(on, key=lambda w: w.denr), max(on, key=lambda w: w.We), min(on, key=lambda w: w.We)]
+        for w in picks:
+            if all(w is not p for p in out):
+                out.append(w)
+    return out
+
+
+@pytest.mark.gpu
+def test_batch_on_the_ensemble_grids_matches_oracle(libs):
+    """the 128 x 64, 256 x 128 and 512 x 256 groups of the benchmarked
+    ensemble, batched, against the oracle for five steps (the same bar as
+    test_batch_matches_oracle)"""
+    gpu, orc = libs
+    wls = ensemble_extremes()
+    assert {(w.nx, w.ny) for w in wls} == set(ic.ENSEMBLE_GRIDS)
+    assert min(w.denr for w in wls) < 1.1e-3 and max(w.We for w in wls) > 90
+    st0 = prepare(gpu, orc, wls)
+    batch = [clone(s) for s in st0]
+    ref = [clone(s) for s in st0]
+    steps = 5
+    try:
+        for _ in range(steps):
+            dts = gpu.integrate_batch(batch)
+            for k, st in enumerate(ref):
+                do = orc.integrate(st)
+                assert abs(dts[k] - do) <= 1e-10 * do, (k, dts[k], do)
+    finally:
+        gpu.batch_release()
+    for k, wl in enumerate(wls):
+        errs = compare_state(batch[k], ref[k])
+        tol = 1e-10
+        if max(errs.values()) > tol:
+            floor = max(max(fma_noise_floor(wl, steps).values()), max(rounding_sensitivity(wl, steps).values()))
+            tol = max(tol, 10 * floor)
+        print(k, (wl.nx, wl.ny), f"We={wl.We:.1f} Re={wl.Re:.1f} denr={wl.denr:.1e}",
+              {s: f"{v:.1e}" for s, v in errs.items()}, "tol", tol)
+        assert max(errs.values()) <= tol, (k, errs, tol)
+
+
+@pytest.mark.gpu
+def test_batch_learned_curvature_on_the_ensemble_grids(libs):
+    """the learned closure batched over the ensemble's three grids: each
+    case as it steps alone, bit for bit"""
+    from simplebubblyflowsolver_gb300 import learned_curvature as L
+    gpu, orc = libs
+    wls = ensemble_extremes()
+    st0 = prepare(gpu, orc, wls)
+    batch = [clone(s) for s in st0]
+    alone = [clone(s) for s in st0]
+    p = L.init_params(3)
+    p[-1] = 0.05  # a bias that puts many outputs inside the closure's range
+    gpu.mlp_set_params(p)
+    gpu.set_curvature_model(1)
+    try:
+        gpu.mlp_take_usage()
+        for _ in range(3):
+            dts = gpu.integrate_batch(batch)
+            for k, st in enumerate(alone):
+                assert gpu.integrate(st) == dts[k]
+        assert gpu.mlp_take_usage() > 0
+    finally:
+        gpu.set_curvature_model(0)
+        gpu.batch_release()
+    for k, (a, b) in enumerate(zip(batch, alone)):
+        for s in SLOTS:
+            assert np.array_equal(a.field(s), b.field(s)), (k, s)
