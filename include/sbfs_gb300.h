@@ -143,7 +143,10 @@ int sbfs_check_newton_raphson(const double *x, double *rcp, double *rsq, int n);
 int sbfs_set_device(int device);
 
 /* page-lock the state arrays integrate() copies (ux, uy, p, psi[0..1], vof)
- * so the host<->device copies run at full link speed; unpin before freeing */
+ * so the host<->device copies run at full link speed; unpin before freeing.
+ * A host-linked step captures its copies for the arrays' registration at the
+ * time; these two calls (and sbfs_invalidate_device, for arrays the caller
+ * registers or unregisters itself) make the next step look again. */
 int sbfs_pin_host_state(fluid_t *fluid, interface_t *interface);
 int sbfs_unpin_host_state(fluid_t *fluid, interface_t *interface);
 

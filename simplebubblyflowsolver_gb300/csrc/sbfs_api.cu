@@ -55,6 +55,9 @@ int g_use_graphs = 1;
 // without host page-table access), 0 = never
 int g_host_link = 1;
 bool g_link_used = false;  // the last integrate() did
+// bumped whenever the library pins or unpins host arrays (or the caller says
+// the host state changed): the registration of the linked arrays is looked at again
+unsigned g_reg_epoch = 0;
 double g_coef[3] = {-1., -1., -1.};
 
 // extra cells of every field (reference include/array_macros/)
@@ -98,10 +101,11 @@ struct Ctx {
   std::vector<double> graph_sig;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   // side stream of the step: decide_dt beside k_props and the interface
-  // kernels, the next substage's k_props beside the predictor, the Poisson
+  // kernels, the bulk fluxes and the force beside the listed interface
+  // faces, the next substage's k_props beside the predictor, the Poisson
   // solve and the correction (fork / join events)
   cudaStream_t s2 = nullptr;
-  cudaEvent_t evf = nullptr, evd = nullptr, evp = nullptr;
+  cudaEvent_t evf = nullptr, evd = nullptr, evp = nullptr, evx = nullptr;
   bool props_ahead = false;  // the next substage's k_props is already on the side stream
   // host-linked step (strict sync mode, host arrays the GPU can address): the
   // step copies the state in and out itself, on the copy stream s3, each
@@ -114,6 +118,12 @@ struct Ctx {
   cudaEvent_t evh[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // vof, velocity, p, psi in; fork
   double **link_tab = nullptr, **link_tab_dev = nullptr;
   std::vector<const void *> link_host;
+  // which of link_host are page-locked (bit per slot), for the arrays and the
+  // registration epoch it was found for: a captured copy-engine copy depends on
+  // it, so a linked graph is captured again when it changes
+  std::vector<const void *> link_prev;
+  unsigned link_epoch = ~0u;
+  uintptr_t link_reg = 0;
   std::map<int, std::vector<const void *>> graph_hosts;
   // diagnostics partials / result and statistics sums (allocated on first use)
   double *diag_part = nullptr, *diag_out = nullptr;
@@ -129,6 +139,7 @@ struct Ctx {
     if (evf) cudaEventDestroy(evf);
     if (evd) cudaEventDestroy(evd);
     if (evp) cudaEventDestroy(evp);
+    if (evx) cudaEventDestroy(evx);
     for (cudaEvent_t e : evh)
       if (e) cudaEventDestroy(e);
     if (link_tab) cudaFreeHost(link_tab);
@@ -441,6 +452,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   CK(cudaEventCreateWithFlags(&c->evf, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->evx, cudaEventDisableTiming));
   CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
   for (cudaEvent_t &e : c->evh) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CK(cudaHostAlloc(reinterpret_cast<void **>(&c->link_tab), sizeof(double *) * kLinkSlots * nc, cudaHostAllocMapped));
@@ -469,6 +481,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   g.cs3 = n3;
   g.css = (size_t)c->nx * M1;
   g.cm = 0;
+  g.ct = rnd(c->nx + 2);
   g.phys = nullptr;
   Bufs &b = c->b;
   b.tiles = default_tiles(c->ny);
@@ -507,6 +520,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   if (dalloc(*c, &tmp, (size_t)kScalars * nc + nc / 2 + 2)) return 1;
   b.scalars = tmp;
   b.status = reinterpret_cast<int *>(tmp + (size_t)kScalars * nc);
+  if (dalloc(*c, &b.coltab, (size_t)3 * kColTabs * g.ct * nc)) return 1;
   CK(cudaMallocHost(&c->small_host, sizeof(double) * ((size_t)kScalars * nc + nc / 2 + 2)));
   if (nc > 1) {
     void *q = nullptr;
@@ -588,6 +602,20 @@ int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
     h[sc_cold(0)] = -dt_old * c.ph.irefden;
     h[sc_cnewy(0)] = h[sc_cnew(0)] * g.ihy;
     h[sc_coldy(0)] = h[sc_cold(0)] * g.ihy;
+    h[sc_coldyp(0)] = h[sc_coldy(0)] / h[sc_pay(0)];
+    h[sc_rpx(0)] = c.ph.rref2 * h[sc_pax(0)];
+    h[sc_rpy(0)] = c.ph.rref2 * h[sc_pay(0)];
+    // the correction's per-column coefficients of slot 0, as k_decide_dt
+    // writes them for the fused step
+    std::vector<double> ct(2 * (size_t)g.ct, 0.);
+    for (int I = 1; I <= c.nx + 1; ++I) {
+      const double ih = 1. / c.hxxf[I - 1];
+      ct[I] = h[sc_cnew(0)] * ih;
+      ct[g.ct + I] = h[sc_cold(0)] * ih / h[sc_pax(0)];
+    }
+    CK(cudaMemcpyAsync(c.b.coltab + (size_t)ct_cnewx(0) * g.ct, ct.data(), sizeof(double) * ct.size(),
+                       cudaMemcpyHostToDevice, c.s));
+    CK(cudaStreamSynchronize(c.s));  // ct dies here
   }
   CK(cudaMemcpyAsync(c.b.scalars, h, sizeof(double) * kScalars, cudaMemcpyHostToDevice, c.s));
   // h is reused by the next call: wait for the copy
@@ -685,9 +713,13 @@ void link_dma(Ctx &c, bool in, int slot, const Layout &l, double *dev) {
   }
 }
 
-// a copy beside the step's kernels, on the copy stream
+// a copy beside the step's kernels, on the copy stream: by copy engine for a
+// single case's page-locked array; by a narrow copy kernel for a batch (one
+// launch for all its cases) and for pageable arrays, which the copy engines
+// move with a fixed cost of several microseconds per call (13 calls a step
+// with the ghost rows)
 void link_side(Ctx &c, bool in, int slot, const Layout &l, double *dev) {
-  if (c.nc == 1)
+  if (c.nc == 1 && ((c.link_reg >> slot) & 1))
     link_dma(c, in, slot, l, dev);
   else
     launch_host_rows(c.s3, c.g, c.link_tab_dev, in, host_rows(c, slot, l, dev), HostRows{}, 1, kLinkNarrow);
@@ -722,7 +754,8 @@ void link_out(Ctx &c, int slot, const Layout &l, double *dev) {
 }
 
 // par: decide_dt runs on the side stream (forked by enqueue_step, joined
-// before the first use of its scalars when wait_dt), and so does the next
+// before the first use of its scalars when wait_dt), and so do the bulk
+// fluxes and the force (beside the listed interface faces) and the next
 // substage's k_props once this substage's last reader of the viscosities and
 // corner normals (k_momflux) is enqueued.  The main stream waits for them
 // before anything reads what they write.
@@ -746,9 +779,22 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
   const bool learned = g_curv_model != 0;
   if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
-  timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
-  timed(c, KC_FLUX_FORCE,
-        [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
+  if (par) {
+    // the faces of single-phase upwind cells and the CSF force need only the
+    // curvature: they run on the side stream beside the listed interface
+    // faces (a few percent of the faces, a kernel that fills the GPU only
+    // partly); the two write disjoint faces, and k_vof_advance waits for both
+    cudaEventRecord(c.evf, c.s);
+    cudaStreamWaitEvent(c.s2, c.evf, 0);
+    launch_interface_stage(c.s2, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2);
+    cudaEventRecord(c.evx, c.s2);
+    launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1);
+    cudaStreamWaitEvent(c.s, c.evx, 0);
+  } else {
+    timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
+    timed(c, KC_FLUX_FORCE,
+          [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
+  }
   if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
   timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   if (c.link && k == 2) link_out(c, HL_VOF_OUT, L_VOF, b.vof);  // vof is final
@@ -1021,7 +1067,8 @@ int launch_step(Ctx &c) {
   auto it = c.graphs.find(key);
   // a host-linked graph holds copy-engine copies of the caller's arrays: it
   // is captured again when the arrays are others
-  const std::vector<const void *> hosts = c.link && c.nc == 1 ? c.link_host : std::vector<const void *>();
+  std::vector<const void *> hosts = c.link && c.nc == 1 ? c.link_host : std::vector<const void *>();
+  if (!hosts.empty()) hosts.push_back(reinterpret_cast<const void *>(c.link_reg));
   if (it != c.graphs.end() && c.graph_hosts[key] != hosts) {
     cudaGraphExecDestroy(it->second);
     c.graphs.erase(it);
@@ -1319,6 +1366,7 @@ int sbfs_set_dt_coefs(double adv, double dif, double itf) {
 
 int sbfs_invalidate_device(void) {
   if (g_ctx) g_ctx->resident = false;
+  ++g_reg_epoch;  // and look at the host arrays' registration again
   return 0;
 }
 
@@ -1482,6 +1530,7 @@ int sbfs_pin_host_state(fluid_t *f, interface_t *itf) {
   void *ptrs[] = {f->ux.data, f->uy.data, f->p.data, f->psi[0].data, f->psi[1].data, itf->vof.data};
   size_t sizes[] = {f->ux.datasize, f->uy.datasize, f->p.datasize, f->psi[0].datasize, f->psi[1].datasize,
                     itf->vof.datasize};
+  ++g_reg_epoch;
   for (int i = 0; i < 6; ++i) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, ptrs[i]) == cudaSuccess && at.type == cudaMemoryTypeHost) continue;
@@ -1493,6 +1542,7 @@ int sbfs_pin_host_state(fluid_t *f, interface_t *itf) {
 
 int sbfs_unpin_host_state(fluid_t *f, interface_t *itf) {
   void *ptrs[] = {f->ux.data, f->uy.data, f->p.data, f->psi[0].data, f->psi[1].data, itf->vof.data};
+  ++g_reg_epoch;
   for (void *p : ptrs) {
     if (cudaHostUnregister(p) != cudaSuccess) cudaGetLastError();
   }
@@ -1595,6 +1645,19 @@ bool link_tab_fill(Ctx &c, int k, fluid_t *f, interface_t *itf) {
     if (!layout_ok(*arr[q], *lay[q]) || !host_addressable(arr[q]->data, &c.link_tab[(size_t)k * kLinkSlots + q]))
       return false;
     if (c.nc == 1) c.link_host[q] = arr[q]->data;
+  }
+  if (c.nc == 1 && (c.link_host != c.link_prev || c.link_epoch != g_reg_epoch)) {
+    // page-locked or pageable: the copy engines move them differently, and a
+    // captured copy keeps the way it was captured with
+    c.link_reg = 0;
+    for (int q = 0; q < HL_COUNT; ++q) {
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, c.link_host[q]) == cudaSuccess && at.type == cudaMemoryTypeHost)
+        c.link_reg |= (uintptr_t)1 << q;
+      cudaGetLastError();
+    }
+    c.link_prev = c.link_host;
+    c.link_epoch = g_reg_epoch;
   }
   return true;
 }

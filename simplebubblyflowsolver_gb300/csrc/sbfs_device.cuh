@@ -57,6 +57,7 @@ struct Grid {
   int nc;
   int cm;
   size_t cs1, cs2, cs3, css;
+  int ct;  // doubles per column table (nx + 2 rounded up; kColTabs x 3 tables per case)
   const struct Phys *phys;
 };
 
@@ -117,6 +118,22 @@ __host__ __device__ constexpr int sc_gdt2(int k) { return 36 + 3 * k; }
 // the correction coefficients times 1 / hy
 __host__ __device__ constexpr int sc_cnewy(int k) { return 43 + 2 * k; }
 __host__ __device__ constexpr int sc_coldy(int k) { return 44 + 2 * k; }
+// fused step: 2 gamma dt / hy (the uy pressure term), coldy / pay (the uy
+// correction by the stored pay e grad psi_old), 2 rho_ref pax and 2 rho_ref
+// pay (k_predict_mf stores e grad psi_old times pax at ux faces and times pay
+// at uy faces: e pa = 2 rho_ref pa / (2 rho) - pa)
+__host__ __device__ constexpr int sc_gdt2y(int k) { return 49 + k; }
+__host__ __device__ constexpr int sc_coldyp(int k) { return 52 + k; }
+__host__ __device__ constexpr int sc_rpx(int k) { return 55 + k; }
+__host__ __device__ constexpr int sc_rpy(int k) { return 58 + k; }
+// per-column coefficients of substage k (Bufs::coltab, kColTabs tables of
+// Grid::ct doubles per substage, I = 0..nx+1), written with the scalars:
+// 2 gamma dt / HXXF(I) (ux pressure term), cnew / HXXF(I) and cold / HXXF(I)
+// / pax (ux correction by the stored pax e grad psi_old)
+constexpr int kColTabs = 3;
+__host__ __device__ constexpr int ct_gdt2x(int k) { return 3 * k; }
+__host__ __device__ constexpr int ct_cnewx(int k) { return 3 * k + 1; }
+__host__ __device__ constexpr int ct_coldx(int k) { return 3 * k + 2; }
 
 // THINC constants (reference src/interface/common.c:4-14)
 constexpr double kGaussPt = 0.2886751345948129;

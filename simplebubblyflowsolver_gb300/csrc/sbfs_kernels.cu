@@ -762,19 +762,23 @@ __global__ void __launch_bounds__(BX *BY)
                  const double *__restrict__ ifrcy, const double *__restrict__ den0, const double *__restrict__ den1,
                  const double *__restrict__ psio, double *__restrict__ sxa, const double *__restrict__ sxb,
                  double *__restrict__ sya, const double *__restrict__ syb, double *__restrict__ egx,
-                 double *__restrict__ egy) {
+                 double *__restrict__ egy, const double *__restrict__ coltab) {
   pdl_entry();
-  const Phys ph = zphys(g, ph0);
   sc += (size_t)blockIdx.z * (kScalars);
+  const double *__restrict__ gx = coltab + ((size_t)blockIdx.z * 3 * kColTabs + ct_gdt2x(k)) * g.ct;
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr, rp = wrap(J + 1, g.ny) + zr;
   // the update is carried as 2u with 2 alpha dt, ... and 1 / (2 rho_face):
-  // powers of two, so every rounding is the one of the plain form
-  const double adt2 = sc[sc_adt2(k)], bdt2 = sc[sc_bdt2(k)], gdt2 = sc[sc_gdt2(k)];
-  const double rref2 = ph.rref2;
+  // powers of two, so every rounding is the one of the plain form; the
+  // pressure term's 2 gamma dt / H comes per column (gx) or per case
+  const double adt2 = sc[sc_adt2(k)], bdt2 = sc[sc_bdt2(k)];
+  const Phys ph = zphys(g, ph0);
+  // e grad psi_old is stored times the Poisson factor pax (x faces) or pay
+  // (y faces): e pa = (2 rho_ref pa) / (2 rho) - pa
+  const double rpx = sc[sc_rpx(k)], pax = sc[sc_pax(k)];
   const double ps0 = psio[ix(g, r, I)];
   // ---- ux at face I
   if (I >= 2) {
@@ -784,14 +788,13 @@ __global__ void __launch_bounds__(BX *BY)
     a = fma(ph.hgrav, rho0, a);
     a = fma(m.q4f[I], pxx[ix(g, r, I - 1)] - pxx[ix(g, r, I - 2)], a);
     a = fma(g.q4y, pxy[ix(g, rp, I - 1)] - pxy[ix(g, r, I - 1)], a);
-    const double gs = (p[ix(g, r, I - 1)] - p[ix(g, r, I)]) * m.ihxxf[I];
     const double ir2 = rcp_nr(den1[ix(g, r, I - 1)] + den1[ix(g, r, I)]);  // 1 / (2 rho^{k+1})
     double u = fma(adt2, a, rho0 * u0);
     if (k != 0) u = fma(bdt2, sxb[ix(g, r, I - 2)], u);
-    u = fma(gdt2, gs, u);
+    u = fma(gx[I], p[ix(g, r, I - 1)] - p[ix(g, r, I)], u);
     ux_out[ix(g, r, I - 1)] = u * ir2;
     sxa[ix(g, r, I - 2)] = a;
-    egx[ix(g, r, I - 1)] = fma(rref2, ir2, -1.) * (ps0 - psio[ix(g, r, I - 1)]);
+    egx[ix(g, r, I - 1)] = fma(rpx, ir2, -pax) * (ps0 - psio[ix(g, r, I - 1)]);
   }
   // ---- uy at face (I, J - 1/2)
   {
@@ -799,28 +802,27 @@ __global__ void __launch_bounds__(BX *BY)
     double a = ifrcy[ix(g, r, I - 1)];
     a = fma(m.q4c[I], pyx[ix(g, r, I)] - pyx[ix(g, r, I - 1)], a);
     a = fma(g.q4y, pyy[ix(g, r, I - 1)] - pyy[ix(g, rm, I - 1)], a);
-    const double gs = (p[ix(g, rm, I)] - p[ix(g, r, I)]) * g.ihy;
     const double rho0 = den0[ix(g, rm, I)] + den0[ix(g, r, I)];  // 2 rho^k
     const double ir2 = rcp_nr(den1[ix(g, rm, I)] + den1[ix(g, r, I)]);
     double u = fma(adt2, a, rho0 * w0);
     if (k != 0) u = fma(bdt2, syb[ix(g, r, I - 1)], u);
-    u = fma(gdt2, gs, u);
+    u = fma(sc[sc_gdt2y(k)], p[ix(g, rm, I)] - p[ix(g, r, I)], u);
     uy_out[ix(g, r, I)] = u * ir2;
     sya[ix(g, r, I - 1)] = a;
-    egy[ix(g, r, I)] = fma(rref2, ir2, -1.) * (ps0 - psio[ix(g, rm, I)]);
+    egy[ix(g, r, I)] = fma(sc[sc_rpy(k)], ir2, -sc[sc_pay(k)]) * (ps0 - psio[ix(g, rm, I)]);
   }
   // walls: impermeable, no-slip; the wall faces' e grad psi_old (zero for a
   // Neumann psi_old, computed as the reference does)
   if (I == 1) {
     ux_out[ix(g, r, 0)] = 0.;
     uy_out[ix(g, r, 0)] = 0.;
-    egx[ix(g, r, 0)] = fma(rref2, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -1.) * (ps0 - psio[ix(g, r, 0)]);
+    egx[ix(g, r, 0)] = fma(rpx, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -pax) * (ps0 - psio[ix(g, r, 0)]);
   }
   if (I == g.nx) {
     ux_out[ix(g, r, g.nx)] = 0.;
     uy_out[ix(g, r, g.nx + 1)] = 0.;
     egx[ix(g, r, g.nx)] =
-        fma(rref2, rcp_nr(den1[ix(g, r, g.nx)] + den1[ix(g, r, g.nx + 1)]), -1.) * (psio[ix(g, r, g.nx + 1)] - ps0);
+        fma(rpx, rcp_nr(den1[ix(g, r, g.nx)] + den1[ix(g, r, g.nx + 1)]), -pax) * (psio[ix(g, r, g.nx + 1)] - ps0);
   }
 }
 
@@ -835,7 +837,8 @@ __global__ void __launch_bounds__(BX *BY)
 //   1. k_poisson_fwd: right-hand side of src/fluid/compute_potential.c:
 //      285-363 for a tile of W columns,
 //        rhs = rho_ref/dt_new div u* - dt_old/dt_new div((rho_ref/rho - 1) grad psi_old)
-//      (the face values of (rho_ref/rho - 1) grad psi_old come from k_predict_mf)
+//      (the face values of (rho_ref/rho - 1) grad psi_old come from k_predict_mf,
+//      already times their Poisson coefficient)
 //      with div and the face differences in the JD = H hy form, packed two
 //      reals per complex, a mixed radix-4/2 Stockham FFT of length ny/2 in
 //      shared memory and the real-to-complex split; spectrum [I][m]
@@ -845,7 +848,7 @@ __global__ void __launch_bounds__(BX *BY)
 // into the right-hand-side coefficients.
 // ---------------------------------------------------------------------------
 
-// Stockham FFT (radix 4, one radix-2 stage first when log2 M is odd) of W
+// Stockham FFT (radix 4, one radix-8 stage first when log2 M is odd) of W
 // rows of length M in shared memory.  Returns the buffer holding the result.
 // tw: the twiddle buffer, exp(-2 pi i m / 2M) for m = 0..M, then W_M^e for
 // e < M, then their conjugates (the inverse's): one load per twiddle.
@@ -853,19 +856,50 @@ template <int W>
 __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__restrict__ tw, bool inverse) {
   const double2 *__restrict__ wm = tw + (M + 1) + (inverse ? M : 0);
   int Ns = 1;
-  if ((__ffs(M) - 1) & 1) {  // log2 M odd
-    const int half = M >> 1;
-    for (int t = threadIdx.x; t < W * half; t += blockDim.x) {
-      const int c = t / half, j = t - c * half;
-      const double2 v0 = x[c * M + j], v1 = x[c * M + j + half];
-      y[c * M + 2 * j] = cadd(v0, v1);
-      y[c * M + 2 * j + 1] = csub(v0, v1);
+  if ((__ffs(M) - 1) & 1) {  // log2 M odd (M >= 8): an untwiddled radix-8 stage
+    // X_2m = DFT4(v_q + v_q+4)_m, X_2m+1 = DFT4((v_q - v_q+4) W8^q)_m; the
+    // 1/sqrt(2) of W8 and W8^3 rides in the odd half's last FMAs: 52 FP64
+    // operations for 8 points, where a radix-2 stage and a twiddled radix-4
+    // stage take 64 for the same three levels
+    const double c8 = 0.70710678118654752440;
+    const int q8 = M >> 3;
+    for (int t = threadIdx.x; t < W * q8; t += blockDim.x) {
+      const int c = t / q8, j = t - c * q8;
+      const double2 *xr = x + c * M;
+      double2 *yr = y + c * M + 8 * j;
+      double2 a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double2 u = xr[j + q * q8], w = xr[j + (q + 4) * q8];
+        a[q] = cadd(u, w);
+        b[q] = csub(u, w);
+      }
+      // even outputs: DFT4 of a; -i (forward) or +i (inverse) rotations are sign flips
+      const double2 e0 = cadd(a[0], a[2]), e1 = csub(a[0], a[2]), e2 = cadd(a[1], a[3]), e3 = csub(a[1], a[3]);
+      const double2 re3 = inverse ? make_double2(-e3.y, e3.x) : make_double2(e3.y, -e3.x);
+      yr[0] = cadd(e0, e2);
+      yr[2] = cadd(e1, re3);
+      yr[4] = csub(e0, e2);
+      yr[6] = csub(e1, re3);
+      // odd outputs: t1 = b1 W8 = c8 P1, t2 = b2 W8^2 (a rotation), t3 = b3 W8^3 = c8 P3
+      const double2 P1 = inverse ? make_double2(b[1].x - b[1].y, b[1].x + b[1].y)
+                                 : make_double2(b[1].x + b[1].y, b[1].y - b[1].x);
+      const double2 P3 = inverse ? make_double2(-(b[3].x + b[3].y), b[3].x - b[3].y)
+                                 : make_double2(b[3].y - b[3].x, -(b[3].x + b[3].y));
+      const double2 t2 = inverse ? make_double2(-b[2].y, b[2].x) : make_double2(b[2].y, -b[2].x);
+      const double2 A0 = cadd(b[0], t2), A1 = csub(b[0], t2);
+      const double2 E = cadd(P1, P3), D = csub(P1, P3);  // t1 + t3 = c8 E, t1 - t3 = c8 D
+      const double2 rD = inverse ? make_double2(-D.y, D.x) : make_double2(D.y, -D.x);
+      yr[1] = make_double2(fma(c8, E.x, A0.x), fma(c8, E.y, A0.y));
+      yr[3] = make_double2(fma(c8, rD.x, A1.x), fma(c8, rD.y, A1.y));
+      yr[5] = make_double2(fma(-c8, E.x, A0.x), fma(-c8, E.y, A0.y));
+      yr[7] = make_double2(fma(-c8, rD.x, A1.x), fma(-c8, rD.y, A1.y));
     }
     __syncthreads();
     double2 *tmp = x;
     x = y;
     y = tmp;
-    Ns = 2;
+    Ns = 8;
   }
   const int q4 = M >> 2;
   for (; Ns < M; Ns <<= 2) {
@@ -923,7 +957,7 @@ __global__ void __launch_bounds__(256)
   double2 *A = smem, *B = smem + W * M;
   double *Ad = reinterpret_cast<double *>(A);
   const int I0 = blockIdx.x * W + 1;
-  const double pdx = sc[sc_pdx(k)], pdy = sc[sc_pdy(k)], pax = sc[sc_pax(k)], pay = sc[sc_pay(k)];
+  const double pdx = sc[sc_pdx(k)], pdy = sc[sc_pdy(k)];
   for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
     const int c = t % W, r = t / W;
     const int I = I0 + c;
@@ -932,13 +966,13 @@ __global__ void __launch_bounds__(256)
       // global rows of this case (the case's rows follow each other)
       const int zr = blockIdx.z * ny;
       const int rg = r + zr, rp = (r == ny - 1 ? 0 : r + 1) + zr;
-      // differences of e grad psi_old across the cell (its faces' values
-      // written by k_predict_mf or k_face_factor)
+      // differences of pax e grad psi_old and pay e grad psi_old across the
+      // cell (its faces' values written by k_predict_mf or k_face_factor)
       const double X = egx[ix(g, rg, I)] - egx[ix(g, rg, I - 1)];
       const double Y = egy[ix(g, rp, I)] - egy[ix(g, rg, I)];
       const double dux = ux[ix(g, rg, I)] - ux[ix(g, rg, I - 1)];
       const double duy = uy[ix(g, rp, I)] - uy[ix(g, rg, I)];
-      val = fma(pdx, dux, fma(pdy, duy, fma(pax, X, pay * Y)));
+      val = fma(pdx, dux, fma(pdy, duy, X + Y));
     }
     Ad[c * ny + r] = val;
   }
@@ -1176,36 +1210,37 @@ __global__ void __launch_bounds__(512)
 //   src/fluid/correct_velocity/ux.c:18-66, uy.c:17-64
 //   src/fluid/update_pressure.c:7-53
 //   u -= dt_new / rho_ref dpsi_new / h;  u += -dt_old (1/rho - 1/rho_ref) dpsi_old / h
-//   with 1/rho - 1/rho_ref = e / rho_ref; e dpsi_old at the faces is egx, egy
-//   (k_predict_mf or k_face_factor)
+//   with 1/rho - 1/rho_ref = e / rho_ref; pax e dpsi_old and pay e dpsi_old at
+//   the faces are egx, egy (k_predict_mf or k_face_factor); the x coefficients
+//   come per column (cnew / HXXF(I), cold / HXXF(I) / pax), the y ones per case
 // thread (I, J): I = 1..nx
 // ---------------------------------------------------------------------------
 template <bool PRES>
 __global__ void __launch_bounds__(BX *BY)
-    k_correct(Grid g, Metrics m, const double *__restrict__ sc, int k, double *__restrict__ ux,
-              double *__restrict__ uy, const double *__restrict__ psin, const double *__restrict__ egx,
-              const double *__restrict__ egy, double *__restrict__ p) {
+    k_correct(Grid g, const double *__restrict__ sc, const double *__restrict__ coltab, int k,
+              double *__restrict__ ux, double *__restrict__ uy, const double *__restrict__ psin,
+              const double *__restrict__ egx, const double *__restrict__ egy, double *__restrict__ p) {
   pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
+  const double *__restrict__ ct = coltab + (size_t)blockIdx.z * 3 * kColTabs * g.ct;
+  const double *__restrict__ cn = ct + ct_cnewx(k) * g.ct, *__restrict__ co = ct + ct_coldx(k) * g.ct;
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const int r = J - 1 + zr, rm = wrap(J - 1, g.ny) + zr;
-  const double cnew = sc[sc_cnew(k)], cold = sc[sc_cold(k)];
-  const double cnewy = sc[sc_cnewy(k)], coldy = sc[sc_coldy(k)];
+  const double cnewy = sc[sc_cnewy(k)], coldyp = sc[sc_coldyp(k)];
   const double pn0 = psin[ix(g, r, I)];
   if (I >= 2) {
-    const double ih = m.ihxxf[I];
     double u = ux[ix(g, r, I - 1)];
-    u = fma(-(cnew * ih), pn0 - psin[ix(g, r, I - 1)], u);
-    u = fma(cold * ih, egx[ix(g, r, I - 1)], u);
+    u = fma(-cn[I], pn0 - psin[ix(g, r, I - 1)], u);
+    u = fma(co[I], egx[ix(g, r, I - 1)], u);
     ux[ix(g, r, I - 1)] = u;
   }
   {
     double u = uy[ix(g, r, I)];
     u = fma(-cnewy, pn0 - psin[ix(g, rm, I)], u);
-    u = fma(coldy, egy[ix(g, r, I)], u);
+    u = fma(coldyp, egy[ix(g, r, I)], u);
     uy[ix(g, r, I)] = u;
   }
   if (I == 1) {
@@ -1252,7 +1287,7 @@ constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
 __global__ void __launch_bounds__(BX *BY)
     k_decide_dt(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
                 unsigned long long *__restrict__ acc, double *__restrict__ sc, int *__restrict__ status,
-                double dt_fixed, double coef_adv) {
+                double dt_fixed, double coef_adv, double *__restrict__ coltab) {
   pdl_entry();
   const Phys ph = zphys(g, ph0);
   if (g.phys) dt_fixed = ph.dtfix;
@@ -1351,28 +1386,45 @@ __global__ void __launch_bounds__(BX *BY)
       sc[sc_cold(k)] = -dtold * ph.irefden;
       sc[sc_cnewy(k)] = sc[sc_cnew(k)] * g.ihy;
       sc[sc_coldy(k)] = sc[sc_cold(k)] * g.ihy;
+      sc[sc_gdt2y(k)] = sc[sc_gdt2(k)] * g.ihy;
+      sc[sc_coldyp(k)] = sc[sc_coldy(k)] / sc[sc_pay(k)];
+      sc[sc_rpx(k)] = ph.rref2 * sc[sc_pax(k)];
+      sc[sc_rpy(k)] = ph.rref2 * sc[sc_pay(k)];
     }
   }
   __syncthreads();
+  // the per-column coefficients of the three substages (none for a caller
+  // without the table)
+  if (coltab) {
+    coltab += (size_t)blockIdx.z * 3 * kColTabs * g.ct;
+    for (int t = tid; t < 3 * (g.nx + 2); t += BX * BY) {
+      const int k = t / (g.nx + 2), I = t - k * (g.nx + 2);
+      const double ih = m.ihxxf[I];
+      coltab[(size_t)ct_gdt2x(k) * g.ct + I] = sc[sc_gdt2(k)] * ih;
+      coltab[(size_t)ct_cnewx(k) * g.ct + I] = sc[sc_cnew(k)] * ih;
+      coltab[(size_t)ct_coldx(k) * g.ct + I] = sc[sc_cold(k)] * ih / sc[sc_pax(k)];
+    }
+  }
   // reset the accumulators for the next launch
   for (int i = tid; i <= g.nx + 3; i += BX * BY) acc[i] = 0ULL;
 }
 
-// e grad psi_old, e = rho_ref / rho - 1, at ux faces (I = 1..nx+1) and uy
-// faces (I = 1..nx) from a density field and psi_old, as k_predict_mf stores
-// it (fine-grained entry points)
-__global__ void k_face_factor(Grid g, Phys ph, const double *__restrict__ den, const double *__restrict__ psio,
-                              double *__restrict__ egx, double *__restrict__ egy) {
+// pax e grad psi_old and pay e grad psi_old, e = rho_ref / rho - 1, at ux
+// faces (I = 1..nx+1) and uy faces (I = 1..nx) from a density field and
+// psi_old, as k_predict_mf stores them (fine-grained entry points; the
+// scalars of slot 0)
+__global__ void k_face_factor(Grid g, const double *__restrict__ sc, const double *__restrict__ den,
+                              const double *__restrict__ psio, double *__restrict__ egx, double *__restrict__ egy) {
   pdl_entry();
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
   const int r = J - 1, rm = wrap(J - 1, g.ny);
   const double ps = psio[ix(g, r, I)];
-  const double ex = fma(ph.rref2, rcp_nr(den[ix(g, r, I - 1)] + den[ix(g, r, I)]), -1.);
+  const double ex = fma(sc[sc_rpx(0)], rcp_nr(den[ix(g, r, I - 1)] + den[ix(g, r, I)]), -sc[sc_pax(0)]);
   egx[ix(g, r, I - 1)] = ex * (ps - psio[ix(g, r, I - 1)]);
   if (I <= g.nx) {
-    const double ey = fma(ph.rref2, rcp_nr(den[ix(g, rm, I)] + den[ix(g, r, I)]), -1.);
+    const double ey = fma(sc[sc_rpy(0)], rcp_nr(den[ix(g, rm, I)] + den[ix(g, r, I)]), -sc[sc_pay(0)]);
     egy[ix(g, r, I)] = ey * (ps - psio[ix(g, rm, I)]);
   }
 }
@@ -1773,7 +1825,7 @@ void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
                        const double *srcux_b, double *srcuy_a, const double *srcuy_b) {
   launch_pdl(k_predict_mf, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g,
              m, ph, sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, b.ifrcx, b.ifrcy, den0, den1,
-             psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy);
+             psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy, b.coltab);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -1848,9 +1900,9 @@ void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs 
                     double *ux, double *uy, const double *psi_new, bool pressure) {
   const dim3 gr = tile_grid(b.tiles, TK_CORRECT, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_CORRECT);
   if (pressure)
-    launch_pdl(k_correct<true>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, b.egx, b.egy, b.p);
+    launch_pdl(k_correct<true>, gr, bl, 0, s, g, sc, b.coltab, k, ux, uy, psi_new, b.egx, b.egy, b.p);
   else
-    launch_pdl(k_correct<false>, gr, bl, 0, s, g, m, sc, k, ux, uy, psi_new, b.egx, b.egy, b.p);
+    launch_pdl(k_correct<false>, gr, bl, 0, s, g, sc, b.coltab, k, ux, uy, psi_new, b.egx, b.egy, b.p);
 }
 
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new) {
@@ -1863,12 +1915,12 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
   const int gx = (g.nx + BX) / BX;
   while (gy > 1 && gx * gy * g.nc > 4 * 152) gy = (gy + 1) / 2;
   launch_pdl(k_decide_dt, dim3(gx, gy, g.nc), dim3(BX, BY), 0, s, g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
-                                                    coef_adv);
+                                                    coef_adv, b.coltab);
 }
 
 void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *den,
                         const double *psi_old) {
-  launch_pdl(k_face_factor, grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s, g, ph, den, psi_old, b.egx, b.egy);
+  launch_pdl(k_face_factor, grid2d(g.nx + 1, g.ny), dim3(BX, BY), 0, s, g, b.scalars, den, psi_old, b.egx, b.egy);
 }
 
 int diag_partial_blocks(const Grid &g) {

@@ -48,6 +48,7 @@ struct Bufs {
   // decide_dt accumulators and per-step scalars
   unsigned long long *dt_acc;  // [0..nx+1] column max |ux| bits, [nx+2] max |uy| bits, [nx+3] block counter
   double *scalars;             // kScalars doubles
+  double *coltab;              // per-column coefficients (3 kColTabs tables of Grid::ct doubles a case)
   int *status;                 // device error word
   // interface cells of the current substage (linear index (J-1)*nx + I-1) and their count;
   // the faces those cells are upwind of (4 * cell + face, face 0..3 = left, right, bottom, top)

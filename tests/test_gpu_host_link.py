@@ -145,3 +145,38 @@ def test_registered_only_link(libs):
         gpu.unpin_host_state(a)
     for s in HOST_SLOTS:
         assert np.array_equal(a.field(s), b.field(s)), s
+
+
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph", "eager"])
+def test_linked_copies_follow_registration(libs, graphs):
+    """a linked step moves page-locked arrays by copy engine and pageable ones
+    by copy kernel, and captures its graph again when the same arrays are
+    pinned or unpinned between steps: every host array, ghost rows included,
+    ends as on the cudaMemcpy path"""
+    gpu, orc = libs
+    wl = ic.bubble_swarm(256, 128, nbubbles=6, seed=5)
+    set_env(wl)
+    for lib in (gpu, orc):
+        lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    gpu.set_sync_mode(SYNC_STATE)
+    st0 = new_state(wl, orc)
+    a, b = clone(st0), clone(st0)
+    for st in (a, b):
+        for s in HOST_SLOTS:
+            st.field(s)[0] = np.nan
+            st.field(s)[-1] = np.nan
+    dta = []
+    try:
+        dta += run(gpu, a, 2, True, graphs)[0]
+        gpu.pin_host_state(a)
+        dta += run(gpu, a, 2, True, graphs)[0]
+        gpu.unpin_host_state(a)
+        dta += run(gpu, a, 2, True, graphs)[0]
+    finally:
+        gpu.unpin_host_state(a)
+    dtb, used_b = run(gpu, b, 6, False, graphs)
+    assert not any(used_b)
+    assert dta == dtb
+    for s in HOST_SLOTS:
+        assert np.array_equal(a.field(s), b.field(s)), s
+        assert np.isfinite(a.field(s)).all(), s
