@@ -277,8 +277,8 @@ int sbfs_mlp_predict(const void *X, int n, float *out);
  * prediction |kappa dx| in the closure's range), plain kappa elsewhere.
  * Square cells.  Applies to integrate() and the timed runs. */
 int sbfs_set_curvature_model(int model);
-/* the closure's range in |kappa dx| (default [0.02, 0.5]: the training
- * circles' radii, 2 .. 50 cells) */
+/* the closure's range in |kappa dx| (default [1/128, 0.5]: the training
+ * circles' radii, 2 .. 128 cells) */
 int sbfs_mlp_set_range(double lo, double hi);
 /* interface cells that took the learned curvature since the last call */
 int sbfs_mlp_take_usage(long long *used);

@@ -319,7 +319,7 @@ class GpuLibrary(ReferenceAPI):
         return u.value
 
     def mlp_set_range(self, lo: float, hi: float):
-        """the closure's range in |kappa dx| (default 0.02 .. 0.5)"""
+        """the closure's range in |kappa dx| (default 1/128 .. 0.5)"""
         self._mlp_types()
         self._mlp("sbfs_mlp_set_range", lo, hi)
 

@@ -570,8 +570,8 @@ size_t smem_infer() { return sizeof(SmemW) + sizeof(__nv_bfloat16) * 8 * 32 * NF
 namespace sbfs {
 bool mlp_ready() { return g_params != nullptr; }
 // the closure's range in |kappa dx|: the curvatures of the training circles,
-// radii 2 .. 50 cells
-float g_kappa_lo = 0.02f, g_kappa_hi = 0.5f;
+// radii 2 .. 128 cells
+float g_kappa_lo = 0.0078125f, g_kappa_hi = 0.5f;
 void mlp_range(float *lo, float *hi) {
   *lo = g_kappa_lo;
   *hi = g_kappa_hi;

@@ -18,13 +18,18 @@ Training set (defaults), each part with the 8 rotations / reflections of
 every stencil and half of it inverted (1 - vof, label -1/R):
   * 2e5 circles, R ~ U[2, 50] cells, centre offset ~ U[0, 1)^2 cells, one
     interface cell per circle at a random angle, exact cell-area VOF
-    (ic.disc_cell_fraction);
-  * as many stencils of circles translated by the solver itself
+    (ic.disc_cell_fraction), and beside that specified set 3.25e5 more with
+    R ~ U[50, 128] cells (the same density per unit radius): a drop of radius
+    64 cells, the static drop at 256^2, lies past 50, where a closure trained
+    on 2 .. 50 only hands part of the interface back to the plain curvature
+    and the mix worsens the Laplace jump;
+  * as many stencils of circles translated by the solver itself, radii to 128
     (advected_circle_stencils): THINC (beta = 1) fluxes turn the sharp
     exact-area profile into a diffuse one within a few cells of travel, and
     a network that has only seen the sharp profile fails on it;
-  * up to as many stencils of static drops held by their exact curvature
-    (relaxed_drop_stencils): the states a good closure meets in the step.
+  * up to as many stencils of static drops held by their exact curvature,
+    radii to 128 (relaxed_drop_stencils): the states a good closure meets in
+    the step.
 Training: Adam, batch 1024, cosine learning rate 2e-3 -> 2e-5, 40 epochs,
 on the GPU (k_mlp_grad / k_mlp_adam of sbfs_mlp.cu).
 """
@@ -378,21 +383,29 @@ class GpuCurvatureModel:
         return out.cpu().numpy()
 
 
-def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfields=2, seed=0, log=None):
+def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfields=2, seed=0, log=None,
+                 rmax=128.0):
     """(features, labels) with the 8 symmetries: the exact-area circles and,
     run on `lib`, up to as many stencils of circles carried by the solver
-    (`advected`) and of drops relaxed under their exact curvature (`relaxed`)"""
+    (`advected`) and of drops relaxed under their exact curvature (`relaxed`).
+    rmax: the largest radius in cells (50: the specified set, R ~ U[2, 50];
+    above 50 the circles beyond 50 come as an extra set of ncircles *
+    (rmax - 50) / 48, R ~ U[50, rmax], so the specified set stays as it is)"""
     st, lab, _ = circle_stencils(ncircles, seed=seed)
     parts_st, parts_lab = [st], [lab]
+    if rmax > 50.0:
+        se, le, _ = circle_stencils(int(ncircles * (rmax - 50.0) / 48.0), rmin=50.0, rmax=rmax, seed=seed + 4)
+        parts_st.append(se)
+        parts_lab.append(le)
     rng = np.random.default_rng(seed + 2)
     if advected:
         sa, la, _ = advected_circle_stencils(lib, n=n, nfields=nfields, steps=160, sample_every=40, seed=seed + 1,
-                                             log=log)
+                                             rmax=rmax, log=log)
         pick = rng.choice(sa.shape[0], min(sa.shape[0], st.shape[0]), replace=False)
         parts_st.append(sa[pick])
         parts_lab.append(la[pick])
     if relaxed:
-        radii = np.exp(rng.uniform(math.log(2.0), math.log(50.0), 48))
+        radii = np.exp(rng.uniform(math.log(2.0), math.log(rmax), 48))
         sr, lr, _ = relaxed_drop_stencils(lib, radii, seed=seed + 3)
         pick = rng.choice(sr.shape[0], min(sr.shape[0], st.shape[0]), replace=False)
         parts_st.append(sr[pick])
@@ -404,10 +417,10 @@ def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfie
     return features(symmetries(st)), np.tile(lab, 8).astype(np.float32)
 
 
-def train_default(lib, ncircles=200000, epochs=40, seed=0, advected=True, relaxed=True, log=None):
-    """train the closure on the default data set on the GPU; returns
-    (model, parameters, loss history)"""
-    X, Y = training_set(lib, ncircles, advected=advected, relaxed=relaxed, seed=seed, log=log)
+def train_default(lib, ncircles=200000, epochs=40, seed=0, advected=True, relaxed=True, log=None, rmax=128.0):
+    """train the closure on the default data set on the GPU (radii up to rmax
+    cells, see training_set); returns (model, parameters, loss history)"""
+    X, Y = training_set(lib, ncircles, advected=advected, relaxed=relaxed, seed=seed, log=log, rmax=rmax)
     m = GpuCurvatureModel(lib, X, Y)
     m.set_params(init_params(seed))
     hist = m.train(epochs=epochs, seed=seed, log=log)
@@ -448,8 +461,8 @@ def interface_stencils(vof_rows: np.ndarray, vofmin=1e-8):
     return st, rr, cc
 
 
-# the closure's default range in |kappa dx|: the training circles, radii 2 .. 50 cells
-KAPPA_RANGE = (0.02, 0.5)
+# the closure's default range in |kappa dx|: the training circles, radii 2 .. 128 cells
+KAPPA_RANGE = (1.0 / 128.0, 0.5)
 
 
 def static_drop_table(lib, ns=(64, 128, 256), steps=1000, params=None, log=None):

@@ -99,14 +99,14 @@ def test_curvature_model_switch(lib):
     assert lib.kernels_per_step() == base
 
 
-@pytest.mark.parametrize("n", [64, 128])
+@pytest.mark.parametrize("n", [64, 128, 256])
 def test_static_drop_in_the_step(lib, trained, n):
     """the closure inside the time step, static drop (density ratio 1e-3, La =
-    12000): the curvature the step uses, and at 64^2 the time-averaged
-    parasitic velocity, learned vs plain.  Over three training seeds
-    (1000 steps): kappa error learned / plain 0.20 .. 0.27 at 64^2 and
-    0.47 .. 0.54 at 128^2; parasitic velocity 0.46 .. 0.58 at 64^2 but
-    0.56 .. 1.0 at 128^2, so only 64^2 is held to it."""
+    12000): the curvature the step uses and the time-averaged parasitic
+    velocity, learned vs plain.  Over three training seeds (1000 steps):
+    kappa error learned / plain 0.20 .. 0.24 at 64^2, 0.32 .. 0.37 at 128^2,
+    0.29 .. 0.39 at 256^2; parasitic velocity 0.42 .. 0.50, 0.41 .. 0.52 and
+    0.49 .. 0.64."""
     _, params, _ = trained
     steps = 400 * n // 64
     a = L.evaluate_static_drop(lib, n=n, steps=steps, model=0, record_every=steps // 8)
@@ -117,9 +117,8 @@ def test_static_drop_in_the_step(lib, trained, n):
           "mean parasitic velocity plain", ua, "learned", ub, "dp err", a["dp_rel_err"], b["dp_rel_err"])
     assert b["learned_cells_per_step"] > 0
     assert np.isfinite(b["umax"]) and np.isfinite(b["dp"])
-    assert b["kappa_rms_rel_err"] < 0.7 * a["kappa_rms_rel_err"]
-    if n == 64:
-        assert ub < 0.8 * ua
+    assert b["kappa_rms_rel_err"] < 0.6 * a["kappa_rms_rel_err"]
+    assert ub < 0.8 * ua
 
 
 def test_training_is_reproducible(lib):
