@@ -279,7 +279,8 @@ def load_traffic():
         for line in open(TRAFFIC_FILE):
             p = line.split()
             if len(p) >= 4 and not line.startswith("#"):
-                out[(p[0], p[1])] = {"traffic": float(p[2]), "fp64_flop": float(p[3])}
+                out[(p[0], p[1])] = {"traffic": float(p[2]), "fp64_flop": float(p[3]),
+                                     "fp64_inst": float(p[4]) if len(p) >= 5 else None}
     return out
 
 
@@ -434,18 +435,26 @@ def roofline_of(prof, lib, cells, grid, step_ms):
     if tr:
         ach = tr["fp64_flop"] / dom_avg_s / 1e9
         out.update(achieved=round(ach, 1), frac=round(ach / fp64_peak, 4), fp64_flop_per_launch=tr["fp64_flop"])
+        if tr.get("fp64_inst"):
+            # DADD and DMUL take an FP64 issue slot like an FMA: the fraction of
+            # the pipe's instruction rate (peak / 2 FMA per second) the kernel issues
+            out["issue_frac"] = round(tr["fp64_inst"] / dom_avg_s / 1e9 / (fp64_peak / 2.0), 4)
     # step-wide: every launch class of a step (decide_dt once, the rest three times)
     if traffic and all(k in traffic for k, v in prof.items() if v[1] > 0):
         per = {k: v[1] / max(1, prof["k_decide_dt"][1]) for k, v in prof.items() if v[1] > 0}
         flop = sum(traffic[k]["fp64_flop"] * n for k, n in per.items())
+        inst = sum((traffic[k]["fp64_inst"] or 0.0) * n for k, n in per.items())
         out["step"] = {"fp64_flop_per_cell_step": round(flop / cells, 1),
                        "fp64_frac": round(flop / (step_ms / 1e3) / 1e9 / fp64_peak, 4),
+                       "fp64_inst_per_cell_step": round(inst / cells, 1),
+                       "fp64_issue_frac": round(inst / (step_ms / 1e3) / 1e9 / (fp64_peak / 2.0), 4),
                        "fused_hbm_frac": round(720.0 * cells / (step_ms / 1e3) / 1e9 / hbm_peak, 4),
                        "dram_bytes_per_cell_step": round(sum(traffic[k]["traffic"] * n for k, n in per.items())
                                                          / cells, 1),
-                       "note": "fp64_frac: the step's FP64 operations (ncu) over its device time and the live FMA "
-                               "rate; fused_hbm_frac: 720 B per cell-step (the fused-minimum dataflow) over the "
-                               "measured HBM bandwidth"}
+                       "note": "fp64_frac: the step's FP64 flops (ncu, FMA = 2) over its device time and the live "
+                               "FMA rate; fp64_issue_frac: its FP64 instructions (an FMA, DADD or DMUL each takes "
+                               "one issue slot) over the FMA instruction rate; fused_hbm_frac: 720 B per cell-step "
+                               "(the fused-minimum dataflow) over the measured HBM bandwidth"}
     return out
 
 

@@ -608,10 +608,11 @@ int put_scalars(Ctx &c, double dt, int k, double dt_old, double dt_new) {
     // the correction's per-column coefficients of slot 0, as k_decide_dt
     // writes them for the fused step
     std::vector<double> ct(2 * (size_t)g.ct, 0.);
+    const double cop = h[sc_cold(0)] / h[sc_pax(0)];
     for (int I = 1; I <= c.nx + 1; ++I) {
       const double ih = 1. / c.hxxf[I - 1];
       ct[I] = h[sc_cnew(0)] * ih;
-      ct[g.ct + I] = h[sc_cold(0)] * ih / h[sc_pax(0)];
+      ct[g.ct + I] = cop * ih;
     }
     CK(cudaMemcpyAsync(c.b.coltab + (size_t)ct_cnewx(0) * g.ct, ct.data(), sizeof(double) * ct.size(),
                        cudaMemcpyHostToDevice, c.s));

@@ -128,8 +128,8 @@ __host__ __device__ constexpr int sc_rpx(int k) { return 55 + k; }
 __host__ __device__ constexpr int sc_rpy(int k) { return 58 + k; }
 // per-column coefficients of substage k (Bufs::coltab, kColTabs tables of
 // Grid::ct doubles per substage, I = 0..nx+1), written with the scalars:
-// 2 gamma dt / HXXF(I) (ux pressure term), cnew / HXXF(I) and cold / HXXF(I)
-// / pax (ux correction by the stored pax e grad psi_old)
+// 2 gamma dt / HXXF(I) (ux pressure term), cnew / HXXF(I) and (cold / pax) /
+// HXXF(I) (ux correction by the stored pax e grad psi_old)
 constexpr int kColTabs = 3;
 __host__ __device__ constexpr int ct_gdt2x(int k) { return 3 * k; }
 __host__ __device__ constexpr int ct_cnewx(int k) { return 3 * k + 1; }

@@ -1397,12 +1397,16 @@ __global__ void __launch_bounds__(BX *BY)
   // without the table)
   if (coltab) {
     coltab += (size_t)blockIdx.z * 3 * kColTabs * g.ct;
+    // cold / pax once per substage: a division per entry made this block the
+    // kernel's tail
+    const double cop[3] = {sc[sc_cold(0)] / sc[sc_pax(0)], sc[sc_cold(1)] / sc[sc_pax(1)],
+                           sc[sc_cold(2)] / sc[sc_pax(2)]};
     for (int t = tid; t < 3 * (g.nx + 2); t += BX * BY) {
       const int k = t / (g.nx + 2), I = t - k * (g.nx + 2);
       const double ih = m.ihxxf[I];
       coltab[(size_t)ct_gdt2x(k) * g.ct + I] = sc[sc_gdt2(k)] * ih;
       coltab[(size_t)ct_cnewx(k) * g.ct + I] = sc[sc_cnew(k)] * ih;
-      coltab[(size_t)ct_coldx(k) * g.ct + I] = sc[sc_cold(k)] * ih / sc[sc_pax(k)];
+      coltab[(size_t)ct_coldx(k) * g.ct + I] = cop[k] * ih;
     }
   }
   // reset the accumulators for the next launch

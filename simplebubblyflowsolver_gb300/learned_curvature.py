@@ -384,13 +384,14 @@ class GpuCurvatureModel:
 
 
 def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfields=2, seed=0, log=None,
-                 rmax=128.0):
+                 rmax=128.0, relaxed_rmax=None):
     """(features, labels) with the 8 symmetries: the exact-area circles and,
     run on `lib`, up to as many stencils of circles carried by the solver
     (`advected`) and of drops relaxed under their exact curvature (`relaxed`).
     rmax: the largest radius in cells (50: the specified set, R ~ U[2, 50];
     above 50 the circles beyond 50 come as an extra set of ncircles *
-    (rmax - 50) / 48, R ~ U[50, rmax], so the specified set stays as it is)"""
+    (rmax - 50) / 48, R ~ U[50, rmax], so the specified set stays as it is);
+    relaxed_rmax: the largest radius of the relaxed drops (default rmax)"""
     st, lab, _ = circle_stencils(ncircles, seed=seed)
     parts_st, parts_lab = [st], [lab]
     if rmax > 50.0:
@@ -405,7 +406,7 @@ def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfie
         parts_st.append(sa[pick])
         parts_lab.append(la[pick])
     if relaxed:
-        radii = np.exp(rng.uniform(math.log(2.0), math.log(rmax), 48))
+        radii = np.exp(rng.uniform(math.log(2.0), math.log(relaxed_rmax or rmax), 48))
         sr, lr, _ = relaxed_drop_stencils(lib, radii, seed=seed + 3)
         pick = rng.choice(sr.shape[0], min(sr.shape[0], st.shape[0]), replace=False)
         parts_st.append(sr[pick])
