@@ -73,6 +73,9 @@ ALG_DOUBLES_PER_CELL = {
     "k_poisson_inv": 1 + 1,    # spectrum -> psi
     "k_correct": 6 + 3,        # u*(2), psi, e grad psi(2), p -> u(2), p
     "k_decide_dt": 2,          # ux, uy
+    "k_csf_force": 3 + 2,      # vof, den, curv -> ifrcx, ifrcy
+    "k_face_flux": 0,          # listed cells only
+    "k_bulk_flux": 3 + 2,      # ux, uy, vof -> fluxx, fluxy
 }
 
 

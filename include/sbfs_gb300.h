@@ -107,6 +107,15 @@ int sbfs_set_pdl(int on);
  * Same results either way, bit for bit. */
 int sbfs_set_compaction(int mode);
 
+/* run each substage's interface geometry ahead of its velocity (default 1):
+ * curvature, the interface-cell list with the cells' THINC factors, and the
+ * CSF force depend on vof alone, so they are formed beside the previous
+ * substage's predictor and Poisson solve, and only the upwind choice and the
+ * face fluxes wait for the corrected velocity; 0 forms them all after the
+ * correction.  Same results either way, bit for bit.  (No counterpart in
+ * the reference, whose src/integrate.c:11-70 runs its operators in turn.) */
+int sbfs_set_geometry_ahead(int on);
+
 /* In SBFS_SYNC_STATE mode, let the step copy the state itself (default 1):
  * when the GPU can address the caller's arrays (pageable host memory on a
  * system with host page-table access, such as Grace-Blackwell, or arrays

@@ -85,6 +85,11 @@ class GpuLibrary(ReferenceAPI):
         """interface-branch compaction: -1 as tuned (default), 0 off, 1 on"""
         self._ext("sbfs_set_compaction", int(mode))
 
+    def set_geometry_ahead(self, on: bool):
+        """form each substage's interface geometry and CSF force ahead of its
+        velocity, beside the previous substage's predictor (default True)"""
+        self._ext("sbfs_set_geometry_ahead", 1 if on else 0)
+
     def set_host_link(self, on):
         """strict-mode steps copy the state in and out themselves, overlapped
         with their kernels, when the GPU can address the host arrays (True or
@@ -230,8 +235,8 @@ class GpuLibrary(ReferenceAPI):
 
     def tiles(self, group: int = -1) -> dict:
         """launch shapes in use (group -1: the single-case context)"""
-        bx = (C.c_int * 7)()
-        by = (C.c_int * 7)()
+        bx = (C.c_int * 16)()
+        by = (C.c_int * 16)()
         fw = C.c_int(0)
         mb = C.c_int(0)
         gw = C.c_int(0)
@@ -239,7 +244,8 @@ class GpuLibrary(ReferenceAPI):
         self.lib.sbfs_tiles.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         self._ext("sbfs_tiles", group, bx, by, C.byref(fw), C.byref(mb), C.byref(gw), C.byref(cm))
-        names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_momflux", "k_predict_mf", "k_correct"]
+        names = ["k_props", "k_curv_list", "k_flux_force", "k_vof_advance", "k_momflux", "k_predict_mf",
+                 "k_correct", "k_csf_force"]
         out = {n: f"{bx[k]}x{by[k]}" for k, n in enumerate(names)}
         out["fft_cols"] = fw.value
         out["tdm_modes"] = mb.value

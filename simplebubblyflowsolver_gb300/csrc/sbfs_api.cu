@@ -92,6 +92,10 @@ struct Ctx {
   // role state of the fused step: current velocity, potential, density,
   // RK-source buffers
   double *U[2], *V[2], *PSI[2], *DEN[2], *SX[2], *SY[2], *SV[2];
+  // CSF force buffers: substage k uses IFX[k & 1], IFY[k & 1] (the last
+  // substage's in b.ifrcx, b.ifrcy, the reference's arrays)
+  double *IFX[2], *IFY[2];
+  double *VOF0 = nullptr;  // the first vof buffer (which of the two holds the current vof keys the graphs)
   int iu = 0, ipsi = 0, iden = 0, isrc = 0;
   bool resident = false;  // device holds the current state
   bool tuned = false;     // launch shapes picked by the autotuner
@@ -105,8 +109,9 @@ struct Ctx {
   // faces, the next substage's k_props beside the predictor, the Poisson
   // solve and the correction (fork / join events)
   cudaStream_t s2 = nullptr;
-  cudaEvent_t evf = nullptr, evd = nullptr, evp = nullptr, evx = nullptr;
+  cudaEvent_t evf = nullptr, evd = nullptr, evp = nullptr, evx = nullptr, evF = nullptr;
   bool props_ahead = false;  // the next substage's k_props is already on the side stream
+  bool geo_ahead = false;    // the next substage's interface geometry and force are already on the side stream
   // host-linked step (strict sync mode, host arrays the GPU can address): the
   // step copies the state in and out itself, on the copy stream s3, each
   // field as early as the step allows.  link_tab: page-locked table of the
@@ -140,6 +145,7 @@ struct Ctx {
     if (evd) cudaEventDestroy(evd);
     if (evp) cudaEventDestroy(evp);
     if (evx) cudaEventDestroy(evx);
+    if (evF) cudaEventDestroy(evF);
     for (cudaEvent_t e : evh)
       if (e) cudaEventDestroy(e);
     if (link_tab) cudaFreeHost(link_tab);
@@ -453,6 +459,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evx, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->evF, cudaEventDisableTiming));
   CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
   for (cudaEvent_t &e : c->evh) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CK(cudaHostAlloc(reinterpret_cast<void **>(&c->link_tab), sizeof(double *) * kLinkSlots * nc, cudaHostAllocMapped));
@@ -489,7 +496,8 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   double **scal[] = {&b.ux, &b.uy, &b.p, &b.psi0, &b.psi1, &b.vof, &b.ux_star, &b.uy_star, &b.den0, &b.den1,
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
-                     &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.egx, &b.egy, &b.pxx, &b.pyy, &b.pxy, &b.pyx};
+                     &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.egx, &b.egy, &b.pxx, &b.pyy, &b.pxy, &b.pyx,
+                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt};
   for (double **p : scal)
     if (dalloc(*c, p, n1 * nc)) return 1;
   if (dalloc(*c, &b.dvof, n2 * nc)) return 1;
@@ -516,6 +524,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   if (dalloc(*c, &tmp, (size_t)nc + 1)) return 1;  // nc cell counts, then nc face counts
   b.icount = reinterpret_cast<int *>(tmp);
   b.fcount = b.icount + nc;
+  if (dalloc(*c, &b.tf, (size_t)kThincTabs * c->nx * c->ny * nc)) return 1;
   // scalars of every case, then one status word per case
   if (dalloc(*c, &tmp, (size_t)kScalars * nc + nc / 2 + 2)) return 1;
   b.scalars = tmp;
@@ -544,6 +553,11 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   c->SY[1] = b.srcuy[1];
   c->SV[0] = b.srcvof[0];
   c->SV[1] = b.srcvof[1];
+  c->IFX[0] = b.ifrcx;
+  c->IFX[1] = b.ifrcx2;
+  c->IFY[0] = b.ifrcy;
+  c->IFY[1] = b.ifrcy2;
+  c->VOF0 = b.vof;
   return 0;
 }
 
@@ -652,11 +666,21 @@ struct Prof {
 
 enum KernelClass {
   KC_PROPS, KC_CURV_LIST, KC_INTERFACE, KC_FLUX_FORCE, KC_VOF_ADVANCE, KC_MOMFLUX, KC_PREDICT,
-  KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_MLP_CURV, KC_COUNT
+  KC_POISSON_FWD, KC_POISSON_TDM, KC_POISSON_INV, KC_CORRECT, KC_DECIDE_DT, KC_MLP_CURV,
+  KC_CSF_FORCE, KC_FACE_FLUX, KC_BULK_FLUX, KC_COUNT
 };
 const char *kKernelNames[KC_COUNT] = {"k_props", "k_curv_list", "k_interface_cells", "k_flux_force", "k_vof_advance", "k_momflux",
                                       "k_predict_mf", "k_poisson_fwd", "k_poisson_tdm", "k_poisson_inv", "k_correct",
-                                      "k_decide_dt", "k_mlp_curv"};
+                                      "k_decide_dt", "k_mlp_curv", "k_csf_force", "k_face_flux", "k_bulk_flux"};
+
+// 1: the interface geometry of a substage (curvature, interface-cell list,
+// THINC factors, CSF force) runs ahead of its velocity, beside the previous
+// substage's predictor and Poisson solve, and the VOF update forms the face
+// fluxes itself (k_vof_advance_itf, into the second vof buffer); 0: after
+// the correction, with the listed faces (k_curv_list<true>,
+// k_interface_cells, k_flux_force) and the VOF update in place.  The same
+// results bit for bit.
+int g_geo_ahead = 1;
 
 // curvature model of the fused step: 0 = the reference's kappa = -div n,
 // 1 = the learned closure in interface cells (plain kappa outside its range)
@@ -755,11 +779,20 @@ void link_out(Ctx &c, int slot, const Layout &l, double *dev) {
 }
 
 // par: decide_dt runs on the side stream (forked by enqueue_step, joined
-// before the first use of its scalars when wait_dt), and so do the bulk
-// fluxes and the force (beside the listed interface faces) and the next
-// substage's k_props once this substage's last reader of the viscosities and
-// corner normals (k_momflux) is enqueued.  The main stream waits for them
-// before anything reads what they write.
+// before the first use of its scalars when wait_dt), and so does whatever
+// does not wait for the main stream's latest result; the main stream waits
+// for it before anything reads what it writes.  With the geometry ahead
+// (g_geo_ahead, the default) the side stream runs:
+//   * the bulk fluxes beside the listed faces (in substage 0 beside k_props
+//     and the geometry too);
+//   * in substage 0, the CSF force beside the listed faces, the VOF update
+//     (which writes vof^{k+1} to the other vof buffer) and k_momflux;
+//   * once k_momflux (the last reader of the viscosities and corner normals)
+//     is enqueued, the next substage's k_props, geometry and CSF force (into
+//     the other force buffer) from the new vof and density, beside this
+//     substage's predictor, Poisson solve and correction.
+// Otherwise (the first form): the bulk fluxes and the force beside the
+// listed interface faces, the next substage's k_props ahead.
 void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   Bufs &b = c.b;
   if (k != 0) c.isrc ^= 1;  // stash the previous stage's sources (pointer swap)
@@ -770,34 +803,83 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   double *sya = c.SY[c.isrc], *syb = c.SY[c.isrc ^ 1];
   double *sva = c.SV[c.isrc], *svb = c.SV[c.isrc ^ 1];
   const double *sc = b.scalars;
-  if (c.props_ahead) {
-    cudaStreamWaitEvent(c.s, c.evp, 0);
-    c.props_ahead = false;
-  } else {
-    timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
-  }
-  if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
-  timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
   const bool learned = g_curv_model != 0;
-  if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
-  if (par) {
-    // the faces of single-phase upwind cells and the CSF force need only the
-    // curvature: they run on the side stream beside the listed interface
-    // faces (a few percent of the faces, a kernel that fills the GPU only
-    // partly); the two write disjoint faces, and k_vof_advance waits for both
-    cudaEventRecord(c.evf, c.s);
-    cudaStreamWaitEvent(c.s2, c.evf, 0);
-    launch_interface_stage(c.s2, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2);
-    cudaEventRecord(c.evx, c.s2);
-    launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1);
-    cudaStreamWaitEvent(c.s, c.evx, 0);
+  const bool ahead = g_geo_ahead != 0;
+  double *ifx = ahead ? c.IFX[k & 1] : b.ifrcx, *ify = ahead ? c.IFY[k & 1] : b.ifrcy;
+  bool force_side = false;  // this substage's force is running on the side stream (evF)
+  if (ahead) {
+    if (c.geo_ahead) {
+      // geometry and force came ahead on the side stream; the bulk fluxes
+      // follow them there, beside the listed faces
+      cudaStreamWaitEvent(c.s, c.evp, 0);
+      c.geo_ahead = false;
+      cudaEventRecord(c.evf, c.s);
+      cudaStreamWaitEvent(c.s2, c.evf, 0);
+      launch_bulk_flux(c.s2, c.g, c.m, c.ph, b, ux, uy);
+      cudaEventRecord(c.evx, c.s2);
+    } else {
+      // substage 0 (or a profiled step): the bulk fluxes first on the side
+      // stream (after decide_dt, which waited for the state), the geometry
+      // here, then the force on the side stream beside the listed faces and
+      // the VOF update (which leaves vof^k in place)
+      if (par) {
+        cudaEventRecord(c.evf, c.s);
+        cudaStreamWaitEvent(c.s2, c.evf, 0);
+        launch_bulk_flux(c.s2, c.g, c.m, c.ph, b, ux, uy);
+        cudaEventRecord(c.evx, c.s2);
+      }
+      timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+      timed(c, KC_CURV_LIST, [&] { launch_geometry(c.s, c.g, c.m, b); });
+      if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
+      if (par) {
+        cudaEventRecord(c.evf, c.s);
+        cudaStreamWaitEvent(c.s2, c.evf, 0);
+        launch_csf_force(c.s2, c.g, c.m, c.ph, b, den0, ifx, ify, learned);
+        cudaEventRecord(c.evF, c.s2);
+        force_side = true;
+      } else {
+        timed(c, KC_CSF_FORCE, [&] { launch_csf_force(c.s, c.g, c.m, c.ph, b, den0, ifx, ify, learned); });
+      }
+    }
+    if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
+    timed(c, KC_FACE_FLUX, [&] { launch_face_flux(c.s, c.g, b, ux, uy); });
+    if (par)
+      cudaStreamWaitEvent(c.s, c.evx, 0);
+    else
+      timed(c, KC_BULK_FLUX, [&] { launch_bulk_flux(c.s, c.g, c.m, c.ph, b, ux, uy); });
+    if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
+    timed(c, KC_VOF_ADVANCE,
+          [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1, b.vof_alt); });
+    std::swap(b.vof, b.vof_alt);  // vof^{k+1} is the current vof
   } else {
-    timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
-    timed(c, KC_FLUX_FORCE,
-          [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
+    if (c.props_ahead) {
+      cudaStreamWaitEvent(c.s, c.evp, 0);
+      c.props_ahead = false;
+    } else {
+      timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+    }
+    if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
+    timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
+    if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
+    if (par) {
+      // the faces of single-phase upwind cells and the CSF force need only the
+      // curvature: they run on the side stream beside the listed interface
+      // faces (a few percent of the faces, a kernel that fills the GPU only
+      // partly); the two write disjoint faces, and k_vof_advance waits for both
+      cudaEventRecord(c.evf, c.s);
+      cudaStreamWaitEvent(c.s2, c.evf, 0);
+      launch_interface_stage(c.s2, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2);
+      cudaEventRecord(c.evx, c.s2);
+      launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1);
+      cudaStreamWaitEvent(c.s, c.evx, 0);
+    } else {
+      timed(c, KC_INTERFACE, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 1); });
+      timed(c, KC_FLUX_FORCE,
+            [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, learned ? 3 : 2); });
+    }
+    if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
+    timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   }
-  if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
-  timed(c, KC_VOF_ADVANCE, [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1); });
   if (c.link && k == 2) link_out(c, HL_VOF_OUT, L_VOF, b.vof);  // vof is final
   // the last substage leaves txy at the walls for the wall-stress log (all of
   // txx, txy, tyy when every array is synchronised), as the reference's
@@ -805,19 +887,29 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   const int stress = k < 2 ? 0 : (g_sync_mode == SBFS_SYNC_ALL ? 2 : 1);
   timed(c, KC_MOMFLUX, [&] { launch_momflux(c.s, c.g, c.m, c.ph, b, ux, uy, stress); });
   if (par && k < 2) {
-    // the next substage's viscosities and corner normals need only the new
+    // the next substage's viscosities and corner normals (and, ahead, its
+    // geometry and force from the new vof and density) need only the new
     // vof: they run beside this substage's predictor, Poisson solve and
-    // correction, none of which reads them
+    // correction, none of which reads what they write
     cudaEventRecord(c.evf, c.s);
     cudaStreamWaitEvent(c.s2, c.evf, 0);
     launch_props(c.s2, c.g, c.m, c.ph, b, false, true, true, nullptr);
+    if (ahead) {
+      launch_geometry(c.s2, c.g, c.m, b);
+      if (learned) launch_mlp_curv(c.s2, c.g, b);
+      launch_csf_force(c.s2, c.g, c.m, c.ph, b, den1, c.IFX[(k + 1) & 1], c.IFY[(k + 1) & 1], learned);
+      c.geo_ahead = true;
+    } else {
+      c.props_ahead = true;
+    }
     cudaEventRecord(c.evp, c.s2);
-    c.props_ahead = true;
   }
+  if (force_side) cudaStreamWaitEvent(c.s, c.evF, 0);
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[2], 0);  // p is in
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[3], 0);  // psi is in
   timed(c, KC_PREDICT, [&] {
-    launch_predict_mf(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, den0, den1, psio, sxa, sxb, sya, syb);
+    launch_predict_mf(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, den0, den1, psio, sxa, sxb, sya, syb, ifx,
+                      ify);
   });
   timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, b, sc, k, uxs, uys); });
   timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
@@ -836,6 +928,7 @@ void enqueue_step(Ctx &c) {
   // profiled steps keep every launch on the main stream (events per launch)
   const bool par = !g_prof.on;
   c.props_ahead = false;
+  c.geo_ahead = false;
   if (c.link) link_in(c);
   if (par) {
     cudaEventRecord(c.evf, c.s);
@@ -880,7 +973,10 @@ int autotune(Ctx &c) {
     CK(cudaMemcpyAsync(save[q], live[q], n * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
   }
   const int iu = c.iu, ipsi = c.ipsi, iden = c.iden, isrc = c.isrc;
+  double *const vof_cur = c.b.vof, *const vof_oth = c.b.vof_alt;
   auto restore = [&]() -> int {
+    c.b.vof = vof_cur;
+    c.b.vof_alt = vof_oth;
     c.iu = iu;
     c.ipsi = ipsi;
     c.iden = iden;
@@ -906,7 +1002,7 @@ int autotune(Ctx &c) {
     if (G * mb <= 4 && poisson_tdm_smem(c.nx, mb, G) <= 200 * 1024) tdms.push_back({mb, G});
   if (tdms.empty()) tdms.push_back({1, G});  // one pair per block (staged in global memory above ~6900 rows)
   const int tk_of[KC_COUNT] = {TK_PROPS, TK_CURV_LIST, -1, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_MOMFLUX, TK_PREDICT,
-                               -1, -1, -1, TK_CORRECT, -1, -1};
+                               -1, -1, -1, TK_CORRECT, -1, -1, TK_FORCE, -1, TK_FLUX_FORCE};
   Tiles best = c.b.tiles;
   float best_ms[TK_COUNT];
   for (int k = 0; k < TK_COUNT; ++k) best_ms[k] = 1e30f;
@@ -1029,7 +1125,8 @@ int autotune(Ctx &c) {
 
 int role_key(const Ctx &c) {
   return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
-         (g_pdl << 6) | ((g_compact + 1) << 7) | ((g_sync_mode == SBFS_SYNC_ALL) << 9);
+         (g_pdl << 6) | ((g_compact + 1) << 7) | ((g_sync_mode == SBFS_SYNC_ALL) << 9) | (g_geo_ahead << 10) |
+         ((c.b.vof != c.VOF0) << 11);
 }
 
 int launch_step(Ctx &c) {
@@ -1077,6 +1174,7 @@ int launch_step(Ctx &c) {
   }
   if (it == c.graphs.end()) {
     const int iu = c.iu, ipsi = c.ipsi, iden = c.iden, isrc = c.isrc;
+    double *const vof = c.b.vof, *const vof_alt = c.b.vof_alt;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
     enqueue_step(c);
@@ -1093,13 +1191,17 @@ int launch_step(Ctx &c) {
     c.ipsi = ipsi;
     c.iden = iden;
     c.isrc = isrc;
+    c.b.vof = vof;
+    c.b.vof_alt = vof_alt;
   }
   CK(cudaGraphLaunch(it->second, c.s));
   // roles after one step (3 substages: velocity, potential and density flip
-  // three times, the RK sources twice)
+  // three times, the RK sources twice, the two vof buffers three times when
+  // the geometry runs ahead)
   c.iu ^= 1;
   c.ipsi ^= 1;
   c.iden ^= 1;
+  if (g_geo_ahead) std::swap(c.b.vof, c.b.vof_alt);
   return 0;
 }
 
@@ -1338,6 +1440,11 @@ int sbfs_set_compaction(int mode) {
   return 0;
 }
 
+int sbfs_set_geometry_ahead(int on) {
+  g_geo_ahead = on ? 1 : 0;
+  return 0;
+}
+
 int sbfs_set_host_link(int on) {
   if (on < 0 || on > 2) return fail("bad host-link mode %d", on);
   g_host_link = on;
@@ -1371,7 +1478,7 @@ int sbfs_invalidate_device(void) {
   return 0;
 }
 
-int sbfs_kernels_per_step(void) { return kKernelsPerStep + (g_curv_model ? 3 : 0); }
+int sbfs_kernels_per_step(void) { return kKernelsPerStep + (g_geo_ahead ? 3 : 0) + (g_curv_model ? 3 : 0); }
 
 int sbfs_set_curvature_model(int model) {
   if (model != 0 && model != 1) return fail("bad curvature model %d", model);

@@ -206,13 +206,27 @@ __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const
 // components along and across it.  With a = K exp(-2 n_a s) and
 // b = exp(-2 n_b g) the two terms are 1 / (1 + a b) and b / (b + a).
 // The caller passes -2 n_a s, which for s = -+1/2 is exactly +-n_a.
-__device__ __forceinline__ double thinc_face(double m2nas, double nb, double K) {
-  const double a = K * exp(m2nas);
-  const double b = exp(-2. * kGaussPt * nb);
+// vel phi for the vof phi of a single-phase upwind cell, the same bits as
+// the product: phi = +0 gives a zero of vel's sign, phi = 1 gives vel (vel is
+// finite), and only other values (the few cells within vofmin of 0 or 1)
+// take a multiply
+__device__ __forceinline__ double vel_phi(double vel, double phi) {
+  const long long pb = dbits(phi);
+  if (pb == 0) return __longlong_as_double(dbits(vel) & (long long)0x8000000000000000ULL);
+  if (pb == 0x3FF0000000000000LL) return vel;
+  return __dmul_rn(vel, phi);
+}
+
+__device__ __forceinline__ double thinc_ab(double a, double b) {
   const double p = fma(a, b, 1.);
   const double q = b + a;
   // b p + q >= b >= exp(-2 g) > 1/2: positive and normal
   return half_pos_normal(fma(b, p, q)) * rcp_nr(p * q);
+}
+// a is rounded on its own (never fused into q = b + a), so that a factor
+// formed ahead of time (k_curv_list<false>) gives the same flux
+__device__ __forceinline__ double thinc_face(double m2nas, double nb, double K) {
+  return thinc_ab(__dmul_rn(K, exp(m2nas)), exp(-2. * kGaussPt * nb));
 }
 
 // ---------------------------------------------------------------------------
@@ -232,13 +246,13 @@ __device__ __forceinline__ double face_kappa_sum(double pl, double pr, double kl
   return il == ir ? kl + kr : (il ? 2. * kl : 2. * kr);
 }
 
-template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY = false, bool ITF_KAPPA = false>
-__global__ void __launch_bounds__(BX *BY)
-    k_flux_force(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
-                 const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
-                 const double *__restrict__ curv, double *__restrict__ fluxx, double *__restrict__ fluxy,
-                 double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
-  pdl_entry();
+template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY, bool ITF_KAPPA>
+__device__ __forceinline__ void flux_force_body(const Grid &g, const Metrics &m, const Phys &ph0,
+                                                const double *__restrict__ ux, const double *__restrict__ uy,
+                                                const double *__restrict__ vof, const double *__restrict__ normal,
+                                                const double *__restrict__ den0, const double *__restrict__ curv,
+                                                double *__restrict__ fluxx, double *__restrict__ fluxy,
+                                                double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
   const Phys ph = zphys(g, ph0);
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -255,7 +269,7 @@ __global__ void __launch_bounds__(BX *BY)
       const int iu = n ? I : I - 1;
       const double phi = n ? v0 : vxm;
       if (single_phase(phi)) {
-        fluxx[ix(g, r, I - 1)] = vel * phi;
+        fluxx[ix(g, r, I - 1)] = vel_phi(vel, phi);
       } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)r * g.p3 + (size_t)(iu - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
@@ -268,7 +282,7 @@ __global__ void __launch_bounds__(BX *BY)
       const int ru = n ? r : rm;
       const double phi = n ? v0 : vym;
       if (single_phase(phi)) {
-        fluxy[ix(g, r, I)] = vel * phi;
+        fluxy[ix(g, r, I)] = vel_phi(vel, phi);
       } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)ru * g.p3 + (size_t)(I - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
@@ -308,12 +322,44 @@ __global__ void __launch_bounds__(BX *BY)
   }
 }
 
+template <bool FLUX, bool FORCE, bool HAVE_K, bool BULK_ONLY = false, bool ITF_KAPPA = false>
+__global__ void __launch_bounds__(BX *BY)
+    k_flux_force(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
+                 const double *__restrict__ vof, const double *__restrict__ normal, const double *__restrict__ den0,
+                 const double *__restrict__ curv, double *__restrict__ fluxx, double *__restrict__ fluxy,
+                 double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
+  pdl_entry();
+  flux_force_body<FLUX, FORCE, HAVE_K, BULK_ONLY, ITF_KAPPA>(g, m, ph0, ux, uy, vof, normal, den0, curv, fluxx, fluxy,
+                                                             ifrcx, ifrcy);
+}
+
+// the fluxes of the faces whose upwind cell is single-phase (flux = vel phi)
+// and the wall faces; the faces of upwind interface cells are k_face_flux's
+__global__ void __launch_bounds__(BX *BY)
+    k_bulk_flux(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
+                const double *__restrict__ vof, double *__restrict__ fluxx, double *__restrict__ fluxy) {
+  pdl_entry();
+  flux_force_body<true, false, true, true, false>(g, m, ph0, ux, uy, vof, nullptr, nullptr, nullptr, fluxx, fluxy,
+                                                  nullptr, nullptr);
+}
+
+// the CSF force alone (it needs no velocity), into the force buffers given
+template <bool ITF_KAPPA>
+__global__ void __launch_bounds__(BX *BY)
+    k_csf_force(Grid g, Metrics m, Phys ph0, const double *__restrict__ vof, const double *__restrict__ den0,
+                const double *__restrict__ curv, double *__restrict__ ifrcx, double *__restrict__ ifrcy) {
+  pdl_entry();
+  flux_force_body<false, true, false, false, ITF_KAPPA>(g, m, ph0, nullptr, nullptr, vof, nullptr, den0, curv,
+                                                        nullptr, nullptr, ifrcx, ifrcy);
+}
+
 // ---------------------------------------------------------------------------
 // Interface compaction of the fused step.  THINC work (normal, intercept,
 // two exponentials per face) exists only in interface cells, a few percent
 // of the domain scattered along the bubbles; done in place it makes whole
-// warps wait on a few lanes.  So:
-//   k_curv_list       curvature of every cell (curvature_tensor.c:100-135),
+// warps wait on a few lanes.  Two arrangements, the same arithmetic:
+// listed faces (the step's first form):
+//   k_curv_list<true> curvature of every cell (curvature_tensor.c:100-135),
 //                     a list of the interface cells and a list of the faces
 //                     they are upwind of (block-aggregated appends)
 //   k_interface_cells one thread per listed face: the cell's normal and
@@ -325,6 +371,18 @@ __global__ void __launch_bounds__(BX *BY)
 //                     flux = vel phi) and the CSF force
 // Each face is written by exactly one of them: the upwind choice and the
 // vofmin test are the same integer tests in both.
+// geometry ahead (the default): everything but the upwind choice depends on
+// vof alone, so it runs beside the previous substage's predictor and
+// Poisson solve, and no flux kernel stands between the correction and the
+// VOF update:
+//   k_curv_list<false> curvature, the interface-cell list and per interface
+//                     cell its THINC factors K exp(+-n_a) for its four faces
+//                     and exp(-2 g n_b) across x and y faces (the block's
+//                     interface cells handed to its first threads)
+//   k_csf_force       the CSF force
+//   k_face_flux       one thread per face of a listed cell: the upwind test,
+//                     then the THINC flux from the cell's factors
+//   k_bulk_flux       every other face, as k_flux_force<.., BULK_ONLY>
 // ---------------------------------------------------------------------------
 // kappa = -div n of cell (I, J) of a case from its four corner normals
 // (curvature_tensor.c:100-135)
@@ -339,19 +397,63 @@ __device__ __forceinline__ void cell_curv(const Grid &g, const Metrics &m, const
   curv[ix(g, r, I)] = -fma(m.hihxxc[I], ddx, g.hihy * ddy);
 }
 
+// unit normal (n0, n1) and K = 1/phi - 1 of interface cell (I, J) of a case
+// (curvature_tensor.c:51-97)
+__device__ __forceinline__ void cell_normal_k(const Grid &g, const Metrics &m, const double2 *__restrict__ dv,
+                                              const double *__restrict__ vof, int zr, int I, int J, double &n0,
+                                              double &n1, double &K) {
+  const size_t q = g.p2 / 2;
+  const int r = J - 1 + zr, rp = wrap(J + 1, g.ny) + zr;
+  const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
+  const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
+  const double mx = (((d00.x + d10.x) + d01.x) + d11.x) * m.ihxxc[I];
+  const double my = (((d00.y + d10.y) + d01.y) + d11.y) * g.ihy;
+  const double inv = inv_norm(fma(mx, mx, my * my));
+  n0 = mx * inv;
+  n1 = my * inv;
+  K = rcp_nr(vof[ix(g, r, I)]) - 1.;
+}
+
+// THINC factors of interface cell (I, J), stored at its cell index `at`
+// (planar, cap entries a table, kThincTabs of them): a of its left, right,
+// bottom and top faces (thinc_face's K exp(-2 n_a s)), then b of its x and
+// of its y faces
+__device__ __forceinline__ void cell_thinc_factors(const Grid &g, const Metrics &m, const double2 *__restrict__ dv,
+                                                   const double *__restrict__ vof, int zr, int I, int J,
+                                                   double *__restrict__ tf, size_t cap, int at) {
+  double n0, n1, K;
+  cell_normal_k(g, m, dv, vof, zr, I, J, n0, n1, K);
+  tf[at] = __dmul_rn(K, exp(n0));
+  tf[cap + at] = __dmul_rn(K, exp(-n0));
+  tf[2 * cap + at] = __dmul_rn(K, exp(n1));
+  tf[3 * cap + at] = __dmul_rn(K, exp(-n1));
+  tf[4 * cap + at] = exp(-2. * kGaussPt * n1);
+  tf[5 * cap + at] = exp(-2. * kGaussPt * n0);
+}
+
 // compact: the cells with a corner normal hand their curvature to the
 // block's first threads (interface-branch compaction); otherwise each thread
 // computes its own.  The same arithmetic either way.
+// FACES: also the list of the faces the interface cells are upwind of (from
+// the velocity); else, without the velocity, the THINC factors of every
+// interface cell (tables by cell index), by the block's first threads
+template <bool FACES>
 __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const double *__restrict__ vof,
                                                       const double *__restrict__ dvof, const double *__restrict__ ux,
                                                       const double *__restrict__ uy, double *__restrict__ curv,
                                                       int *__restrict__ list, int *__restrict__ count,
-                                                      int *__restrict__ flist, int *__restrict__ fcount, int compact) {
+                                                      int *__restrict__ flist, int *__restrict__ fcount,
+                                                      double *__restrict__ tf, int compact) {
   pdl_entry();
-  list += (size_t)blockIdx.z * ((size_t)g.nx * g.ny);
+  const size_t cap = (size_t)g.nx * g.ny;
+  list += (size_t)blockIdx.z * cap;
   count += (size_t)blockIdx.z * (1);
-  flist += (size_t)blockIdx.z * (4 * (size_t)g.nx * g.ny);
-  fcount += (size_t)blockIdx.z * (1);
+  if (FACES) {
+    flist += (size_t)blockIdx.z * (4 * cap);
+    fcount += (size_t)blockIdx.z * (1);
+  } else {
+    tf += (size_t)blockIdx.z * (kThincTabs * cap);
+  }
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const bool in = I <= g.nx && J <= g.ny;
@@ -370,7 +472,7 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
     if (!kap) curv[ix(g, r, I)] = -0.;
     else if (!compact) cell_curv(g, m, dv, curv, zr, I, J);
     itf = !single_phase(vof[ix(g, r, I)]);
-    if (itf) {
+    if (FACES && itf) {
       // upwind tests of update/fluxx.c, fluxy.c; the wall faces belong to k_flux_force
       up |= (I >= 2 && neg(ux[ix(g, r, I - 1)])) ? 1u : 0u;
       up |= (I < g.nx && !neg(ux[ix(g, r, I)])) ? 2u : 0u;
@@ -388,18 +490,21 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
   const unsigned below = (1u << lane) - 1u;
   const unsigned kmask = __ballot_sync(0xffffffffu, kap);
   const unsigned mask = __ballot_sync(0xffffffffu, itf);
-  unsigned fm[4];
+  unsigned fm[4] = {0u, 0u, 0u, 0u};
   int nfw = 0;
+  if (FACES) {
 #pragma unroll
-  for (int f = 0; f < 4; ++f) {
-    fm[f] = __ballot_sync(0xffffffffu, (up >> f) & 1u);
-    nfw += __popc(fm[f]);
+    for (int f = 0; f < 4; ++f) {
+      fm[f] = __ballot_sync(0xffffffffu, (up >> f) & 1u);
+      nfw += __popc(fm[f]);
+    }
   }
   // per warp: its interface cell / face / curvature cell count, then its
   // offset in the block (lists) or among the block's curvature cells
   __shared__ int wofs[3][BX * BY / 32];
-  __shared__ int bbase[3];
+  __shared__ int bbase[3], btot[3];
   __shared__ int klist[BX * BY];
+  __shared__ int ilocal[FACES ? 1 : BX * BY];
   if (lane == 0) {
     wofs[0][warp] = __popc(mask);
     wofs[1][warp] = nfw;
@@ -413,25 +518,37 @@ __global__ void __launch_bounds__(BX *BY) k_curv_list(Grid g, Metrics m, const d
       wofs[tid][w] = run;
       run += c;
     }
+    btot[tid] = run;
     bbase[tid] = tid == 2 ? run : (run ? atomicAdd(tid == 0 ? count : fcount, run) : 0);
   }
   __syncthreads();
-  if (itf) list[bbase[0] + wofs[0][warp] + __popc(mask & below)] = cell;
-  int fo = bbase[1] + wofs[1][warp];
+  const int ipos = wofs[0][warp] + __popc(mask & below);  // this cell's place among the block's interface cells
+  if (itf) list[bbase[0] + ipos] = cell;
+  if (FACES) {
+    int fo = bbase[1] + wofs[1][warp];
 #pragma unroll
-  for (int f = 0; f < 4; ++f) {
-    if ((up >> f) & 1u) flist[fo + __popc(fm[f] & below)] = 4 * cell + f;
-    fo += __popc(fm[f]);
+    for (int f = 0; f < 4; ++f) {
+      if ((up >> f) & 1u) flist[fo + __popc(fm[f] & below)] = 4 * cell + f;
+      fo += __popc(fm[f]);
+    }
+  } else if (itf) {
+    ilocal[ipos] = tid;
   }
   // compacted curvature: the cells with a corner normal lie in the THINC
   // tails, often a few to a warp (the prefix of their counts came with the
   // lists' above)
-  if (!compact) return;  // uniform over the block
-  if (kap) klist[wofs[2][warp] + __popc(kmask & below)] = tid;
-  __syncthreads();
-  if (tid < bbase[2]) {
+  if (compact && kap) klist[wofs[2][warp] + __popc(kmask & below)] = tid;
+  if (!FACES || compact) __syncthreads();  // uniform over the block
+  if (compact && tid < bbase[2]) {
     const int sy = klist[tid] / blockDim.x, sx = klist[tid] - sy * blockDim.x;
     cell_curv(g, m, dv, curv, zr, blockIdx.x * blockDim.x + sx + 1, blockIdx.y * blockDim.y + sy + 1);
+  }
+  // the THINC factors of the block's interface cells
+  if (!FACES && tid < btot[0]) {
+    const int c = ilocal[tid];
+    const int sy = c / blockDim.x, sx = c - sy * blockDim.x;
+    const int Ic = blockIdx.x * blockDim.x + sx + 1, Jc = blockIdx.y * blockDim.y + sy + 1;
+    cell_thinc_factors(g, m, dv, vof, zr, Ic, Jc, tf, cap, (Jc - 1) * g.nx + (Ic - 1));
   }
 }
 
@@ -445,7 +562,6 @@ __global__ void __launch_bounds__(256)
   const int n = *fcount;
   const int zr = blockIdx.z * g.ny;  // first row of this case
   const double2 *dv = reinterpret_cast<const double2 *>(dvof);
-  const size_t q = g.p2 / 2;
   // one thread per upwind face of an interface cell: every thread runs the
   // same instructions (no face branches)
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -453,13 +569,8 @@ __global__ void __launch_bounds__(256)
     const int id = code >> 2, f = code & 3;
     const int r0 = id / g.nx, I = id - r0 * g.nx + 1;
     const int J = r0 + 1, r = r0 + zr, rp = wrap(J + 1, g.ny) + zr;
-    const double2 d00 = dv[(size_t)r * q + (I - 1)], d10 = dv[(size_t)r * q + I];
-    const double2 d01 = dv[(size_t)rp * q + (I - 1)], d11 = dv[(size_t)rp * q + I];
-    const double mx = (((d00.x + d10.x) + d01.x) + d11.x) * m.ihxxc[I];
-    const double my = (((d00.y + d10.y) + d01.y) + d11.y) * g.ihy;
-    const double inv = inv_norm(fma(mx, mx, my * my));
-    const double n0 = mx * inv, n1 = my * inv;
-    const double K = rcp_nr(vof[ix(g, r, I)]) - 1.;
+    double n0, n1, K;
+    cell_normal_k(g, m, dv, vof, zr, I, J, n0, n1, K);
     // face f: 0 left (x face I), 1 right (x face I + 1), 2 bottom (y face J - 1/2), 3 top (J + 1/2)
     const bool xf = f < 2;
     const double na = xf ? n0 : n1, nb = xf ? n1 : n0;
@@ -480,12 +591,14 @@ __global__ void __launch_bounds__(256)
 //   src = (F_x(i) - F_x(i+1)) / HXXC + (F_y(j) - F_y(j+1)) / hy
 // FUSED additionally writes rho^{k+1} (src/fluid/density.c) and the mass
 // fluxes u + (rho_r - 1) flux into separate buffers
-// (src/interface/mass_flux.c:10-58).
+// (src/interface/mass_flux.c:10-58).  OUT: vof^{k+1} goes to vof_out
+// (the geometry-ahead step, whose side stream still reads vof^k), else in
+// place.
 // thread (I, J): I = 1..nx
 // ---------------------------------------------------------------------------
-template <bool FUSED>
+template <bool FUSED, bool OUT>
 __global__ void __launch_bounds__(BX *BY)
-    k_vof_advance(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, double *__restrict__ vof,
+    k_vof_advance(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, double *vof, double *vof_out,
                   const double *__restrict__ fluxx, const double *__restrict__ fluxy, double *__restrict__ src_a,
                   const double *__restrict__ src_b, const double *__restrict__ ux, const double *__restrict__ uy,
                   double *__restrict__ mfx, double *__restrict__ mfy, double *__restrict__ den1) {
@@ -504,9 +617,10 @@ __global__ void __launch_bounds__(BX *BY)
   double v = vof[ix(g, r, I)];
   v = fma(sc[sc_adt(k)], s, v);
   if (k != 0) v = fma(sc[sc_bdt(k)], src_b[ix(g, r, I - 1)], v);
-  vof[ix(g, r, I)] = v;
-  if (I == 1) vof[ix(g, r, 0)] = 0.;
-  if (I == g.nx) vof[ix(g, r, g.nx + 1)] = 0.;
+  double *vo = OUT ? vof_out : vof;
+  vo[ix(g, r, I)] = v;
+  if (I == 1) vo[ix(g, r, 0)] = 0.;
+  if (I == g.nx) vo[ix(g, r, g.nx + 1)] = 0.;
   if (FUSED) {
     const double c = ph.dm1;
     den1[ix(g, r, I)] = clip_pos(fma(c, v, 1.), ph.den_lo, ph.den_hi);
@@ -521,6 +635,43 @@ __global__ void __launch_bounds__(BX *BY)
       mfx[ix(g, r, g.nx)] = fma(c, fxp, ux[ix(g, r, g.nx)]);
       mfy[ix(g, r, g.nx + 1)] = fma(c, fluxy[ix(g, r, g.nx + 1)], uy[ix(g, r, g.nx + 1)]);
     }
+  }
+}
+
+// one thread per face of a listed interface cell (four per cell, face f = 0
+// left, 1 right, 2 bottom, 3 top): the upwind test of update/fluxx.c and
+// fluxy.c, then, where the cell is upwind of the face, its THINC flux from
+// the cell's factors (k_curv_list<false>, tables by cell index) into fluxx /
+// fluxy.  The wall faces carry no flux.  Each block takes a contiguous share
+// of the entries, so that every SM gets some.
+__global__ void __launch_bounds__(256)
+    k_face_flux(Grid g, const double *__restrict__ ux, const double *__restrict__ uy, const int *__restrict__ list,
+                const int *__restrict__ count, const double *__restrict__ tf, double *__restrict__ fluxx,
+                double *__restrict__ fluxy) {
+  pdl_entry();
+  const size_t cap = (size_t)g.nx * g.ny;
+  list += (size_t)blockIdx.z * cap;
+  count += (size_t)blockIdx.z * (1);
+  tf += (size_t)blockIdx.z * (kThincTabs * cap);
+  const int n4 = 4 * *count;
+  const int zr = blockIdx.z * g.ny;  // first row of this case
+  const int per = ((n4 + (int)gridDim.x - 1) / (int)gridDim.x + 31) & ~31;
+  const int t0 = blockIdx.x * per, t1 = min(n4, t0 + per);
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    const int f = t & 3;
+    const int id = list[t >> 2];
+    const int r0 = id / g.nx, I = id - r0 * g.nx + 1;
+    const int J = r0 + 1, r = r0 + zr, rp = wrap(J + 1, g.ny) + zr;
+    const bool xf = f < 2;
+    const size_t at = xf ? ix(g, r, I - 1 + f) : ix(g, f == 2 ? r : rp, I);
+    const double vel = xf ? ux[at] : uy[at];
+    const bool up = f == 0 ? (I >= 2 && neg(vel)) : (f == 1 ? (I < g.nx && !neg(vel)) : (f == 2 ? neg(vel) : !neg(vel)));
+    if (!up) continue;
+    const double fl = vel * thinc_ab(tf[f * cap + id], tf[(4 + (f >> 1)) * cap + id]);
+    if (xf)
+      fluxx[at] = fl;
+    else
+      fluxy[at] = fl;
   }
 }
 
@@ -1300,6 +1451,7 @@ __global__ void __launch_bounds__(BX *BY)
   const int I = blockIdx.x * BX + threadIdx.x + 1;  // 1..nx+1
   unsigned long long mx = 0ULL, my = 0ULL;
   if (I <= g.nx) {
+#pragma unroll 4
     for (int J = blockIdx.y * BY + threadIdx.y + 1; J <= g.ny; J += gridDim.y * BY) {
       const int r = J - 1 + (int)blockIdx.z * g.ny;
       if (I >= 2) {
@@ -1340,8 +1492,9 @@ __global__ void __launch_bounds__(BX *BY)
   const double small = 1.e-8;
   double d = 1.;
   unsigned long long nb = 0ULL;
+  // the other blocks' atomics are done at L2 and fenced: read past L1
   for (int i = tid + 2; i <= g.nx; i += BX * BY) {
-    const unsigned long long b = atomicAdd(acc + i, 0ULL);
+    const unsigned long long b = __ldcg(acc + i);
     nb |= (b >= kInfBits) ? 1ULL : 0ULL;
     d = fmin(d, m.hxxf[i] / (__longlong_as_double((long long)b) + small));
   }
@@ -1356,7 +1509,7 @@ __global__ void __launch_bounds__(BX *BY)
     __syncthreads();
   }
   if (tid == 0) {
-    const unsigned long long by = atomicAdd(acc + g.nx + 2, 0ULL);
+    const unsigned long long by = __ldcg(acc + g.nx + 2);
     double dt = fmin(dmin[0], g.hy / (__longlong_as_double((long long)by) + small));
     dt *= coef_adv;
     dt = fmin(dt, dt_fixed);
@@ -1778,8 +1931,9 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
   const dim3 gr = tile_grid(b.tiles, TK_FLUX_FORCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_FLUX_FORCE);
   if (stage == 0) {
     cudaMemsetAsync(b.icount, 0, sizeof(int) * 2 * g.nc, s);  // cell and face counts
-    launch_pdl(k_curv_list, tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST), 0, s,
-        g, m, b.vof, b.dvof, ux, uy, b.curv, b.ilist, b.icount, b.flist, b.fcount, compaction(b.tiles));
+    launch_pdl(k_curv_list<true>, tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST),
+               0, s, g, m, b.vof, b.dvof, ux, uy, b.curv, b.ilist, b.icount, b.flist, b.fcount, (double *)nullptr,
+               compaction(b.tiles));
   } else if (stage == 1) {
     launch_pdl(k_interface_cells, dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s,
         g, m, ux, uy, b.vof, b.dvof, b.flist, b.fcount, b.fluxx, b.fluxy);
@@ -1792,16 +1946,46 @@ void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, con
   }
 }
 
+void launch_geometry(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b) {
+  cudaMemsetAsync(b.icount, 0, sizeof(int) * 2 * g.nc, s);  // cell and face counts
+  launch_pdl(k_curv_list<false>, tile_grid(b.tiles, TK_CURV_LIST, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_CURV_LIST),
+             0, s, g, m, b.vof, b.dvof, (const double *)nullptr, (const double *)nullptr, b.curv, b.ilist, b.icount,
+             b.flist, b.fcount, b.tf, compaction(b.tiles));
+}
+
+void launch_bulk_flux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                      const double *ux, const double *uy) {
+  launch_pdl(k_bulk_flux, tile_grid(b.tiles, TK_FLUX_FORCE, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_FLUX_FORCE), 0, s,
+             g, m, ph, ux, uy, b.vof, b.fluxx, b.fluxy);
+}
+
+void launch_csf_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                      const double *den0, double *ifx, double *ify, bool itf_kappa) {
+  const dim3 gr = tile_grid(b.tiles, TK_FORCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_FORCE);
+  if (itf_kappa)
+    launch_pdl(k_csf_force<true>, gr, bl, 0, s, g, m, ph, b.vof, den0, b.curv, ifx, ify);
+  else
+    launch_pdl(k_csf_force<false>, gr, bl, 0, s, g, m, ph, b.vof, den0, b.curv, ifx, ify);
+}
+
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                         const double *sc, int k, double *src_a, const double *src_b, bool fused, const double *ux,
-                        const double *uy, double *den1) {
+                        const double *uy, double *den1, double *vof_out) {
   const dim3 gr = tile_grid(b.tiles, TK_VOF_ADVANCE, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_VOF_ADVANCE);
-  if (fused)
-    launch_pdl(k_vof_advance<true>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, b.mfluxx,
-                                          b.mfluxy, den1);
+  if (fused && vof_out)
+    launch_pdl(k_vof_advance<true, true>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, vof_out, b.fluxx, b.fluxy, src_a, src_b,
+               ux, uy, b.mfluxx, b.mfluxy, den1);
+  else if (fused)
+    launch_pdl(k_vof_advance<true, false>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, (double *)nullptr, b.fluxx, b.fluxy,
+               src_a, src_b, ux, uy, b.mfluxx, b.mfluxy, den1);
   else
-    launch_pdl(k_vof_advance<false>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, b.fluxx, b.fluxy, src_a, src_b, ux, uy, nullptr,
-                                           nullptr, nullptr);
+    launch_pdl(k_vof_advance<false, false>, gr, bl, 0, s, g, m, ph, sc, k, b.vof, (double *)nullptr, b.fluxx, b.fluxy,
+               src_a, src_b, ux, uy, (double *)nullptr, (double *)nullptr, (double *)nullptr);
+}
+
+void launch_face_flux(cudaStream_t s, const Grid &g, const Bufs &b, const double *ux, const double *uy) {
+  launch_pdl(k_face_flux, dim3(max(2, (4 * 152 + g.nc - 1) / g.nc), 1, g.nc), 256, 0, s, g, ux, uy, b.ilist, b.icount,
+             b.tf, b.fluxx, b.fluxy);
 }
 
 void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *ux,
@@ -1826,9 +2010,10 @@ void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
 void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                        const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
                        const double *den0, const double *den1, const double *psi_old, double *srcux_a,
-                       const double *srcux_b, double *srcuy_a, const double *srcuy_b) {
+                       const double *srcux_b, double *srcuy_a, const double *srcuy_b, const double *ifx,
+                       const double *ify) {
   launch_pdl(k_predict_mf, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g,
-             m, ph, sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, b.ifrcx, b.ifrcy, den0, den1,
+             m, ph, sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, ifx, ify, den0, den1,
              psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy, b.coltab);
 }
 
@@ -1917,7 +2102,7 @@ void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phy
                       const double *ux, const double *uy, double dt_fixed, double coef_adv) {
   int gy = (g.ny + BY - 1) / BY;
   const int gx = (g.nx + BX) / BX;
-  while (gy > 1 && gx * gy * g.nc > 4 * 152) gy = (gy + 1) / 2;
+  while (gy > 1 && gx * gy * g.nc > 16 * 152) gy = (gy + 1) / 2;
   launch_pdl(k_decide_dt, dim3(gx, gy, g.nc), dim3(BX, BY), 0, s, g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
                                                     coef_adv, b.coltab);
 }

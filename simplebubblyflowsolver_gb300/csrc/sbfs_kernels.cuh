@@ -10,7 +10,10 @@ namespace sbfs {
 // launch shapes of the fused step, picked by the autotuner (sbfs_api.cu) or
 // the defaults below; results do not depend on them (every cell, column
 // and mode is computed independently of its block)
-enum TileKernel { TK_PROPS, TK_CURV_LIST, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_MOMFLUX, TK_PREDICT, TK_CORRECT, TK_COUNT };
+// (TK_FORCE: k_csf_force, the force alone when the geometry runs ahead)
+enum TileKernel {
+  TK_PROPS, TK_CURV_LIST, TK_FLUX_FORCE, TK_VOF_ADVANCE, TK_MOMFLUX, TK_PREDICT, TK_CORRECT, TK_FORCE, TK_COUNT
+};
 struct Tiles {
   unsigned short bx[TK_COUNT], by[TK_COUNT];  // block shape (bx * by <= 256)
   int fft_w;   // columns per block of the Poisson transforms: 1, 2, 4 or 8
@@ -21,6 +24,9 @@ struct Tiles {
                 // compacted to the first threads of each block; 0: done in place
 };
 Tiles default_tiles(int ny);
+
+// THINC factor tables per listed interface cell (Bufs::tf)
+constexpr int kThincTabs = 6;
 
 struct Bufs {
   // state
@@ -55,6 +61,15 @@ struct Bufs {
   // and their count (fcount = icount + nc)
   int *ilist, *icount;
   int *flist, *fcount;
+  // THINC factors of the interface cells (kThincTabs planar tables of nx * ny
+  // entries a case, by cell index; k_curv_list<false>), read by k_face_flux
+  double *tf;
+  // the second vof buffer: the geometry-ahead step writes vof^{k+1} there
+  // (the host code then swaps it with vof, which always holds the current vof)
+  double *vof_alt;
+  // second CSF force buffers: the force of the next substage is formed
+  // beside the predictor that reads this one's
+  double *ifrcx2, *ifrcy2;
   // launch shapes (host side)
   Tiles tiles;
 };
@@ -73,9 +88,10 @@ void launch_flux_force(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
 // with the face curvature taken from the interface side (learned curvature)
 void launch_interface_stage(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                             const double *ux, const double *uy, const double *den0, int stage);
+// vof_out: vof^{k+1} there instead of in place (fused only)
 void launch_vof_advance(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                         const double *sc, int k, double *src_a, const double *src_b, bool fused,
-                        const double *ux, const double *uy, double *den1);
+                        const double *ux, const double *uy, double *den1, double *vof_out = nullptr);
 void launch_mass_flux_inplace(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b,
                               const double *ux, const double *uy);
 // the reference's txx, txy, tyy (fine-grained entry point)
@@ -93,12 +109,26 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
 // reads it), 2 the whole of txx, txy, tyy
 void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                     const double *ux, const double *uy, int stress);
-// fused step: the predictor from those fluxes; also writes e grad psi_old at
-// the faces (b.egx, b.egy) for the Poisson right-hand side and the correction
+// fused step: the predictor from those fluxes and the CSF force ifx, ify;
+// also writes e grad psi_old at the faces (b.egx, b.egy) for the Poisson
+// right-hand side and the correction
 void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                        const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
                        const double *den0, const double *den1, const double *psi_old, double *srcux_a,
-                       const double *srcux_b, double *srcuy_a, const double *srcuy_b);
+                       const double *srcux_b, double *srcuy_a, const double *srcuy_b, const double *ifx,
+                       const double *ify);
+// fused step with the interface geometry ahead of the velocity: curvature,
+// interface-cell list and the cells' THINC factors from vof and the corner
+// normals alone (counts reset first)
+void launch_geometry(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b);
+// the THINC fluxes of the faces the listed interface cells are upwind of
+void launch_face_flux(cudaStream_t s, const Grid &g, const Bufs &b, const double *ux, const double *uy);
+// the fluxes of every other face (upwind cell single-phase, walls)
+void launch_bulk_flux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                      const double *ux, const double *uy);
+// the CSF force into ifx, ify (itf_kappa: the learned closure's face curvature)
+void launch_csf_force(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
+                      const double *den0, double *ifx, double *ify, bool itf_kappa);
 // the Poisson solve; the right-hand side reads b.egx, b.egy
 void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                     const double *uy, double *psi_new);

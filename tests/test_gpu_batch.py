@@ -277,3 +277,36 @@ def test_batch_learned_curvature_on_the_ensemble_grids(libs):
     for k, (a, b) in enumerate(zip(batch, alone)):
         for s in SLOTS:
             assert np.array_equal(a.field(s), b.field(s)), (k, s)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("resident", [False, True], ids=["linked", "resident"])
+def test_batch_geometry_ahead_identical(libs, resident):
+    """the benchmarked ensemble's three grids batched, with the interface
+    geometry and force formed ahead of the velocity (on the side stream,
+    beside the VOF update and the predictor of other substages) and after
+    the correction: the same bits, in strict (host-linked) and resident
+    steps.  Guards the ordering of the side stream against the in-place
+    updates of the main one (vof, velocity)."""
+    gpu, orc = libs
+    wls = ensemble_extremes()
+    st0 = prepare(gpu, orc, wls)
+    runs = {}
+    try:
+        for ahead in (False, True):
+            gpu.set_geometry_ahead(ahead)
+            gpu.set_sync_mode(SYNC_NONE if resident else SYNC_STATE)
+            batch = [clone(s) for s in st0]
+            dts = [list(gpu.integrate_batch(batch)) for _ in range(5)]
+            if resident:
+                gpu.batch_sync_to_host(batch)
+            gpu.batch_release()
+            runs[ahead] = (dts, batch)
+    finally:
+        gpu.set_geometry_ahead(True)
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.batch_release()
+    assert runs[False][0] == runs[True][0]
+    for k in range(len(wls)):
+        for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+            assert np.array_equal(runs[False][1][k].field(s), runs[True][1][k].field(s)), (k, s)

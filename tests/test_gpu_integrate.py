@@ -224,3 +224,46 @@ def test_autotuned_shapes_give_identical_steps(libs):
     assert da == db
     for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
         assert np.array_equal(a.field(s), b.field(s)), s
+
+
+def ahead_vs_after(gpu, st0, steps=2, graphs=True):
+    """steps with the interface geometry formed ahead of the velocity and
+    after the correction: (dts, final state) of each, every array
+    synchronised (strict steps, then resident ones)"""
+    from simplebubblyflowsolver_gb300 import SYNC_ALL
+    runs = {}
+    gpu.set_use_graphs(graphs)
+    try:
+        for ahead in (False, True):
+            gpu.release()
+            gpu.set_geometry_ahead(ahead)
+            st = clone(st0)
+            gpu.set_sync_mode(SYNC_ALL)
+            dts = [gpu.integrate(st) for _ in range(steps)]
+            gpu.set_sync_mode(SYNC_NONE)
+            dts += [gpu.integrate(st) for _ in range(steps)]
+            gpu.set_sync_mode(SYNC_ALL)
+            dts.append(gpu.integrate(st))
+            runs[ahead] = (dts, st)
+    finally:
+        gpu.set_geometry_ahead(True)
+        gpu.set_use_graphs(True)
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.release()
+    return runs
+
+
+@pytest.mark.parametrize("name,graphs", [("single_bubble", True), ("swarm", True), ("swarm", False)],
+                         ids=["single_bubble", "swarm", "swarm_eager"])
+def test_geometry_ahead_gives_identical_steps(libs, name, graphs):
+    """the interface geometry (curvature, interface-cell list, THINC factors)
+    and the CSF force formed ahead of the velocity, beside the previous
+    substage's predictor, reorder the work but not the arithmetic: the same
+    bits as forming them after the correction, in every array"""
+    gpu, orc = libs
+    wl = ic.single_bubble(256, 128) if name == "single_bubble" else ic.bubble_swarm(512, 256, nbubbles=12, seed=3)
+    st0 = prepare(libs, wl)
+    runs = ahead_vs_after(gpu, st0, graphs=graphs)
+    assert runs[False][0] == runs[True][0]
+    for s in runs[True][1].slots():
+        assert np.array_equal(runs[False][1].field(s), runs[True][1].field(s)), s

@@ -134,3 +134,28 @@ def test_training_is_reproducible(lib):
         m.train(epochs=2, seed=3)
         runs.append(m.params())
     assert np.array_equal(runs[0], runs[1])
+
+
+def test_geometry_ahead_learned_identical(lib, trained):
+    """with the learned closure the interface geometry, the closure and the
+    force formed ahead of the velocity give the same bits as after the
+    correction, in every array"""
+    from simplebubblyflowsolver_gb300 import ic
+
+    from ._helpers import new_state, set_env
+    from .test_gpu_integrate import ahead_vs_after
+    import oracle
+    _, params, _ = trained
+    wl = ic.bubble_swarm(512, 256, nbubbles=12, seed=3)
+    set_env(wl)
+    lib.set_dt_coefs(wl.coef_dt_adv, wl.coef_dt_dif, wl.coef_dt_int)
+    st0 = new_state(wl, oracle.Oracle())
+    lib.mlp_set_params(params)
+    lib.set_curvature_model(1)
+    try:
+        runs = ahead_vs_after(lib, st0)
+    finally:
+        lib.set_curvature_model(0)
+    assert runs[False][0] == runs[True][0]
+    for s in runs[True][1].slots():
+        assert np.array_equal(runs[False][1].field(s), runs[True][1].field(s)), s
