@@ -107,6 +107,14 @@ int sbfs_set_pdl(int on);
  * Same results either way, bit for bit. */
 int sbfs_set_compaction(int mode);
 
+/* launch the step's kernels at their streams' priorities (default 1): the
+ * main and copy streams high, the side stream (decide_dt, the interface
+ * geometry, the bulk fluxes) low, so that the GPU schedules the main stream's
+ * blocks first and the side stream's where SMs are free; 0 launches all at
+ * the default priority.  Same results either way, bit for bit.  (No
+ * counterpart in the reference.) */
+int sbfs_set_stream_priorities(int on);
+
 /* run each substage's interface geometry ahead of its velocity (default 1):
  * curvature, the interface-cell list with the cells' THINC factors, and the
  * CSF force depend on vof alone, so they are formed beside the previous

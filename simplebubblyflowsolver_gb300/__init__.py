@@ -85,6 +85,11 @@ class GpuLibrary(ReferenceAPI):
         """interface-branch compaction: -1 as tuned (default), 0 off, 1 on"""
         self._ext("sbfs_set_compaction", int(mode))
 
+    def set_stream_priorities(self, on: bool):
+        """launch the step's kernels at their streams' priorities (main high,
+        side low; default True)"""
+        self._ext("sbfs_set_stream_priorities", 1 if on else 0)
+
     def set_geometry_ahead(self, on: bool):
         """form each substage's interface geometry and CSF force ahead of its
         velocity, beside the previous substage's predictor (default True)"""

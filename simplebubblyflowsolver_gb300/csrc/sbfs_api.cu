@@ -452,15 +452,19 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   c->lx = d->lengths[0];
   c->ly = d->lengths[1];
   c->hxxf.assign(d->hxxf, d->hxxf + c->nx + 1);
-  CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+  // the main and copy streams at the highest priority, the side stream at
+  // the default (lowest): see g_stream_prio
+  int prio_lo = 0, prio_hi = 0;
+  CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+  CK(cudaStreamCreateWithPriority(&c->s, cudaStreamNonBlocking, prio_hi));
   CK(cudaEventCreate(&c->e0));
-  CK(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithPriority(&c->s2, cudaStreamNonBlocking, prio_lo));
   CK(cudaEventCreateWithFlags(&c->evf, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evd, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evp, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evx, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->evF, cudaEventDisableTiming));
-  CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithPriority(&c->s3, cudaStreamNonBlocking, prio_hi));
   for (cudaEvent_t &e : c->evh) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CK(cudaHostAlloc(reinterpret_cast<void **>(&c->link_tab), sizeof(double *) * kLinkSlots * nc, cudaHostAllocMapped));
   CK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->link_tab_dev), c->link_tab, 0));
@@ -1126,7 +1130,7 @@ int autotune(Ctx &c) {
 int role_key(const Ctx &c) {
   return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
          (g_pdl << 6) | ((g_compact + 1) << 7) | ((g_sync_mode == SBFS_SYNC_ALL) << 9) | (g_geo_ahead << 10) |
-         ((c.b.vof != c.VOF0) << 11);
+         ((c.b.vof != c.VOF0) << 11) | (g_stream_prio << 12);
 }
 
 int launch_step(Ctx &c) {
@@ -1437,6 +1441,11 @@ int sbfs_set_pdl(int on) {
 int sbfs_set_compaction(int mode) {
   if (mode < -1 || mode > 1) return fail("bad compaction mode %d", mode);
   g_compact = mode;
+  return 0;
+}
+
+int sbfs_set_stream_priorities(int on) {
+  g_stream_prio = on ? 1 : 0;
   return 0;
 }
 

@@ -28,6 +28,7 @@
 namespace sbfs {
 
 int g_pdl = 1;  // step kernels launched with programmatic stream serialisation
+int g_stream_prio = 1;
 int g_compact = -1;
 
 namespace {
@@ -206,17 +207,6 @@ __global__ void __launch_bounds__(BX *BY) k_normal_curv(Grid g, Metrics m, const
 // components along and across it.  With a = K exp(-2 n_a s) and
 // b = exp(-2 n_b g) the two terms are 1 / (1 + a b) and b / (b + a).
 // The caller passes -2 n_a s, which for s = -+1/2 is exactly +-n_a.
-// vel phi for the vof phi of a single-phase upwind cell, the same bits as
-// the product: phi = +0 gives a zero of vel's sign, phi = 1 gives vel (vel is
-// finite), and only other values (the few cells within vofmin of 0 or 1)
-// take a multiply
-__device__ __forceinline__ double vel_phi(double vel, double phi) {
-  const long long pb = dbits(phi);
-  if (pb == 0) return __longlong_as_double(dbits(vel) & (long long)0x8000000000000000ULL);
-  if (pb == 0x3FF0000000000000LL) return vel;
-  return __dmul_rn(vel, phi);
-}
-
 __device__ __forceinline__ double thinc_ab(double a, double b) {
   const double p = fma(a, b, 1.);
   const double q = b + a;
@@ -269,7 +259,7 @@ __device__ __forceinline__ void flux_force_body(const Grid &g, const Metrics &m,
       const int iu = n ? I : I - 1;
       const double phi = n ? v0 : vxm;
       if (single_phase(phi)) {
-        fluxx[ix(g, r, I - 1)] = vel_phi(vel, phi);
+        fluxx[ix(g, r, I - 1)] = vel * phi;
       } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)r * g.p3 + (size_t)(iu - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);
@@ -282,7 +272,7 @@ __device__ __forceinline__ void flux_force_body(const Grid &g, const Metrics &m,
       const int ru = n ? r : rm;
       const double phi = n ? v0 : vym;
       if (single_phase(phi)) {
-        fluxy[ix(g, r, I)] = vel_phi(vel, phi);
+        fluxy[ix(g, r, I)] = vel * phi;
       } else if (!BULK_ONLY) {
         const double *nv = normal + (size_t)ru * g.p3 + (size_t)(I - 1) * 3;
         const double K = HAVE_K ? nv[2] : exp(-2. * nv[2]);

@@ -165,18 +165,27 @@ void launch_bc_vof(cudaStream_t s, const Grid &g, double *vof);
 // them plainly
 extern int g_pdl;
 extern int g_compact;  // -1: per context (Tiles::compact), else 0 / 1 for all
+// 1: each launch carries its stream's priority (the step's main and copy
+// streams high, its side stream low), so that the block scheduler fills the
+// SMs with the main stream's blocks first and the side stream's in the gaps;
+// 0: every launch at the default priority.  Scheduling only: the same results
+extern int g_stream_prio;
 template <typename... P, typename... A>
 void launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A &&...a) {
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = g_pdl ? 1 : 0;
+  int prio = 0;
+  if (g_stream_prio) cudaStreamGetPriority(s, &prio);
+  at[1].id = cudaLaunchAttributePriority;
+  at[1].val.priority = prio;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(a)...);
 }
 
