@@ -210,7 +210,8 @@ int sbfs_statistics_output(const char dirname[], const domain_t *domain);
  * device memory only from their own pre-sized pool, or that must not call
  * cudaMalloc/cudaFree while running because those calls synchronise the GPU
  * and take unbounded time.  The velocities are already on the GPU; the
- * kernel's scratch (per-column maxima and a block counter) lives in a fixed
+ * kernels' scratch (per-column maxima, the least quotient and a block
+ * counter) lives in a fixed
  * array inside the library (SBFS_NOALLOC_MAX_NX + 8 words, 64 KB, one copy on
  * every GPU that loads the library, kept until the process exits), so the
  * call allocates nothing.

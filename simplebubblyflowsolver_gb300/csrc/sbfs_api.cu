@@ -926,7 +926,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   c.iden ^= 1;
 }
 
-constexpr int kKernelsPerStep = 1 + 3 * 11;
+constexpr int kKernelsPerStep = 3 + 3 * 11;
 
 void enqueue_step(Ctx &c) {
   // profiled steps keep every launch on the main stream (events per launch)

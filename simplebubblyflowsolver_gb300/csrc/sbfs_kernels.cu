@@ -1416,28 +1416,27 @@ __global__ void k_pressure(Grid g, const double *__restrict__ psin, double *__re
 // ---------------------------------------------------------------------------
 // time step size (src/decide_dt.c:34-169)
 // min over faces of h / (|u| + 1e-8) equals h / (max |u| + 1e-8) for a
-// fixed h because both roundings are monotone; so the kernel reduces max |u|
+// fixed h because both roundings are monotone; so k_decide_dt reduces max |u|
 // per x column (ux) and over the domain (uy) on the integer patterns of the
-// non-negative doubles, and one block finishes with nx + 1 divisions.  A
-// non-finite velocity sets bit 0 of the status word.  The finishing block
-// also writes every per-substage scalar of the step.
+// non-negative doubles, and k_decide_dt_fin forms the nx - 1 quotients of the
+// columns over its blocks and their minimum (the minimum of positive doubles
+// is that of their bit patterns), then its last block the dt and every
+// per-substage scalar of the step.  A non-finite velocity sets bit 0 of the
+// status word.  Scratch per case (nx + 8 words, zero between launches):
+// [2..nx] column max |ux| bits, [nx+2] max |uy| bits, [nx+4] the complement
+// of the least quotient's bits (so that zero means none yet), [nx+5] the
+// finishing blocks' counter.
 // ---------------------------------------------------------------------------
 constexpr unsigned long long kAbsMask = 0x7fffffffffffffffULL;
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
 
 __global__ void __launch_bounds__(BX *BY)
-    k_decide_dt(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
-                unsigned long long *__restrict__ acc, double *__restrict__ sc, int *__restrict__ status,
-                double dt_fixed, double coef_adv, double *__restrict__ coltab) {
+    k_decide_dt(Grid g, const double *__restrict__ ux, const double *__restrict__ uy,
+                unsigned long long *__restrict__ acc) {
   pdl_entry();
-  const Phys ph = zphys(g, ph0);
-  if (g.phys) dt_fixed = ph.dtfix;
   acc += (size_t)blockIdx.z * ((size_t)g.nx + 8);
-  sc += (size_t)blockIdx.z * (kScalars);
-  status += (size_t)blockIdx.z * (1);
   __shared__ unsigned long long colmax[BY][BX];
   __shared__ unsigned long long ymax[BY * BX];
-  __shared__ bool last;
   const int I = blockIdx.x * BX + threadIdx.x + 1;  // 1..nx+1
   unsigned long long mx = 0ULL, my = 0ULL;
   if (I <= g.nx) {
@@ -1460,50 +1459,74 @@ __global__ void __launch_bounds__(BX *BY)
     unsigned long long v = 0ULL;
     for (int k = 0; k < BY; ++k) v = colmax[k][threadIdx.x] > v ? colmax[k][threadIdx.x] : v;
     if (I <= g.nx && v) atomicMax(acc + I, v);
-    __threadfence();
   }
   for (int w = BX * BY / 2; w > 0; w >>= 1) {
     if (tid < w) ymax[tid] = ymax[tid + w] > ymax[tid] ? ymax[tid + w] : ymax[tid];
     __syncthreads();
   }
+  if (tid == 0 && ymax[0]) atomicMax(acc + g.nx + 2, ymax[0]);
+}
+
+// the finishing kernel: one column per thread (I = 2..nx over the blocks),
+// then the last block of each case: dt, the scalars and the reset of the
+// scratch
+constexpr int kDtFinThreads = 256;
+__global__ void __launch_bounds__(kDtFinThreads)
+    k_decide_dt_fin(Grid g, Metrics m, Phys ph0, unsigned long long *__restrict__ acc, double *__restrict__ sc,
+                    int *__restrict__ status, double dt_fixed, double coef_adv) {
+  pdl_entry();
+  const Phys ph = zphys(g, ph0);
+  if (g.phys) dt_fixed = ph.dtfix;
+  acc += (size_t)blockIdx.z * ((size_t)g.nx + 8);
+  sc += (size_t)blockIdx.z * (kScalars);
+  status += (size_t)blockIdx.z * (1);
+  __shared__ double wmin[kDtFinThreads / 32];
+  __shared__ int wbad[kDtFinThreads / 32];
+  __shared__ bool last;
+  const double small = 1.e-8;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // dt_adv = coef * min(1, min_i hx_i / (max|ux|_i + small), hy / (max|uy| + small))
+  double d = 1.;
+  int bad = 0;
+  const int i = blockIdx.x * kDtFinThreads + tid + 2;
+  if (i <= g.nx) {
+    // the column maxima are final (the stream order) and were formed at L2
+    const unsigned long long b = __ldcg(acc + i);
+    bad = b >= kInfBits ? 1 : 0;
+    d = m.hxxf[i] / (__longlong_as_double((long long)b) + small);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    d = fmin(d, __shfl_xor_sync(0xffffffffu, d, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if (lane == 0) {
+    wmin[warp] = d;
+    wbad[warp] = bad;
+  }
+  __syncthreads();
   if (tid == 0) {
-    if (ymax[0]) atomicMax(acc + g.nx + 2, ymax[0]);
+    for (int w = 1; w < kDtFinThreads / 32; ++w) {
+      d = fmin(d, wmin[w]);
+      bad |= wbad[w];
+    }
+    // a positive d (or 1): the least bit pattern is the least value
+    atomicMax(acc + g.nx + 4, ~(unsigned long long)dbits(d));
+    if (bad) atomicOr(status, 1);
     __threadfence();
-    const unsigned int nb = gridDim.x * gridDim.y;
-    const unsigned int done = atomicAdd(reinterpret_cast<unsigned int *>(acc + g.nx + 3), 1u);
-    last = (done == nb - 1);
+    const unsigned int done = atomicAdd(reinterpret_cast<unsigned int *>(acc + g.nx + 5), 1u);
+    last = (done == gridDim.x - 1);
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // finishing block: dt_adv = coef * min(1, min_i hx_i / (max|ux|_i + small), hy / (max|uy| + small))
-  __shared__ double dmin[BY * BX];
-  __shared__ unsigned long long bad[BY * BX];
-  const double small = 1.e-8;
-  double d = 1.;
-  unsigned long long nb = 0ULL;
-  // the other blocks' atomics are done at L2 and fenced: read past L1
-  for (int i = tid + 2; i <= g.nx; i += BX * BY) {
-    const unsigned long long b = __ldcg(acc + i);
-    nb |= (b >= kInfBits) ? 1ULL : 0ULL;
-    d = fmin(d, m.hxxf[i] / (__longlong_as_double((long long)b) + small));
-  }
-  dmin[tid] = d;
-  bad[tid] = nb;
-  __syncthreads();
-  for (int w = BX * BY / 2; w > 0; w >>= 1) {
-    if (tid < w) {
-      dmin[tid] = fmin(dmin[tid], dmin[tid + w]);
-      bad[tid] |= bad[tid + w];
-    }
-    __syncthreads();
-  }
   if (tid == 0) {
+    const double dmin = __longlong_as_double((long long)~__ldcg(acc + g.nx + 4));
     const unsigned long long by = __ldcg(acc + g.nx + 2);
-    double dt = fmin(dmin[0], g.hy / (__longlong_as_double((long long)by) + small));
+    double dt = fmin(dmin, g.hy / (__longlong_as_double((long long)by) + small));
     dt *= coef_adv;
     dt = fmin(dt, dt_fixed);
-    if (bad[0] || by >= kInfBits) atomicOr(status, 1);
+    if (by >= kInfBits) atomicOr(status, 1);
     // per-substage scalars; RK3 coefficients of src/runge_kutta.c:8-15
     const double al[3] = {32. / 60., 25. / 60., 45. / 60.};
     const double be[3] = {0. / 60., -17. / 60., -25. / 60.};
@@ -1536,24 +1559,29 @@ __global__ void __launch_bounds__(BX *BY)
     }
   }
   __syncthreads();
-  // the per-column coefficients of the three substages (none for a caller
-  // without the table)
-  if (coltab) {
-    coltab += (size_t)blockIdx.z * 3 * kColTabs * g.ct;
-    // cold / pax once per substage: a division per entry made this block the
-    // kernel's tail
-    const double cop[3] = {sc[sc_cold(0)] / sc[sc_pax(0)], sc[sc_cold(1)] / sc[sc_pax(1)],
-                           sc[sc_cold(2)] / sc[sc_pax(2)]};
-    for (int t = tid; t < 3 * (g.nx + 2); t += BX * BY) {
-      const int k = t / (g.nx + 2), I = t - k * (g.nx + 2);
-      const double ih = m.ihxxf[I];
-      coltab[(size_t)ct_gdt2x(k) * g.ct + I] = sc[sc_gdt2(k)] * ih;
-      coltab[(size_t)ct_cnewx(k) * g.ct + I] = sc[sc_cnew(k)] * ih;
-      coltab[(size_t)ct_coldx(k) * g.ct + I] = cop[k] * ih;
-    }
+  // reset the scratch for the next launch
+  for (int t = tid; t <= g.nx + 5; t += kDtFinThreads) acc[t] = 0ULL;
+}
+
+// the per-column coefficients of the three substages from the scalars (one
+// column per thread, over many blocks: on one block they were the finishing
+// kernel's tail)
+__global__ void __launch_bounds__(kDtFinThreads)
+    k_decide_dt_tab(Grid g, Metrics m, const double *__restrict__ sc, double *__restrict__ coltab) {
+  pdl_entry();
+  sc += (size_t)blockIdx.z * (kScalars);
+  coltab += (size_t)blockIdx.z * 3 * kColTabs * g.ct;
+  const int I = blockIdx.x * kDtFinThreads + threadIdx.x;
+  if (I > g.nx + 1) return;
+  const double ih = m.ihxxf[I];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // cold / pax once per column and substage (the same quotient everywhere)
+    const double cop = sc[sc_cold(k)] / sc[sc_pax(k)];
+    coltab[(size_t)ct_gdt2x(k) * g.ct + I] = sc[sc_gdt2(k)] * ih;
+    coltab[(size_t)ct_cnewx(k) * g.ct + I] = sc[sc_cnew(k)] * ih;
+    coltab[(size_t)ct_coldx(k) * g.ct + I] = cop * ih;
   }
-  // reset the accumulators for the next launch
-  for (int i = tid; i <= g.nx + 3; i += BX * BY) acc[i] = 0ULL;
 }
 
 // pax e grad psi_old and pay e grad psi_old, e = rho_ref / rho - 1, at ux
@@ -2090,11 +2118,21 @@ void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double 
 
 void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                       const double *ux, const double *uy, double dt_fixed, double coef_adv) {
+  launch_decide_dt_raw(s, g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed, coef_adv, b.coltab);
+}
+
+void launch_decide_dt_raw(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const double *ux,
+                          const double *uy, unsigned long long *acc, double *sc, int *status, double dt_fixed,
+                          double coef_adv, double *coltab) {
   int gy = (g.ny + BY - 1) / BY;
   const int gx = (g.nx + BX) / BX;
   while (gy > 1 && gx * gy * g.nc > 16 * 152) gy = (gy + 1) / 2;
-  launch_pdl(k_decide_dt, dim3(gx, gy, g.nc), dim3(BX, BY), 0, s, g, m, ph, ux, uy, b.dt_acc, b.scalars, b.status, dt_fixed,
-                                                    coef_adv, b.coltab);
+  launch_pdl(k_decide_dt, dim3(gx, gy, g.nc), dim3(BX, BY), 0, s, g, ux, uy, acc);
+  launch_pdl(k_decide_dt_fin, dim3((g.nx - 1 + kDtFinThreads - 1) / kDtFinThreads, 1, g.nc), dim3(kDtFinThreads), 0, s,
+             g, m, ph, acc, sc, status, dt_fixed, coef_adv);
+  if (coltab)
+    launch_pdl(k_decide_dt_tab, dim3((g.nx + 2 + kDtFinThreads - 1) / kDtFinThreads, 1, g.nc), dim3(kDtFinThreads), 0,
+               s, g, m, (const double *)sc, coltab);
 }
 
 void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *den,

@@ -140,8 +140,14 @@ void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *ps
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
                     double *ux, double *uy, const double *psi_new, bool pressure);
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new);
+// decide_dt: the column and domain maxima, then the finishing kernel (dt, the
+// scalars and, with a coltab, the column tables); acc holds nx + 8 zero
+// words per case between launches
 void launch_decide_dt(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                       const double *ux, const double *uy, double dt_fixed, double coef_adv);
+void launch_decide_dt_raw(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const double *ux,
+                          const double *uy, unsigned long long *acc, double *sc, int *status, double dt_fixed,
+                          double coef_adv, double *coltab);
 // e grad psi_old at the faces (b.egx, b.egy) from a density field and psi_old,
 // as k_predict_mf stores it (fine-grained entry points)
 void launch_face_factor(cudaStream_t s, const Grid &g, const Phys &ph, const Bufs &b, const double *den,

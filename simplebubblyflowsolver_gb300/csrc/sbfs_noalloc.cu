@@ -5,10 +5,10 @@
 // program that must not call cudaMalloc / cudaFree once it is running
 // because those calls synchronise the device and take unbounded time.  Such
 // a caller already holds the velocity fields on the GPU and only needs the
-// time step.  This entry point runs the library's decide_dt kernel on the
-// caller's device arrays with the kernel's scratch (the per-column maxima of
-// |ux| and the block counter) taken from a fixed array in the library's own
-// device image, so nothing is allocated.
+// time step.  This entry point runs the library's decide_dt kernels on the
+// caller's device arrays with their scratch (the per-column maxima of |ux|,
+// the |uy| maximum, the least quotient and a block counter) taken from a
+// fixed array in the library's own device image, so nothing is allocated.
 //
 // The scratch array is sized for nx <= SBFS_NOALLOC_MAX_NX; it exists once
 // per GPU that loads the library and stays there until the process exits.
@@ -36,7 +36,8 @@ using namespace sbfs;
 
 namespace {
 
-// per-column maxima (nx + 2 words), the |uy| maximum and the block counter
+// per-column maxima (nx + 2 words), the |uy| maximum, the least quotient
+// and the block counter (words nx + 2 .. nx + 5)
 constexpr int kScratchWords = SBFS_NOALLOC_MAX_NX + 8;
 static __device__ __align__(256) unsigned long long g_dt_scratch[kScratchWords];
 
@@ -75,7 +76,7 @@ extern "C" int sbfs_decide_dt_noalloc(int nx, int ny, double lx, double ly, cons
   unsigned long long *scratch = static_cast<unsigned long long *>(p);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the kernel needs zeroed accumulators; the array keeps the last call's words
-  e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (nx + 4), s);
+  e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (nx + 6), s);
   if (e != cudaSuccess) return report("sbfs_decide_dt_noalloc: clearing the scratch", e);
   Grid g{};
   g.nc = 1;
