@@ -94,7 +94,7 @@ struct Ctx {
   double *U[2], *V[2], *PSI[2], *DEN[2], *SX[2], *SY[2], *SV[2];
   // CSF force buffers: substage k uses IFX[k & 1], IFY[k & 1] (the last
   // substage's in b.ifrcx, b.ifrcy, the reference's arrays)
-  double *IFX[2], *IFY[2];
+  double *IFX[3], *IFY[3];
   double *VOF0 = nullptr;  // the first vof buffer (which of the two holds the current vof keys the graphs)
   int iu = 0, ipsi = 0, iden = 0, isrc = 0;
   bool resident = false;  // device holds the current state
@@ -112,6 +112,15 @@ struct Ctx {
   cudaEvent_t evf = nullptr, evd = nullptr, evp = nullptr, evx = nullptr, evF = nullptr;
   bool props_ahead = false;  // the next substage's k_props is already on the side stream
   bool geo_ahead = false;    // the next substage's interface geometry and force are already on the side stream
+  // device-resident steps: the last step formed the next step's first-substage
+  // geometry and force (into IFX[2]) from its final vof and density, for the
+  // configuration geo_next_cfg; any change of the state or of that
+  // configuration clears it (state_touched)
+  bool geo_next = false;
+  unsigned long long geo_next_cfg = 0;
+  // this step: its first substage's geometry came from the last step
+  // (pre_first), it forms the next step's (make_next); set by launch_step
+  bool pre_first = false, make_next = false;
   // host-linked step (strict sync mode, host arrays the GPU can address): the
   // step copies the state in and out itself, on the copy stream s3, each
   // field as early as the step allows.  link_tab: page-locked table of the
@@ -339,8 +348,11 @@ void finish_phys(Phys &p, const Grid &g) {
 }
 
 void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
-  c.ph = phys_of(f, itf);
-  finish_phys(c.ph, c.g);
+  Phys p = phys_of(f, itf);
+  finish_phys(p, c.g);
+  // other physics: a first-substage geometry formed ahead is stale
+  if (memcmp(&p, &c.ph, sizeof(Phys)) != 0) c.geo_next = false;
+  c.ph = p;
 }
 
 double fixed_dt(const Ctx &c, const domain_t *d, const fluid_t *f, const interface_t *itf) {
@@ -501,7 +513,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
                      &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.egx, &b.egy, &b.pxx, &b.pyy, &b.pxy, &b.pyx,
-                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt};
+                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt, &b.ifrcx3, &b.ifrcy3};
   for (double **p : scal)
     if (dalloc(*c, p, n1 * nc)) return 1;
   if (dalloc(*c, &b.dvof, n2 * nc)) return 1;
@@ -561,6 +573,8 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
   c->IFX[1] = b.ifrcx2;
   c->IFY[0] = b.ifrcy;
   c->IFY[1] = b.ifrcy2;
+  c->IFX[2] = b.ifrcx3;
+  c->IFY[2] = b.ifrcy3;
   c->VOF0 = b.vof;
   return 0;
 }
@@ -690,6 +704,18 @@ int g_geo_ahead = 1;
 // 1 = the learned closure in interface cells (plain kappa outside its range)
 int g_curv_model = 0;
 
+// the configuration the next step's ahead geometry was formed for: the
+// curvature model and the closure's parameters and range
+unsigned long long geo_cfg() {
+  return (unsigned long long)g_curv_model | ((unsigned long long)g_geo_ahead << 1) |
+         ((unsigned long long)g_mlp_epoch << 8);
+}
+
+// the device state or its configuration changes outside a step: a first
+// substage geometry formed ahead by the last step is stale
+void state_touched(Ctx &c) { c.geo_next = false; }
+
+
 template <class F>
 void timed(Ctx &c, int cls, F &&launch) {
   if (!g_prof.on) {
@@ -809,7 +835,11 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   const double *sc = b.scalars;
   const bool learned = g_curv_model != 0;
   const bool ahead = g_geo_ahead != 0;
-  double *ifx = ahead ? c.IFX[k & 1] : b.ifrcx, *ify = ahead ? c.IFY[k & 1] : b.ifrcy;
+  // force buffers: substage k's IFX[k & 1], the first substage's IFX[2] when
+  // the last step formed it
+  const bool pre = ahead && k == 0 && c.pre_first;
+  const int fb = pre ? 2 : (k & 1);
+  double *ifx = ahead ? c.IFX[fb] : b.ifrcx, *ify = ahead ? c.IFY[fb] : b.ifrcy;
   bool force_side = false;  // this substage's force is running on the side stream (evF)
   if (ahead) {
     if (c.geo_ahead) {
@@ -821,6 +851,10 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
       cudaStreamWaitEvent(c.s2, c.evf, 0);
       launch_bulk_flux(c.s2, c.g, c.m, c.ph, b, ux, uy);
       cudaEventRecord(c.evx, c.s2);
+    } else if (pre) {
+      // the last step formed this substage's geometry and force: the bulk
+      // fluxes here, beside decide_dt on the side stream
+      launch_bulk_flux(c.s, c.g, c.m, c.ph, b, ux, uy);
     } else {
       // substage 0 (or a profiled step): the bulk fluxes first on the side
       // stream (after decide_dt, which waited for the state), the geometry
@@ -847,10 +881,11 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     }
     if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
     timed(c, KC_FACE_FLUX, [&] { launch_face_flux(c.s, c.g, b, ux, uy); });
-    if (par)
-      cudaStreamWaitEvent(c.s, c.evx, 0);
-    else
+    if (par) {
+      if (!pre) cudaStreamWaitEvent(c.s, c.evx, 0);
+    } else {
       timed(c, KC_BULK_FLUX, [&] { launch_bulk_flux(c.s, c.g, c.m, c.ph, b, ux, uy); });
+    }
     if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
     timed(c, KC_VOF_ADVANCE,
           [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1, b.vof_alt); });
@@ -890,19 +925,22 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   // fluid_t holds the stress of its last predictor
   const int stress = k < 2 ? 0 : (g_sync_mode == SBFS_SYNC_ALL ? 2 : 1);
   timed(c, KC_MOMFLUX, [&] { launch_momflux(c.s, c.g, c.m, c.ph, b, ux, uy, stress); });
-  if (par && k < 2) {
+  if (par && (k < 2 || (ahead && c.make_next))) {
     // the next substage's viscosities and corner normals (and, ahead, its
     // geometry and force from the new vof and density) need only the new
     // vof: they run beside this substage's predictor, Poisson solve and
-    // correction, none of which reads what they write
+    // correction, none of which reads what they write.  After the last
+    // substage of a device-resident step they are the next step's first
+    // substage's (force into IFX[2]; the step joins them at its end)
     cudaEventRecord(c.evf, c.s);
     cudaStreamWaitEvent(c.s2, c.evf, 0);
     launch_props(c.s2, c.g, c.m, c.ph, b, false, true, true, nullptr);
     if (ahead) {
+      const int nb = k < 2 ? (k + 1) & 1 : 2;
       launch_geometry(c.s2, c.g, c.m, b);
       if (learned) launch_mlp_curv(c.s2, c.g, b);
-      launch_csf_force(c.s2, c.g, c.m, c.ph, b, den1, c.IFX[(k + 1) & 1], c.IFY[(k + 1) & 1], learned);
-      c.geo_ahead = true;
+      launch_csf_force(c.s2, c.g, c.m, c.ph, b, den1, c.IFX[nb], c.IFY[nb], learned);
+      c.geo_ahead = k < 2;
     } else {
       c.props_ahead = true;
     }
@@ -946,6 +984,8 @@ void enqueue_step(Ctx &c) {
           [&] { launch_decide_dt(c.s, c.g, c.m, c.ph, c.b, c.U[c.iu], c.V[c.iu], c.dt_fixed, g_coef[0]); });
   }
   for (int k = 0; k < 3; ++k) enqueue_substage(c, k, par, par && k == 0);
+  // the next step's first-substage geometry (device-resident steps) joins here
+  if (par && g_geo_ahead && c.make_next) cudaStreamWaitEvent(c.s, c.evp, 0);
   if (c.link) {
     // the velocity and p of the last correction, then the copy stream joins
     launch_host_rows(c.s, c.g, c.link_tab_dev, false, host_rows(c, HL_UX_OUT, L_UX, c.U[c.iu]),
@@ -969,6 +1009,7 @@ void enqueue_step(Ctx &c) {
 int g_autotune = 0;
 
 int autotune(Ctx &c) {
+  c.pre_first = c.make_next = false;  // the trials form every substage's geometry themselves
   const size_t n = c.g.cs1 * c.nc;
   double *live[6] = {c.U[c.iu], c.V[c.iu], c.b.p, c.PSI[c.ipsi], c.b.vof, c.DEN[c.iden]};
   double *save[6] = {nullptr};
@@ -1122,6 +1163,7 @@ int autotune(Ctx &c) {
   for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
   c.graphs.clear();
   c.tuned = true;
+  state_touched(c);
   if (rc || rr) return 1;
   if (e != cudaSuccess) return fail("autotune: %s", cudaGetErrorString(e));
   return 0;
@@ -1130,7 +1172,7 @@ int autotune(Ctx &c) {
 int role_key(const Ctx &c) {
   return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
          (g_pdl << 6) | ((g_compact + 1) << 7) | ((g_sync_mode == SBFS_SYNC_ALL) << 9) | (g_geo_ahead << 10) |
-         ((c.b.vof != c.VOF0) << 11) | (g_stream_prio << 12);
+         ((c.b.vof != c.VOF0) << 11) | (g_stream_prio << 12) | ((int)c.pre_first << 13) | ((int)c.make_next << 14);
 }
 
 int launch_step(Ctx &c) {
@@ -1141,8 +1183,21 @@ int launch_step(Ctx &c) {
     c.link = link;
     if (rc) return 1;
   }
+  // the first substage's geometry from the last step (device-resident
+  // steps in the same configuration), and this step's for the next one
+  auto plan = [&c]() {
+    const bool par = !g_prof.on;
+    c.pre_first = par && g_geo_ahead && c.geo_next && !c.link && c.geo_next_cfg == geo_cfg();
+    c.make_next = par && g_geo_ahead && g_sync_mode == SBFS_SYNC_NONE && !c.link;
+  };
+  auto planned = [&c]() {
+    c.geo_next = c.make_next;
+    if (c.make_next) c.geo_next_cfg = geo_cfg();
+  };
   if (!g_use_graphs || g_prof.on) {
+    plan();
     enqueue_step(c);
+    planned();
     CK(cudaGetLastError());
     return 0;
   }
@@ -1163,8 +1218,10 @@ int launch_step(Ctx &c) {
       for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
       c.graphs.clear();
       c.graph_sig = all;
+      state_touched(c);
     }
   }
+  plan();
   const int key = role_key(c);
   auto it = c.graphs.find(key);
   // a host-linked graph holds copy-engine copies of the caller's arrays: it
@@ -1206,10 +1263,12 @@ int launch_step(Ctx &c) {
   c.ipsi ^= 1;
   c.iden ^= 1;
   if (g_geo_ahead) std::swap(c.b.vof, c.b.vof_alt);
+  planned();
   return 0;
 }
 
 int upload_fields(Ctx &c, const fluid_t *f, const interface_t *itf) {
+  state_touched(c);
   return h2d(c, f->ux, L_UX, c.U[c.iu]) || h2d(c, f->uy, L_UY, c.V[c.iu]) || h2d(c, f->p, L_P, c.b.p) ||
          h2d(c, f->psi[0], L_P, c.PSI[c.ipsi]) || h2d(c, itf->vof, L_VOF, c.b.vof);
 }
@@ -1351,6 +1410,7 @@ Batch *prepare_batch(int n, const domain_t *const *d, fluid_t *const *f, interfa
     if (re_changed && upload_metrics(c, dq, re.data())) return nullptr;
     if (re_changed || memcmp(ph.data(), c.phys_host.data(), sizeof(Phys) * c.nc) != 0) {
       c.phys_host = ph;
+      c.geo_next = false;  // other physics: a geometry formed ahead is stale
       // a group of one case has no table: its kernels take c.ph
       if (c.phys_dev && (cudaMemcpyAsync(c.phys_dev, c.phys_host.data(), sizeof(Phys) * c.nc,
                                          cudaMemcpyHostToDevice, c.s) != cudaSuccess ||
@@ -1483,6 +1543,7 @@ int sbfs_set_dt_coefs(double adv, double dif, double itf) {
 
 int sbfs_invalidate_device(void) {
   if (g_ctx) g_ctx->resident = false;
+  if (g_ctx) state_touched(*g_ctx);
   ++g_reg_epoch;  // and look at the host arrays' registration again
   return 0;
 }
@@ -1970,6 +2031,7 @@ int decide_dt(const domain_t *d, const fluid_t *f, const interface_t *itf, doubl
   Ctx *c = prepare_step(d, const_cast<fluid_t *>(f), const_cast<interface_t *>(itf));
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (h2d(*c, f->ux, L_UX, c->b.ux) || h2d(*c, f->uy, L_UY, c->b.uy)) return 1;
   launch_decide_dt(c->s, c->g, c->m, c->ph, c->b, c->b.ux, c->b.uy, c->dt_fixed, g_coef[0]);
   int status = 0;
@@ -1987,6 +2049,7 @@ int fluid_compute_density(const domain_t *d, fluid_t *f, const interface_t *itf,
   Ctx *c = get_ctx(d, f, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (h2d(*c, itf->vof, L_VOF, c->b.vof)) return 1;
   launch_props(c->s, c->g, c->m, c->ph, c->b, true, false, false, c->b.den0);
   if (d2h(*c, f->den[index], L_DEN, c->b.den0)) return 1;
@@ -1998,6 +2061,7 @@ int fluid_compute_viscosity(const domain_t *d, fluid_t *f, const interface_t *it
   Ctx *c = get_ctx(d, f, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (h2d(*c, itf->vof, L_VOF, c->b.vof)) return 1;
   launch_props(c->s, c->g, c->m, c->ph, c->b, false, true, false, nullptr);
   if (d2h(*c, f->visux, L_VISUX, c->b.visux) || d2h(*c, f->visuy, L_VISUY, c->b.visuy)) return 1;
@@ -2009,6 +2073,7 @@ int interface_compute_curvature_tensor(const domain_t *d, interface_t *itf) {
   Ctx *c = get_ctx(d, nullptr, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   // cells outside the interface band keep their previous normal, as in the reference
   if (h2d(*c, itf->vof, L_VOF, c->b.vof) || h2d(*c, itf->normal, L_NORMAL, c->b.normal)) return 1;
   launch_props(c->s, c->g, c->m, c->ph, c->b, false, false, true, nullptr);
@@ -2024,6 +2089,7 @@ int interface_compute_force(const domain_t *d, const fluid_t *f, interface_t *it
   Ctx *c = get_ctx(d, f, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (h2d(*c, f->den[0], L_DEN, c->b.den0) || h2d(*c, itf->vof, L_VOF, c->b.vof) ||
       h2d(*c, itf->curv, L_CURV, c->b.curv))
     return 1;
@@ -2039,6 +2105,7 @@ int interface_update_vof(const domain_t *d, const size_t rkstep, const double dt
   Ctx *c = get_ctx(d, f, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (rkstep != 0) swap_data(itf->src[0], itf->src[1]);
   Bufs &b = c->b;
   if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, itf->vof, L_VOF, b.vof) ||
@@ -2059,6 +2126,7 @@ int interface_compute_mass_flux(const domain_t *d, const fluid_t *f, interface_t
   Ctx *c = get_ctx(d, f, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   Bufs &b = c->b;
   if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, itf->fluxx, L_FLUXX, b.fluxx) ||
       h2d(*c, itf->fluxy, L_FLUXY, b.fluxy))
@@ -2075,6 +2143,7 @@ int fluid_predict_field(const domain_t *d, const size_t rkstep, const double dt,
   Ctx *c = get_ctx(d, f, itf);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (rkstep != 0) {
     swap_data(f->srcux[0], f->srcux[1]);
     swap_data(f->srcuy[0], f->srcuy[1]);
@@ -2104,6 +2173,7 @@ int fluid_compute_potential(const domain_t *d, const double dt_old, const double
   Ctx *c = get_ctx(d, f, nullptr);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   Bufs &b = c->b;
   if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, f->psi[0], L_P, b.psi0) ||
       h2d(*c, f->den[1], L_DEN, b.den1))
@@ -2120,6 +2190,7 @@ int fluid_correct_velocity(const domain_t *d, const double dt_old, const double 
   Ctx *c = get_ctx(d, f, nullptr);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   Bufs &b = c->b;
   if (h2d(*c, f->ux, L_UX, b.ux) || h2d(*c, f->uy, L_UY, b.uy) || h2d(*c, f->psi[0], L_P, b.psi0) ||
       h2d(*c, f->psi[1], L_P, b.psi1) || h2d(*c, f->den[1], L_DEN, b.den1))
@@ -2136,6 +2207,7 @@ int fluid_update_pressure(const domain_t *d, fluid_t *f) {
   Ctx *c = get_ctx(d, f, nullptr);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   if (h2d(*c, f->p, L_P, c->b.p) || h2d(*c, f->psi[1], L_P, c->b.psi1)) return 1;
   launch_pressure(c->s, c->g, c->b, c->b.psi1);
   if (d2h(*c, f->p, L_P, c->b.p)) return 1;
@@ -2148,6 +2220,7 @@ static int bc_call(const domain_t *d, array_t *a, const Layout &l, int kind) {
   Ctx *c = get_ctx(d, nullptr, nullptr);
   if (!c) return 1;
   c->resident = false;
+  state_touched(*c);
   double *buf = c->b.txy;  // scratch
   if (h2d(*c, *a, l, buf)) return 1;
   if (kind == 0) launch_bc_ux(c->s, c->g, buf);

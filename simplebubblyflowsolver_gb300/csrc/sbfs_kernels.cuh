@@ -70,6 +70,9 @@ struct Bufs {
   // second CSF force buffers: the force of the next substage is formed
   // beside the predictor that reads this one's
   double *ifrcx2, *ifrcy2;
+  // third CSF force buffers: the first substage's force when the previous
+  // step formed it (device-resident steps)
+  double *ifrcx3, *ifrcy3;
   // launch shapes (host side)
   Tiles tiles;
 };
@@ -217,6 +220,7 @@ cudaError_t measure_fp64_peak(double *gflops);
 // in-step kernel overwriting curv in the listed interface cells
 bool mlp_ready();
 void mlp_range(float *lo, float *hi);  // the closure's range in |kappa dx|
+extern unsigned g_mlp_epoch;           // changes with the closure's parameters or range
 void launch_mlp_curv(cudaStream_t s, const Grid &g, const Bufs &b);
 
 // one scalar field between a host array of the reference's layout (tab[z *

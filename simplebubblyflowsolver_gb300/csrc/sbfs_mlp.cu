@@ -572,6 +572,7 @@ bool mlp_ready() { return g_params != nullptr; }
 // the closure's range in |kappa dx|: the curvatures of the training circles,
 // radii 2 .. 128 cells
 float g_kappa_lo = 0.0078125f, g_kappa_hi = 0.5f;
+unsigned g_mlp_epoch = 0;  // bumped whenever the closure's parameters or range change
 void mlp_range(float *lo, float *hi) {
   *lo = g_kappa_lo;
   *hi = g_kappa_hi;
@@ -593,6 +594,7 @@ int sbfs_mlp_set_range(double lo, double hi) {
   }
   sbfs::g_kappa_lo = (float)lo;
   sbfs::g_kappa_hi = (float)hi;
+  ++sbfs::g_mlp_epoch;
   return 0;
 }
 
@@ -606,6 +608,7 @@ int sbfs_mlp_set_params(const float *host, int n) {
   MCK(cudaMemset(g_m2, 0, sizeof(float) * NPARAM));
   MCK(cudaMemset(g_grad, 0, sizeof(float) * NPARAM));
   g_adam_t = 0;
+  ++sbfs::g_mlp_epoch;
   return 0;
 }
 
@@ -640,6 +643,7 @@ int sbfs_mlp_train_epoch(const void *X, const float *Y, const int *idx, int n, i
   if (ensure_alloc()) return 1;
   const int nb = (batch + TILE - 1) / TILE;
   if (ensure_blocks(nb)) return 1;
+  ++sbfs::g_mlp_epoch;  // the parameters change
   MCK(cudaMemset(g_loss, 0, sizeof(double)));
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   for (int off = 0; off + batch <= n; off += batch) {

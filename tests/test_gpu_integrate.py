@@ -267,3 +267,43 @@ def test_geometry_ahead_gives_identical_steps(libs, name, graphs):
     assert runs[False][0] == runs[True][0]
     for s in runs[True][1].slots():
         assert np.array_equal(runs[False][1].field(s), runs[True][1].field(s)), s
+
+
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph", "eager"])
+def test_resident_geometry_ahead_follows_changes(libs, graphs):
+    """device-resident steps form the next step's first-substage geometry and
+    force at the end of each step.  A new state (other host arrays, then
+    sbfs_invalidate_device) or other physics (We) between steps must not
+    reuse it: the whole sequence gives the same bits as the first form,
+    which forms nothing ahead"""
+    from simplebubblyflowsolver_gb300 import SYNC_NONE
+    gpu, orc = libs
+    wl = ic.bubble_swarm(256, 128, nbubbles=6, seed=5)
+    st0 = prepare(libs, wl)
+    other = new_state(ic.bubble_swarm(256, 128, nbubbles=5, seed=9), orc)
+    runs = {}
+    gpu.set_use_graphs(graphs)
+    try:
+        for ahead in (False, True):
+            gpu.release()
+            gpu.set_geometry_ahead(ahead)
+            gpu.set_sync_mode(SYNC_NONE)
+            st = clone(st0)
+            dts = [gpu.integrate(st) for _ in range(3)]
+            gpu.sync_to_host(st)
+            for s in st.slots():
+                st.field(s)[...] = other.field(s)
+            gpu.invalidate_device()
+            dts += [gpu.integrate(st) for _ in range(3)]
+            st.interface.We = 2.0 * st.interface.We
+            dts += [gpu.integrate(st) for _ in range(3)]
+            gpu.sync_to_host(st)
+            runs[ahead] = (dts, st)
+    finally:
+        gpu.set_geometry_ahead(True)
+        gpu.set_use_graphs(True)
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.release()
+    assert runs[False][0] == runs[True][0]
+    for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+        assert np.array_equal(runs[False][1].field(s), runs[True][1].field(s)), s
