@@ -859,8 +859,10 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
       // substage 0 (or a profiled step): the bulk fluxes first on the side
       // stream (after decide_dt, which waited for the state), the geometry
       // here, then the force on the side stream beside the listed faces and
-      // the VOF update (which leaves vof^k in place)
-      if (par) {
+      // the VOF update (which leaves vof^k in place).  A host-linked step
+      // has its velocity last: the bulk fluxes then follow the listed faces
+      // here, beside decide_dt, which waits for the same velocity
+      if (par && !c.link) {
         cudaEventRecord(c.evf, c.s);
         cudaStreamWaitEvent(c.s2, c.evf, 0);
         launch_bulk_flux(c.s2, c.g, c.m, c.ph, b, ux, uy);
@@ -881,11 +883,9 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     }
     if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
     timed(c, KC_FACE_FLUX, [&] { launch_face_flux(c.s, c.g, b, ux, uy); });
-    if (par) {
-      if (!pre) cudaStreamWaitEvent(c.s, c.evx, 0);
-    } else {
-      timed(c, KC_BULK_FLUX, [&] { launch_bulk_flux(c.s, c.g, c.m, c.ph, b, ux, uy); });
-    }
+    const bool bulk_here = !par || (k == 0 && c.link);
+    if (par && !pre && !bulk_here) cudaStreamWaitEvent(c.s, c.evx, 0);
+    if (bulk_here) timed(c, KC_BULK_FLUX, [&] { launch_bulk_flux(c.s, c.g, c.m, c.ph, b, ux, uy); });
     if (wait_dt) cudaStreamWaitEvent(c.s, c.evd, 0);
     timed(c, KC_VOF_ADVANCE,
           [&] { launch_vof_advance(c.s, c.g, c.m, c.ph, b, sc, k, sva, svb, true, ux, uy, den1, b.vof_alt); });
