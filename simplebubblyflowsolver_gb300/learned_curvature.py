@@ -466,24 +466,35 @@ def interface_stencils(vof_rows: np.ndarray, vofmin=1e-8):
 KAPPA_RANGE = (1.0 / 128.0, 0.5)
 
 
-def static_drop_table(lib, ns=(64, 128, 256), steps=1000, params=None, log=None):
+def matched_steps(n, steps64=1000):
+    """steps of the n x n static drop that reach the physical time of
+    `steps64` steps at 64 x 64: the capillary limit makes dt scale as
+    dx^1.5 (1000, 2828 and 8000 steps at 64, 128 and 256, t ~ 0.52)"""
+    return int(round(steps64 * (n / 64.0) ** 1.5))
+
+
+def static_drop_table(lib, ns=(64, 128, 256), steps=None, params=None, log=None):
     """the static-drop comparison of the plain curvature, the learned closure
     (trained with train_default unless params are given) and the exact
     curvature (a constant network output kappa dx = 4 / n, the closure's range
     opened so that it applies everywhere); one row per (n, variant) with the
-    measures of evaluate_static_drop and the mean of 10 parasitic-velocity
-    samples over the run"""
+    measures of evaluate_static_drop, the mean of the parasitic-velocity
+    samples over the run and the Laplace jump averaged over its second half.
+    steps: per grid; by default matched_steps(n), the same physical time on
+    every grid (a fixed step count would stop the finer grids in the drop's
+    initial capillary transient)"""
     if params is None:
         _, params, _ = train_default(lib, log=log)
     rows = []
     for n in ns:
+        nsteps = steps or matched_steps(n)
         exact = np.zeros(NPARAM, dtype=np.float32)
         exact[-1] = 4.0 / n
         for name, model, p, rng in (("plain", 0, None, KAPPA_RANGE), ("learned", 1, params, KAPPA_RANGE),
                                     ("exact", 1, exact, (0.0, 1.0))):
             lib.mlp_set_range(*rng)
             try:
-                r = evaluate_static_drop(lib, n=n, steps=steps, model=model, params=p, record_every=steps // 10)
+                r = evaluate_static_drop(lib, n=n, steps=nsteps, model=model, params=p, record_every=nsteps // 20)
             finally:
                 lib.mlp_set_range(*KAPPA_RANGE)
             r["variant"] = name
@@ -491,8 +502,25 @@ def static_drop_table(lib, ns=(64, 128, 256), steps=1000, params=None, log=None)
             rows.append(r)
             if log:
                 log(f"{n} {name}: kappa rms {r['kappa_rms_rel_err']:.3g} umax mean {r['umax_mean']:.3g} "
-                    f"dp err {r['dp_rel_err']:.3g}")
+                    f"dp err {r['dp_rel_err']:.3g} late-mean dp err {r['dp_late_rel_err']:.3g}")
     return rows
+
+
+def _laplace_jump(st, n):
+    """pressure inside minus outside the static drop, around its own centre
+    (it may drift under parasitic currents): its vof centroid, y periodic
+    (mean direction on the circle); interior cells vof > 0.99 within 0.15,
+    exterior cells vof < 0.01 beyond 0.35"""
+    p, vof = st.interior_rows("p")[:, 1:-1], st.interior_rows("vof")[:, 1:-1]
+    xc = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(xc, xc)
+    w = vof / vof.sum()
+    cx = float((w * X).sum())
+    ang = 2 * np.pi * Y
+    cy = float(np.arctan2((w * np.sin(ang)).sum(), (w * np.cos(ang)).sum()) / (2 * np.pi)) % 1.0
+    dy = np.abs(Y - cy)
+    d = np.hypot(X - cx, np.minimum(dy, 1.0 - dy))
+    return float(p[(vof > 0.99) & (d < 0.15)].mean() - p[(vof < 0.01) & (d > 0.35)].mean())
 
 
 def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_every=0):
@@ -500,7 +528,11 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
     La = 12000) for `steps` steps with curvature model 0 (-div n) or 1 (the
     learned closure with `params`) and measure the parasitic currents, the
     Laplace pressure jump (exact: kappa / We = 4) and the error of the
-    curvature the step used in the interface cells (exact: 4)."""
+    curvature the step used in the interface cells (exact: 4).  With
+    record_every, the parasitic velocity and the jump are also sampled along
+    the run (umax_history, dp_history), and the jump averaged over the
+    samples of the run's second half (dp_late, dp_late_rel_err): the jump
+    oscillates while the drop settles."""
     import os
 
     from . import SYNC_ALL, SYNC_NONE, SYNC_STATE
@@ -518,12 +550,14 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
         lib.mlp_take_usage() if model else None
         lib.set_sync_mode(SYNC_NONE)
         t = 0.0
-        hist = []
+        hist, dph = [], []
         for s in range(steps):
             t += lib.integrate(st)
             if record_every and (s + 1) % record_every == 0:
                 dg = lib.diagnostics(st)
                 hist.append((s + 1, t, max(dg["umax"], dg["vmax"])))
+                lib.sync_to_host(st)
+                dph.append((s + 1, t, _laplace_jump(st, n)))
         lib.set_sync_mode(SYNC_ALL)  # every array, the last curvature included
         lib.sync_to_host(st)
         used = lib.mlp_take_usage() if model else 0
@@ -531,20 +565,11 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
         lib.set_sync_mode(SYNC_STATE)
         lib.set_curvature_model(0)
     ux, uy = st.interior_rows("ux"), st.interior_rows("uy")
-    p, vof = st.interior_rows("p")[:, 1:-1], st.interior_rows("vof")[:, 1:-1]
-    xc = (np.arange(n) + 0.5) / n
-    X, Y = np.meshgrid(xc, xc)
-    # around the drop's own centre (it may drift under parasitic currents):
-    # its vof centroid, y periodic (mean direction on the circle)
-    w = vof / vof.sum()
-    cx = float((w * X).sum())
-    ang = 2 * np.pi * Y
-    cy = float(np.arctan2((w * np.sin(ang)).sum(), (w * np.cos(ang)).sum()) / (2 * np.pi)) % 1.0
-    dy = np.abs(Y - cy)
-    d = np.hypot(X - cx, np.minimum(dy, 1.0 - dy))
-    p_in = p[(vof > 0.99) & (d < 0.15)].mean()
-    p_out = p[(vof < 0.01) & (d > 0.35)].mean()
+    vof = st.interior_rows("vof")[:, 1:-1]
+    dp = _laplace_jump(st, n)
     exact = 1.0 / (wl.We * 0.25)
+    late = [v for s_, t_, v in dph if t_ >= 0.5 * t]
+    dp_late = float(np.mean(late)) if late else dp
     umax = max(float(np.abs(ux).max()), float(np.abs(uy).max()))
     st_i, _, _ = interface_stencils(st.interior_rows("vof"))
     # curvature the last substage used, in its interface cells (exact: 1 / r = 4)
@@ -554,6 +579,7 @@ def evaluate_static_drop(lib, n=64, steps=500, model=0, params=None, record_ever
     return {"n": n, "steps": steps, "time": t, "umax": umax, "capillary_number": umax * wl.We / wl.Re,
             "kappa_rms_rel_err": float(np.sqrt(np.mean(kerr ** 2))),
             "kappa_median_abs_rel_err": float(np.median(np.abs(kerr))),
-            "dp": float(p_in - p_out), "dp_rel_err": float(abs(p_in - p_out - exact) / exact),
+            "dp": dp, "dp_rel_err": float(abs(dp - exact) / exact),
+            "dp_late": dp_late, "dp_late_rel_err": float(abs(dp_late - exact) / exact), "dp_history": dph,
             "learned_cells_per_step": used / (3.0 * steps) if model else 0.0,
             "interface_cells": int(st_i.shape[0]), "umax_history": hist}
