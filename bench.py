@@ -67,8 +67,8 @@ ALG_DOUBLES_PER_CELL = {
     "k_flux_force": 5 + 4,     # ux, uy, vof, den, curv -> fluxx, fluxy, ifrcx, ifrcy
     "k_vof_advance": 6 + 5,    # fluxx, fluxy, vof, src_b, ux, uy -> src_a, vof, den1, mflux(2)
     "k_momflux": 6 + 4,        # ux, uy, visux, visuy, mflux(2) -> momentum fluxes (4)
-    "k_predict_mf": 14 + 6,    # ux, uy, fluxes(4), p, ifrc(2), den(2), psi_old, src_b(2) -> u*(2), src_a(2), e grad psi(2)
-    "k_poisson_fwd": 4 + 1,    # u*(2), e grad psi(2) -> spectrum
+    "k_predict_mf": 14 + 8,    # ux, uy, fluxes(4), p, ifrc(2), den(2), psi_old, src_b(2) -> u*(2), src_a(2), e grad psi(2), q(2)
+    "k_poisson_fwd": 2 + 1,    # q(2) -> spectrum
     "k_poisson_tdm": 2 + 1,    # spectrum, pivots -> spectrum
     "k_poisson_inv": 1 + 1,    # spectrum -> psi
     "k_correct": 6 + 3,        # u*(2), psi, e grad psi(2), p -> u(2), p

@@ -513,7 +513,7 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
                      &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.egx, &b.egy, &b.pxx, &b.pyy, &b.pxy, &b.pyx,
-                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt, &b.ifrcx3, &b.ifrcy3};
+                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt, &b.ifrcx3, &b.ifrcy3, &b.qx, &b.qy};
   for (double **p : scal)
     if (dalloc(*c, p, n1 * nc)) return 1;
   if (dalloc(*c, &b.dvof, n2 * nc)) return 1;
@@ -953,7 +953,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     launch_predict_mf(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, den0, den1, psio, sxa, sxb, sya, syb, ifx,
                       ify);
   });
-  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd(c.s, c.g, b, sc, k, uxs, uys); });
+  timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd_q(c.s, c.g, b, sc, k); });
   timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
   timed(c, KC_POISSON_INV, [&] { launch_poisson_inv(c.s, c.g, b, psin); });
   // psi of substages 2 and 3 are final: the caller's psi[1] and psi[0] after the step

@@ -903,10 +903,13 @@ __global__ void __launch_bounds__(BX *BY)
                  const double *__restrict__ ifrcy, const double *__restrict__ den0, const double *__restrict__ den1,
                  const double *__restrict__ psio, double *__restrict__ sxa, const double *__restrict__ sxb,
                  double *__restrict__ sya, const double *__restrict__ syb, double *__restrict__ egx,
-                 double *__restrict__ egy, const double *__restrict__ coltab) {
+                 double *__restrict__ egy, const double *__restrict__ coltab, double *__restrict__ qx,
+                 double *__restrict__ qy) {
   pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   const double *__restrict__ gx = coltab + ((size_t)blockIdx.z * 3 * kColTabs + ct_gdt2x(k)) * g.ct;
+  // the Poisson right-hand side's face values q = pd u* + pa e grad psi_old
+  // (k_poisson_fwd<W, true> takes their differences across each cell)
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx || J > g.ny) return;
@@ -933,9 +936,12 @@ __global__ void __launch_bounds__(BX *BY)
     double u = fma(adt2, a, rho0 * u0);
     if (k != 0) u = fma(bdt2, sxb[ix(g, r, I - 2)], u);
     u = fma(gx[I], p[ix(g, r, I - 1)] - p[ix(g, r, I)], u);
-    ux_out[ix(g, r, I - 1)] = u * ir2;
+    const double us = u * ir2;
+    ux_out[ix(g, r, I - 1)] = us;
     sxa[ix(g, r, I - 2)] = a;
-    egx[ix(g, r, I - 1)] = fma(rpx, ir2, -pax) * (ps0 - psio[ix(g, r, I - 1)]);
+    const double e = fma(rpx, ir2, -pax) * (ps0 - psio[ix(g, r, I - 1)]);
+    egx[ix(g, r, I - 1)] = e;
+    qx[ix(g, r, I - 1)] = fma(sc[sc_pdx(k)], us, e);
   }
   // ---- uy at face (I, J - 1/2)
   {
@@ -948,22 +954,29 @@ __global__ void __launch_bounds__(BX *BY)
     double u = fma(adt2, a, rho0 * w0);
     if (k != 0) u = fma(bdt2, syb[ix(g, r, I - 1)], u);
     u = fma(sc[sc_gdt2y(k)], p[ix(g, rm, I)] - p[ix(g, r, I)], u);
-    uy_out[ix(g, r, I)] = u * ir2;
+    const double ws = u * ir2;
+    uy_out[ix(g, r, I)] = ws;
     sya[ix(g, r, I - 1)] = a;
-    egy[ix(g, r, I)] = fma(sc[sc_rpy(k)], ir2, -sc[sc_pay(k)]) * (ps0 - psio[ix(g, rm, I)]);
+    const double e = fma(sc[sc_rpy(k)], ir2, -sc[sc_pay(k)]) * (ps0 - psio[ix(g, rm, I)]);
+    egy[ix(g, r, I)] = e;
+    qy[ix(g, r, I)] = fma(sc[sc_pdy(k)], ws, e);
   }
   // walls: impermeable, no-slip; the wall faces' e grad psi_old (zero for a
   // Neumann psi_old, computed as the reference does)
   if (I == 1) {
     ux_out[ix(g, r, 0)] = 0.;
     uy_out[ix(g, r, 0)] = 0.;
-    egx[ix(g, r, 0)] = fma(rpx, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -pax) * (ps0 - psio[ix(g, r, 0)]);
+    const double e = fma(rpx, rcp_nr(den1[ix(g, r, 0)] + den1[ix(g, r, 1)]), -pax) * (ps0 - psio[ix(g, r, 0)]);
+    egx[ix(g, r, 0)] = e;
+    qx[ix(g, r, 0)] = fma(sc[sc_pdx(k)], 0., e);
   }
   if (I == g.nx) {
     ux_out[ix(g, r, g.nx)] = 0.;
     uy_out[ix(g, r, g.nx + 1)] = 0.;
-    egx[ix(g, r, g.nx)] =
+    const double e =
         fma(rpx, rcp_nr(den1[ix(g, r, g.nx)] + den1[ix(g, r, g.nx + 1)]), -pax) * (psio[ix(g, r, g.nx + 1)] - ps0);
+    egx[ix(g, r, g.nx)] = e;
+    qx[ix(g, r, g.nx)] = fma(sc[sc_pdx(k)], 0., e);
   }
 }
 
@@ -979,7 +992,9 @@ __global__ void __launch_bounds__(BX *BY)
 //      285-363 for a tile of W columns,
 //        rhs = rho_ref/dt_new div u* - dt_old/dt_new div((rho_ref/rho - 1) grad psi_old)
 //      (the face values of (rho_ref/rho - 1) grad psi_old come from k_predict_mf,
-//      already times their Poisson coefficient)
+//      already times their Poisson coefficient; in the fused step the
+//      predictor also adds the u* term at each face, so the transform only
+//      differences the sums)
 //      with div and the face differences in the JD = H hy form, packed two
 //      reals per complex, a mixed radix-4/2 Stockham FFT of length ny/2 in
 //      shared memory and the real-to-complex split; spectrum [I][m]
@@ -1085,7 +1100,10 @@ __device__ double2 *fft_rows(double2 *x, double2 *y, int M, const double2 *__res
   return x;
 }
 
-template <int W>
+// Q: the right-hand side from the predictor's face values q = pd u* + pa e
+// grad psi_old (ux, uy are qx, qy; egx, egy unused): 3 FP64 operations per
+// cell instead of 7
+template <int W, bool Q>
 __global__ void __launch_bounds__(256)
     k_poisson_fwd(Grid g, const double *__restrict__ sc, int k, const double *__restrict__ ux,
                   const double *__restrict__ uy, const double *__restrict__ egx, const double *__restrict__ egy,
@@ -1109,11 +1127,15 @@ __global__ void __launch_bounds__(256)
       const int rg = r + zr, rp = (r == ny - 1 ? 0 : r + 1) + zr;
       // differences of pax e grad psi_old and pay e grad psi_old across the
       // cell (its faces' values written by k_predict_mf or k_face_factor)
-      const double X = egx[ix(g, rg, I)] - egx[ix(g, rg, I - 1)];
-      const double Y = egy[ix(g, rp, I)] - egy[ix(g, rg, I)];
-      const double dux = ux[ix(g, rg, I)] - ux[ix(g, rg, I - 1)];
-      const double duy = uy[ix(g, rp, I)] - uy[ix(g, rg, I)];
-      val = fma(pdx, dux, fma(pdy, duy, X + Y));
+      if (Q) {
+        val = (ux[ix(g, rg, I)] - ux[ix(g, rg, I - 1)]) + (uy[ix(g, rp, I)] - uy[ix(g, rg, I)]);
+      } else {
+        const double X = egx[ix(g, rg, I)] - egx[ix(g, rg, I - 1)];
+        const double Y = egy[ix(g, rp, I)] - egy[ix(g, rg, I)];
+        const double dux = ux[ix(g, rg, I)] - ux[ix(g, rg, I - 1)];
+        const double duy = uy[ix(g, rp, I)] - uy[ix(g, rg, I)];
+        val = fma(pdx, dux, fma(pdy, duy, X + Y));
+      }
     }
     Ad[c * ny + r] = val;
   }
@@ -1874,11 +1896,17 @@ int tdm_warps_for(int nx, int ny, int nc) {
 cudaError_t configure_kernels() {
   cudaError_t e;
   const int big = 227 * 1024;
-  e = cudaFuncSetAttribute(k_poisson_fwd<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  e = cudaFuncSetAttribute(k_poisson_fwd<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_poisson_fwd<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  e = cudaFuncSetAttribute(k_poisson_fwd<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_poisson_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  e = cudaFuncSetAttribute(k_poisson_fwd<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_fwd<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_fwd<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_fwd<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_poisson_inv<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
@@ -1886,7 +1914,9 @@ cudaError_t configure_kernels() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_poisson_inv<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_poisson_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  e = cudaFuncSetAttribute(k_poisson_fwd<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_fwd<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_poisson_inv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
@@ -2032,7 +2062,7 @@ void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
                        const double *ify) {
   launch_pdl(k_predict_mf, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g,
              m, ph, sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, ifx, ify, den0, den1,
-             psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy, b.coltab);
+             psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy, b.coltab, b.qx, b.qy);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -2045,24 +2075,34 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
                                                         srcux_b, srcux_g, srcuy_a, srcuy_b, srcuy_g);
 }
 
-template <int W>
+template <int W, bool Q>
 void poisson_fwd_w(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                    const double *uy) {
   const int nb = (g.nx + W - 1) / W;
-  launch_pdl(k_poisson_fwd<W>, dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s, g, sc, k, ux, uy, b.egx, b.egy,
-             b.twiddle, b.spec);
+  launch_pdl(k_poisson_fwd<W, Q>, dim3(nb, 1, g.nc), 256, poisson_fft_smem(g.ny, W), s, g, sc, k, ux, uy, b.egx,
+             b.egy, b.twiddle, b.spec);
+}
+
+template <bool Q>
+void poisson_fwd_any(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
+                     const double *uy) {
+  if (b.tiles.fft_w == 1)
+    poisson_fwd_w<1, Q>(s, g, b, sc, k, ux, uy);
+  else if (b.tiles.fft_w == 2)
+    poisson_fwd_w<2, Q>(s, g, b, sc, k, ux, uy);
+  else if (b.tiles.fft_w == 8)
+    poisson_fwd_w<8, Q>(s, g, b, sc, k, ux, uy);
+  else
+    poisson_fwd_w<4, Q>(s, g, b, sc, k, ux, uy);
 }
 
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                         const double *uy) {
-  if (b.tiles.fft_w == 1)
-    poisson_fwd_w<1>(s, g, b, sc, k, ux, uy);
-  else if (b.tiles.fft_w == 2)
-    poisson_fwd_w<2>(s, g, b, sc, k, ux, uy);
-  else if (b.tiles.fft_w == 8)
-    poisson_fwd_w<8>(s, g, b, sc, k, ux, uy);
-  else
-    poisson_fwd_w<4>(s, g, b, sc, k, ux, uy);
+  poisson_fwd_any<false>(s, g, b, sc, k, ux, uy);
+}
+
+void launch_poisson_fwd_q(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k) {
+  poisson_fwd_any<true>(s, g, b, sc, k, b.qx, b.qy);
 }
 
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {

@@ -46,6 +46,9 @@ struct Bufs {
   // e grad psi_old at the ux and uy faces, e = rho_ref / rho^{k+1} - 1: the
   // variable-density part of the Poisson right-hand side and of the correction
   double *egx, *egy;
+  // the fused step's Poisson right-hand side at the faces, pd u* + e grad
+  // psi_old (k_predict_mf writes them, the transform differences them)
+  double *qx, *qy;
   // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
   double2 *spec;
   double2 *tdm_fac[3];  // (w, v, P, Q) per row for 1, 2, 4 warps per system, see k_poisson_tdm
@@ -113,8 +116,8 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
 void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                     const double *ux, const double *uy, int stress);
 // fused step: the predictor from those fluxes and the CSF force ifx, ify;
-// also writes e grad psi_old at the faces (b.egx, b.egy) for the Poisson
-// right-hand side and the correction
+// also writes e grad psi_old at the faces (b.egx, b.egy) for the correction
+// and the Poisson right-hand side's face values (b.qx, b.qy)
 void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
                        const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
                        const double *den0, const double *den1, const double *psi_old, double *srcux_a,
@@ -137,6 +140,8 @@ void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *
                     const double *uy, double *psi_new);
 void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k, const double *ux,
                         const double *uy);
+// fused step: the transform of the right-hand side from b.qx, b.qy
+void launch_poisson_fwd_q(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k);
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b);
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new);
 // velocity correction (+ pressure); reads b.egx, b.egy
