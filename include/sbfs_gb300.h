@@ -115,6 +115,13 @@ int sbfs_set_compaction(int mode);
  * counterpart in the reference.) */
 int sbfs_set_stream_priorities(int on);
 
+/* where a grid solves its tridiagonal systems with four warps each, run the
+ * four systems of a wavenumber pair as a cluster of four CTAs, one quarter
+ * of the rows each, exchanging the chunk maps through distributed shared
+ * memory (default 1); 0 keeps one block per pair or two.  Same results
+ * either way, bit for bit.  (No counterpart in the reference.) */
+int sbfs_set_tdm_cluster(int on);
+
 /* run each substage's interface geometry ahead of its velocity (default 1):
  * curvature, the interface-cell list with the cells' THINC factors, and the
  * CSF force depend on vof alone, so they are formed beside the previous
@@ -265,8 +272,9 @@ int sbfs_set_autotune(int on);
 /* shapes in use (group -1: the single-case context): bx[7], by[7] for
  * props, curvature list, flux/force, vof advance, stress, predict,
  * correct; the Poisson transform width, wavenumbers per tridiagonal block
- * and warps per tridiagonal system; compact (may be NULL): 1 when the
- * corner-gradient and curvature work is compacted within blocks */
+ * (0: one pair per cluster of four CTAs) and warps per tridiagonal system;
+ * compact (may be NULL): 1 when the corner-gradient and curvature work is
+ * compacted within blocks */
 int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_warps, int *compact);
 /* number of grid groups and cases per group of the current batch */
 int sbfs_batch_groups(int *ngroups, int *cases_per_group);

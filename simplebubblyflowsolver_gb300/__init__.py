@@ -90,6 +90,11 @@ class GpuLibrary(ReferenceAPI):
         side low; default True)"""
         self._ext("sbfs_set_stream_priorities", 1 if on else 0)
 
+    def set_tdm_cluster(self, on: bool):
+        """solve a wavenumber pair's four tridiagonal systems as a cluster of
+        four CTAs where the grid takes four warps a system (default True)"""
+        self._ext("sbfs_set_tdm_cluster", 1 if on else 0)
+
     def set_geometry_ahead(self, on: bool):
         """form each substage's interface geometry and CSF force ahead of its
         velocity, beside the previous substage's predictor (default True)"""
@@ -253,7 +258,7 @@ class GpuLibrary(ReferenceAPI):
                  "k_correct", "k_csf_force"]
         out = {n: f"{bx[k]}x{by[k]}" for k, n in enumerate(names)}
         out["fft_cols"] = fw.value
-        out["tdm_modes"] = mb.value
+        out["tdm_modes"] = mb.value  # 0: a cluster of four CTAs per pair
         out["tdm_warps"] = gw.value
         out["compact"] = cm.value
         return out

@@ -1043,6 +1043,11 @@ int autotune(Ctx &c) {
     if (fft_w_fits(c.ny, w)) fws.push_back(w);
   if (fws.empty()) fws.push_back(poisson_fft_cols(c.ny));
   const int G = c.b.tiles.tdm_g;  // fixed by the grid
+  {
+    Tiles cl = c.b.tiles;
+    cl.tdm_cl = 1;
+    if (tdm_uses_cluster(cl, c.nx)) tdms.push_back({0, G});  // 0: a cluster of four CTAs per pair
+  }
   for (int mb : {1, 2, 4})
     if (G * mb <= 4 && poisson_tdm_smem(c.nx, mb, G) <= 200 * 1024) tdms.push_back({mb, G});
   if (tdms.empty()) tdms.push_back({1, G});  // one pair per block (staged in global memory above ~6900 rows)
@@ -1131,7 +1136,8 @@ int autotune(Ctx &c) {
     bms = 1e30f;
     for (size_t i = 0; i < tdms.size() && !rc && tdms.size() > 1; ++i) {
       Tiles cand = best;
-      cand.tdm_mb = tdms[i].first;
+      cand.tdm_cl = tdms[i].first == 0 ? 1 : 0;
+      cand.tdm_mb = tdms[i].first == 0 ? 1 : tdms[i].first;
       cand.tdm_g = tdms[i].second;
       float ms = 0.f;
       if (step_ms(cand, &ms)) rc = 1;
@@ -1172,7 +1178,7 @@ int autotune(Ctx &c) {
 int role_key(const Ctx &c) {
   return c.iu | (c.ipsi << 1) | (c.iden << 2) | (c.isrc << 3) | (g_curv_model << 4) | ((int)c.link << 5) |
          (g_pdl << 6) | ((g_compact + 1) << 7) | ((g_sync_mode == SBFS_SYNC_ALL) << 9) | (g_geo_ahead << 10) |
-         ((c.b.vof != c.VOF0) << 11) | (g_stream_prio << 12) | ((int)c.pre_first << 13) | ((int)c.make_next << 14);
+         ((c.b.vof != c.VOF0) << 11) | (g_stream_prio << 12) | ((int)c.pre_first << 13) | ((int)c.make_next << 14) | (g_tdm_cluster << 15);
 }
 
 int launch_step(Ctx &c) {
@@ -1501,6 +1507,11 @@ int sbfs_set_pdl(int on) {
 int sbfs_set_compaction(int mode) {
   if (mode < -1 || mode > 1) return fail("bad compaction mode %d", mode);
   g_compact = mode;
+  return 0;
+}
+
+int sbfs_set_tdm_cluster(int on) {
+  g_tdm_cluster = on ? 1 : 0;
   return 0;
 }
 
@@ -1989,7 +2000,7 @@ int sbfs_tiles(int group, int *bx, int *by, int *fft_w, int *tdm_mb, int *tdm_wa
     by[k] = c->b.tiles.by[k];
   }
   *fft_w = c->b.tiles.fft_w;
-  *tdm_mb = tdm_modes_per_block(c->b.tiles, c->nx);
+  *tdm_mb = tdm_uses_cluster(c->b.tiles, c->nx) ? 0 : tdm_modes_per_block(c->b.tiles, c->nx);
   *tdm_warps = c->b.tiles.tdm_g > 0 ? c->b.tiles.tdm_g : 1;
   if (compact) *compact = c->b.tiles.compact;
   return 0;

@@ -20,6 +20,8 @@
 //     pattern of the double; cells whose stencil inputs are bitwise equal
 //     (single-phase bulk) take the exact short cut.
 // The reference file:line each kernel follows is cited at the kernel.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cfloat>
 
@@ -36,7 +38,6 @@ namespace {
 constexpr int BX = 32, BY = 8;
 
 __device__ __forceinline__ size_t ix(const Grid &g, int row, int col) { return (size_t)row * g.p1 + col; }
-__device__ __forceinline__ double half_sum(double a, double b) { return 0.5 * (a + b); }
 __device__ __forceinline__ bool same(double a, double b) { return dbits(a) == dbits(b); }
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
@@ -1368,6 +1369,167 @@ __global__ void __launch_bounds__(512)
   }
 }
 
+// The same solves with four warps per system, spread over a cluster of four
+// CTAs: CTA r of a cluster owns rows 32 L r .. 32 L (r + 1) - 1 of the four
+// systems of one wavenumber pair (warp s: system s), so a launch has four
+// CTAs per pair where k_poisson_tdm has one block per pair or two, and the
+// 4 (ny/4 + 1) CTAs of a case even out over the SMs (in a launch of blocks
+// of one or two pairs, ny/4 + 1 pairs leave SMs idle while the last blocks
+// run, one in six for ny = 1024).  The chunk-map totals of
+// the other CTAs come through distributed shared memory and are combined in
+// the order k_poisson_tdm<false> combines its warps' at G = 4, so both give
+// the same bits.  L = tdm_chunk(nx, 4), S = L | 1; fac is the G = 4 table.
+constexpr int kTdmCluster = 4;
+__global__ void __cluster_dims__(kTdmCluster, 1, 1) __launch_bounds__(128)
+    k_poisson_tdm_cl(Grid g, int L, int S, const double4_32a *__restrict__ fac, const double2 *__restrict__ tw,
+                     double2 *__restrict__ spec) {
+  pdl_entry();
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double smem_cl[];
+  // per system: forward (T, B) and backward (S, C) totals of this CTA's warp, the gauge sum
+  __shared__ double xf[4][2], xb[4][2], xg[4];
+  const int nx = g.nx, M = g.ny / 2, M1 = M + 1;
+  const int rank = (int)cl.block_rank();
+  const int p = (int)blockIdx.x / kTdmCluster;  // the pair (p, M - p), p = 0 .. M/2
+  const int rows = 32 * L, r0 = rank * rows;   // this CTA's rows r0 .. r0 + rows - 1
+  const int sys_len = 32 * S;
+  double2 *sp = spec + (size_t)blockIdx.z * g.css;
+  // ---- load and split (as in k_poisson_tdm), this CTA's rows
+  for (int t = threadIdx.x; t < rows; t += blockDim.x) {
+    const int i = r0 + t;
+    const int at = (t / L) * S + (t % L);
+    double2 xa = make_double2(0., 0.), xbv = make_double2(0., 0.);
+    if (i < nx) {
+      const double2 zm = sp[(size_t)i * M1 + p];
+      const double2 zr = sp[(size_t)i * M1 + (p == 0 ? 0 : M - p)];
+      const double2 E = make_double2(zm.x + zr.x, zm.y - zr.y);
+      const double2 O = make_double2(zm.y + zr.y, zr.x - zm.x);
+      const double2 wa = tw[p], wb = tw[M - p];
+      xa = make_double2(fma(wa.x, O.x, fma(-wa.y, O.y, E.x)), fma(wa.x, O.y, fma(wa.y, O.x, E.y)));
+      xbv = make_double2(fma(wb.x, O.x, fma(wb.y, O.y, E.x)), fma(wb.y, O.x, fma(-wb.x, O.y, -E.y)));
+    }
+    smem_cl[0 * sys_len + at] = xa.x;
+    smem_cl[1 * sys_len + at] = xa.y;
+    smem_cl[2 * sys_len + at] = xbv.x;
+    smem_cl[3 * sys_len + at] = xbv.y;
+  }
+  __syncthreads();
+  const int sys = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lanes = 32 * kTdmCluster, j = rank * 32 + lane;  // chunk of the system
+  const int m = (sys & 2) ? M - p : p;
+  double *x = smem_cl + sys * sys_len + lane * S;
+  const double4_32a *f = fac + (size_t)m * L * lanes + j;
+  double T, B;
+  {
+    double t = 0.;
+#pragma unroll 8
+    for (int k = 0; k < L; ++k) {
+      const double4_32a c = f[(size_t)k * lanes];
+      t = fma(-c.y, t, c.x * x[k]);
+      x[k] = t;
+    }
+    T = t;
+    B = f[(size_t)(L - 1) * lanes].z;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double Tp = __shfl_up_sync(0xffffffffu, T, d), Bp = __shfl_up_sync(0xffffffffu, B, d);
+      if (lane >= d) {
+        T = fma(B, Tp, T);
+        B *= Bp;
+      }
+    }
+  }
+  if (lane == 31) {
+    xf[sys][0] = T;
+    xf[sys][1] = B;
+  }
+  cl.sync();
+  double Cin = 0.;
+  for (int q = 0; q < rank; ++q) {
+    const double *o = cl.map_shared_rank(&xf[sys][0], q);
+    Cin = fma(o[1], Cin, o[0]);
+  }
+  double Sx, Cc;
+  {
+    const double Tu = __shfl_up_sync(0xffffffffu, T, 1), Bu = __shfl_up_sync(0xffffffffu, B, 1);
+    const double carry = lane == 0 ? Cin : fma(Bu, Cin, Tu);
+    double u = 0.;
+#pragma unroll 8
+    for (int k = L - 1; k >= 0; --k) {
+      const double4_32a c = f[(size_t)k * lanes];
+      const double y = fma(c.z, carry, x[k]);
+      u = fma(-c.y, u, y);
+      x[k] = u;
+    }
+    Sx = u;
+    Cc = f[0].w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double Sp = __shfl_down_sync(0xffffffffu, Sx, d), Cp = __shfl_down_sync(0xffffffffu, Cc, d);
+      if (lane + d < 32) {
+        Sx = fma(Cc, Sp, Sx);
+        Cc *= Cp;
+      }
+    }
+  }
+  if (lane == 0) {
+    xb[sys][0] = Sx;
+    xb[sys][1] = Cc;
+  }
+  cl.sync();
+  double Din = 0.;
+  for (int q = kTdmCluster - 1; q > rank; --q) {
+    const double *o = cl.map_shared_rank(&xb[sys][0], q);
+    Din = fma(o[1], Din, o[0]);
+  }
+  {
+    const double Sd = __shfl_down_sync(0xffffffffu, Sx, 1), Cd = __shfl_down_sync(0xffffffffu, Cc, 1);
+    const double next = lane == 31 ? Din : fma(Cd, Din, Sd);
+#pragma unroll 8
+    for (int k = 0; k < L; ++k) x[k] = fma(f[(size_t)k * lanes].w, next, x[k]);
+  }
+  // the singular mode m = 0 (systems 0, 1 of pair 0): zero mean over x,
+  // imaginary part 0 (p is the same on the whole cluster)
+  if (p == 0) {
+    const bool gauge = (sys & 2) == 0;
+    double acc = 0.;
+    if (gauge) {
+      for (int k = 0; k < L; ++k) acc += (j * L + k < nx) ? x[k] : 0.;
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+      if (lane == 0) xg[sys] = acc;
+    }
+    cl.sync();
+    if (gauge) {
+      acc = 0.;
+      for (int q = 0; q < kTdmCluster; ++q) acc += *cl.map_shared_rank(&xg[sys], q);
+      const double mean = (sys & 1) ? 0. : acc / nx;
+      for (int k = 0; k < L; ++k) x[k] = (sys & 1) ? 0. : x[k] - mean;
+    }
+  }
+  // no CTA of the cluster reads another's shared memory after this point
+  cl.sync();
+  // ---- complex-to-real split (as in k_poisson_tdm), this CTA's rows
+  for (int t = threadIdx.x; t < rows; t += blockDim.x) {
+    const int i = r0 + t;
+    if (i >= nx) break;
+    const int at = (t / L) * S + (t % L);
+    const double2 Xa = make_double2(smem_cl[0 * sys_len + at], smem_cl[1 * sys_len + at]);
+    const double2 Xb = make_double2(smem_cl[2 * sys_len + at], smem_cl[3 * sys_len + at]);
+    const double2 E = make_double2(Xa.x + Xb.x, Xa.y - Xb.y);
+    const double2 D = make_double2(Xa.x - Xb.x, Xa.y + Xb.y);
+    const double2 wa = tw[p];
+    sp[(size_t)i * M1 + p] =
+        make_double2(fma(D.x, wa.y, fma(-D.y, wa.x, E.x)), fma(D.y, wa.y, fma(D.x, wa.x, E.y)));
+    if (p != 0 && 2 * p != M) {
+      const double2 wb = tw[M - p];
+      sp[(size_t)i * M1 + (M - p)] =
+          make_double2(fma(-D.y, wb.x, fma(-D.x, wb.y, E.x)), fma(D.y, wb.y, fma(-D.x, wb.x, -E.y)));
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // velocity correction (+ pressure update)
 //   src/fluid/correct_velocity/ux.c:18-66, uy.c:17-64
@@ -1857,6 +2019,7 @@ Tiles default_tiles(int ny) {
   t.tdm_mb = 0;
   t.tdm_g = 1;
   t.compact = 1;
+  t.tdm_cl = 1;
   return t;
 }
 int tdm_chunk(int nx, int G) { return (nx + 32 * G - 1) / (32 * G); }
@@ -1879,8 +2042,12 @@ int tdm_group_index(int G) { return G == 4 ? 2 : (G == 2 ? 1 : 0); }
 // that put about 2048 warps in flight (13 per SM), as long as every lane
 // keeps at least 4 rows (with 2, the cross-warp combine costs more than the
 // shorter recurrences save; 4 rows a lane beat 8 and 16 on every grid from
-// 256 x 128 to 1024 x 512).  A rule of the grid, not a tuned choice: it sets
-// how the chunk maps are combined, and so the rounding of the solve.
+// 256 x 128 to 1024 x 512; on the 2048 x 1024 swarm 4 warps a system in
+// clusters balance the SMs better but add 6% to the solve's FP64 work, and
+// the step gains nothing: the side stream fills the SMs a block-per-pair
+// launch leaves idle).  At 4 warps a system the solves of a pair run as a
+// cluster of four CTAs (k_poisson_tdm_cl).  A rule of the grid, not a tuned choice: it sets how
+// the chunk maps are combined, and so the rounding of the solve.
 int tdm_modes_per_block(const Tiles &t, int nx) {
   const int G = t.tdm_g > 0 ? t.tdm_g : 1;
   const int mb = t.tdm_mb > 0 ? t.tdm_mb : poisson_tdm_modes(nx);
@@ -1921,6 +2088,8 @@ cudaError_t configure_kernels() {
   e = cudaFuncSetAttribute(k_poisson_inv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_poisson_tdm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTdmSmemMax);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_poisson_tdm_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTdmSmemMax);
   return e;
 }
 
@@ -2105,10 +2274,23 @@ void launch_poisson_fwd_q(cudaStream_t s, const Grid &g, const Bufs &b, const do
   poisson_fwd_any<true>(s, g, b, sc, k, b.qx, b.qy);
 }
 
+int g_tdm_cluster = 1;
+
+bool tdm_uses_cluster(const Tiles &t, int nx) {
+  return g_tdm_cluster && t.tdm_cl && t.tdm_g == 4 &&
+         4 * 32 * (size_t)tdm_stride(nx, 4) * sizeof(double) <= kTdmSmemMax;
+}
+
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b) {
   const int G = b.tiles.tdm_g > 0 ? b.tiles.tdm_g : 1;
   const int pairs = g.ny / 4 + 1;
   const double4_32a *fac = reinterpret_cast<const double4_32a *>(b.tdm_fac[tdm_group_index(G)]);
+  if (tdm_uses_cluster(b.tiles, g.nx)) {  // four CTAs per pair, four warps each
+    const int L = tdm_chunk(g.nx, 4), S = tdm_stride(g.nx, 4);
+    launch_pdl(k_poisson_tdm_cl, dim3(kTdmCluster * pairs, 1, g.nc), 128, 4 * 32 * (size_t)S * sizeof(double), s, g,
+               L, S, fac, b.twiddle, b.spec);
+    return;
+  }
   if (tdm_global_stage(g.nx, G)) {  // one pair per block, staged in b.tdm_stage
     launch_pdl(k_poisson_tdm<true>, dim3(pairs, 1, g.nc), 128 * G, 0, s, g, 1, G, tdm_chunk(g.nx, G), tdm_stride(g.nx, G),
                                                                  fac, b.twiddle, b.spec, b.tdm_stage);

@@ -22,6 +22,8 @@ struct Tiles {
                // tdm_warps_for from the grid (it changes the rounding, so it is not tuned)
   int compact;  // 1: the FP64 work of the corner-gradient and curvature branches is
                 // compacted to the first threads of each block; 0: done in place
+  int tdm_cl;   // 1: at tdm_g = 4 the tridiagonal solves run as clusters of four CTAs per
+                // wavenumber pair (k_poisson_tdm_cl, the same bits as one block per pair)
 };
 Tiles default_tiles(int ny);
 
@@ -210,6 +212,9 @@ int tdm_chunk(int nx, int G);
 int tdm_group_index(int G);  // 1, 2, 4 -> 0, 1, 2
 int tdm_warps_for(int nx, int ny, int nc);
 int tdm_modes_per_block(const Tiles &t, int nx);
+// the tridiagonal solves run as k_poisson_tdm_cl (switch g_tdm_cluster, tile choice tdm_cl, tdm_g = 4)
+extern int g_tdm_cluster;
+bool tdm_uses_cluster(const Tiles &t, int nx);
 size_t poisson_tdm_smem(int nx, int mb, int G);
 size_t poisson_fft_smem(int ny, int w);
 bool fft_w_fits(int ny, int w);

@@ -310,3 +310,34 @@ def test_batch_geometry_ahead_identical(libs, resident):
     for k in range(len(wls)):
         for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
             assert np.array_equal(runs[False][1][k].field(s), runs[True][1][k].field(s)), (k, s)
+
+
+@pytest.mark.gpu
+def test_batch_tdm_cluster_identical(libs):
+    """the ensemble's three grids batched, resident, with the tridiagonal
+    solves of the four-warp groups (512 x 256) as clusters of four CTAs per
+    wavenumber pair and as one block per pair: the same bits"""
+    gpu, orc = libs
+    wls = ensemble_extremes()
+    st0 = prepare(gpu, orc, wls)
+    runs, modes = {}, {}
+    try:
+        for on in (True, False):
+            gpu.set_tdm_cluster(on)
+            gpu.set_sync_mode(SYNC_NONE)
+            batch = [clone(s) for s in st0]
+            dts = [list(gpu.integrate_batch(batch)) for _ in range(4)]
+            gpu.batch_sync_to_host(batch)
+            ng = len(gpu.batch_groups())
+            modes[on] = sorted((gpu.tiles(g)["tdm_warps"], gpu.tiles(g)["tdm_modes"]) for g in range(ng))
+            gpu.batch_release()
+            runs[on] = (dts, batch)
+    finally:
+        gpu.set_tdm_cluster(True)
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.batch_release()
+    assert (4, 0) in modes[True] and all(m > 0 for _, m in modes[False]), modes
+    assert runs[False][0] == runs[True][0]
+    for k in range(len(wls)):
+        for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+            assert np.array_equal(runs[False][1][k].field(s), runs[True][1][k].field(s)), (k, s)

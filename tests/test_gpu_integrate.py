@@ -131,6 +131,42 @@ def test_pdl_equals_plain_launches(libs, graphs):
         assert np.array_equal(a.field(s), b.field(s)), s
 
 
+@pytest.mark.parametrize("nx,ny,graphs", [(512, 256, True), (600, 256, True), (600, 256, False)],
+                         ids=["512x256", "600x256", "600x256_eager"])
+def test_tdm_cluster_equals_block_solves(libs, nx, ny, graphs):
+    """the tridiagonal solves of a wavenumber pair spread over a cluster of
+    four CTAs (chunk maps through distributed shared memory) give the bits of
+    one block per pair at four warps a system; 600 rows leave the last CTA of
+    each cluster partly past the wall"""
+    gpu, orc = libs
+    wl = ic.bubble_swarm(nx, ny, nbubbles=8, seed=4)
+    st0 = prepare(libs, wl)
+    runs, modes = {}, {}
+    gpu.set_use_graphs(graphs)
+    try:
+        for on in (True, False):
+            gpu.release()
+            gpu.set_tdm_cluster(on)
+            st = clone(st0)
+            dts = [gpu.integrate(st) for _ in range(2)]
+            gpu.set_sync_mode(SYNC_NONE)
+            dts += [gpu.integrate(st) for _ in range(2)]
+            gpu.sync_to_host(st)
+            gpu.set_sync_mode(SYNC_STATE)
+            t = gpu.tiles()
+            modes[on] = (t["tdm_warps"], t["tdm_modes"])
+            runs[on] = (dts, st)
+    finally:
+        gpu.set_tdm_cluster(True)
+        gpu.set_use_graphs(True)
+        gpu.set_sync_mode(SYNC_STATE)
+        gpu.release()
+    assert modes[True] == (4, 0) and modes[False][0] == 4 and modes[False][1] > 0, modes
+    assert runs[True][0] == runs[False][0]
+    for s in ("ux", "uy", "p", "psi0", "psi1", "vof"):
+        assert np.array_equal(runs[True][1].field(s), runs[False][1].field(s)), s
+
+
 def test_matches_reference_fixtures(libs):
     """the GPU against the reference's own results (golden fixtures made by
     tests/golden/make_golden.py from the reference sources)"""
