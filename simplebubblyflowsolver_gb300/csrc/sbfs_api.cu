@@ -513,7 +513,8 @@ int build_ctx(Ctx *c, const domain_t *d, int nc) {
                      &b.visux, &b.visuy, &b.txx, &b.txy, &b.tyy, &b.curv, &b.ifrcx, &b.ifrcy, &b.fluxx, &b.fluxy,
                      &b.mfluxx, &b.mfluxy, &b.srcux[0], &b.srcux[1], &b.srcux[2], &b.srcuy[0], &b.srcuy[1],
                      &b.srcuy[2], &b.srcvof[0], &b.srcvof[1], &b.egx, &b.egy, &b.pxx, &b.pyy, &b.pxy, &b.pyx,
-                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt, &b.ifrcx3, &b.ifrcy3, &b.qx, &b.qy};
+                     &b.ifrcx2, &b.ifrcy2, &b.vof_alt, &b.ifrcx3, &b.ifrcy3, &b.qx, &b.qy,
+                     &b.rhofx, &b.rhofy, &b.dpsix, &b.dpsiy};
   for (double **p : scal)
     if (dalloc(*c, p, n1 * nc)) return 1;
   if (dalloc(*c, &b.dvof, n2 * nc)) return 1;
@@ -949,16 +950,21 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   if (force_side) cudaStreamWaitEvent(c.s, c.evF, 0);
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[2], 0);  // p is in
   if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[3], 0);  // psi is in
+  // the face sums of rho and the differences of psi_old come from the last
+  // substage's predictor and correction: this step's, or for the first
+  // substage the last device-resident step's (the same condition as its
+  // geometry, pre_first)
+  const bool cached = k > 0 || c.pre_first;
   timed(c, KC_PREDICT, [&] {
     launch_predict_mf(c.s, c.g, c.m, c.ph, b, sc, k, ux, uy, uxs, uys, den0, den1, psio, sxa, sxb, sya, syb, ifx,
-                      ify);
+                      ify, cached);
   });
   timed(c, KC_POISSON_FWD, [&] { launch_poisson_fwd_q(c.s, c.g, b, sc, k); });
   timed(c, KC_POISSON_TDM, [&] { launch_poisson_tdm(c.s, c.g, b); });
   timed(c, KC_POISSON_INV, [&] { launch_poisson_inv(c.s, c.g, b, psin); });
   // psi of substages 2 and 3 are final: the caller's psi[1] and psi[0] after the step
   if (c.link && k >= 1) link_out(c, k == 1 ? HL_PSI1_OUT : HL_PSI0_OUT, L_P, psin);
-  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, b, sc, k, uxs, uys, psin, true); });
+  timed(c, KC_CORRECT, [&] { launch_correct(c.s, c.g, c.m, b, sc, k, uxs, uys, psin, true, k < 2 || c.make_next); });
   c.iu ^= 1;
   c.ipsi ^= 1;
   c.iden ^= 1;
@@ -2208,7 +2214,7 @@ int fluid_correct_velocity(const domain_t *d, const double dt_old, const double 
     return 1;
   if (put_scalars(*c, 0., -1, dt_old, dt_new)) return 1;
   launch_face_factor(c->s, c->g, c->ph, b, b.den1, b.psi0);
-  launch_correct(c->s, c->g, c->m, b, b.scalars, 0, b.ux, b.uy, b.psi1, false);
+  launch_correct(c->s, c->g, c->m, b, b.scalars, 0, b.ux, b.uy, b.psi1, false, false);
   if (d2h(*c, f->ux, L_UX, b.ux) || d2h(*c, f->uy, L_UY, b.uy)) return 1;
   return sync(*c);
 }

@@ -893,9 +893,16 @@ __global__ void __launch_bounds__(BX *BY)
 // term of the Poisson right-hand side (src/fluid/compute_potential.c:
 // 285-363) and of the velocity correction (src/fluid/correct_velocity/ux.c:
 // 18-66, uy.c:17-64) is the same face quantity, so both read it from here.
+// CACHED: 2 rho^k at the faces is the 2 rho^{k+1} the previous substage's
+// predictor formed (srx, sry, which this one overwrites with its own), and
+// psi_old's differences across the faces are the ones the previous
+// substage's correction formed (dpx, dpy); else both come from den0 and
+// psio (first substage of a step whose state may be new).  The same values
+// either way.
 // thread (I, J): I = 1..nx handles the ux face I (I >= 2) and the uy face
 // (I, J - 1/2)
 // ---------------------------------------------------------------------------
+template <bool CACHED>
 __global__ void __launch_bounds__(BX *BY)
     k_predict_mf(Grid g, Metrics m, Phys ph0, const double *__restrict__ sc, int k, const double *__restrict__ ux,
                  const double *__restrict__ uy, double *__restrict__ ux_out, double *__restrict__ uy_out,
@@ -905,7 +912,8 @@ __global__ void __launch_bounds__(BX *BY)
                  const double *__restrict__ psio, double *__restrict__ sxa, const double *__restrict__ sxb,
                  double *__restrict__ sya, const double *__restrict__ syb, double *__restrict__ egx,
                  double *__restrict__ egy, const double *__restrict__ coltab, double *__restrict__ qx,
-                 double *__restrict__ qy) {
+                 double *__restrict__ qy, double *__restrict__ srx, double *__restrict__ sry,
+                 const double *__restrict__ dpx, const double *__restrict__ dpy) {
   pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   const double *__restrict__ gx = coltab + ((size_t)blockIdx.z * 3 * kColTabs + ct_gdt2x(k)) * g.ct;
@@ -924,23 +932,25 @@ __global__ void __launch_bounds__(BX *BY)
   // e grad psi_old is stored times the Poisson factor pax (x faces) or pay
   // (y faces): e pa = (2 rho_ref pa) / (2 rho) - pa
   const double rpx = sc[sc_rpx(k)], pax = sc[sc_pax(k)];
-  const double ps0 = psio[ix(g, r, I)];
+  const double ps0 = CACHED && I != 1 && I != g.nx ? 0. : psio[ix(g, r, I)];
   // ---- ux at face I
   if (I >= 2) {
     const double u0 = ux[ix(g, r, I - 1)];
     double a = ifrcx[ix(g, r, I - 2)];
-    const double rho0 = den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];  // 2 rho^k
+    const double rho0 = CACHED ? srx[ix(g, r, I - 1)] : den0[ix(g, r, I - 1)] + den0[ix(g, r, I)];  // 2 rho^k
     a = fma(ph.hgrav, rho0, a);
     a = fma(m.q4f[I], pxx[ix(g, r, I - 1)] - pxx[ix(g, r, I - 2)], a);
     a = fma(g.q4y, pxy[ix(g, rp, I - 1)] - pxy[ix(g, r, I - 1)], a);
-    const double ir2 = rcp_nr(den1[ix(g, r, I - 1)] + den1[ix(g, r, I)]);  // 1 / (2 rho^{k+1})
+    const double rho1 = den1[ix(g, r, I - 1)] + den1[ix(g, r, I)];  // 2 rho^{k+1}
+    srx[ix(g, r, I - 1)] = rho1;
+    const double ir2 = rcp_nr(rho1);
     double u = fma(adt2, a, rho0 * u0);
     if (k != 0) u = fma(bdt2, sxb[ix(g, r, I - 2)], u);
     u = fma(gx[I], p[ix(g, r, I - 1)] - p[ix(g, r, I)], u);
     const double us = u * ir2;
     ux_out[ix(g, r, I - 1)] = us;
     sxa[ix(g, r, I - 2)] = a;
-    const double e = fma(rpx, ir2, -pax) * (ps0 - psio[ix(g, r, I - 1)]);
+    const double e = fma(rpx, ir2, -pax) * (CACHED ? dpx[ix(g, r, I - 1)] : ps0 - psio[ix(g, r, I - 1)]);
     egx[ix(g, r, I - 1)] = e;
     qx[ix(g, r, I - 1)] = fma(sc[sc_pdx(k)], us, e);
   }
@@ -950,15 +960,18 @@ __global__ void __launch_bounds__(BX *BY)
     double a = ifrcy[ix(g, r, I - 1)];
     a = fma(m.q4c[I], pyx[ix(g, r, I)] - pyx[ix(g, r, I - 1)], a);
     a = fma(g.q4y, pyy[ix(g, r, I - 1)] - pyy[ix(g, rm, I - 1)], a);
-    const double rho0 = den0[ix(g, rm, I)] + den0[ix(g, r, I)];  // 2 rho^k
-    const double ir2 = rcp_nr(den1[ix(g, rm, I)] + den1[ix(g, r, I)]);
+    const double rho0 = CACHED ? sry[ix(g, r, I)] : den0[ix(g, rm, I)] + den0[ix(g, r, I)];  // 2 rho^k
+    const double rho1 = den1[ix(g, rm, I)] + den1[ix(g, r, I)];
+    sry[ix(g, r, I)] = rho1;
+    const double ir2 = rcp_nr(rho1);
     double u = fma(adt2, a, rho0 * w0);
     if (k != 0) u = fma(bdt2, syb[ix(g, r, I - 1)], u);
     u = fma(sc[sc_gdt2y(k)], p[ix(g, rm, I)] - p[ix(g, r, I)], u);
     const double ws = u * ir2;
     uy_out[ix(g, r, I)] = ws;
     sya[ix(g, r, I - 1)] = a;
-    const double e = fma(sc[sc_rpy(k)], ir2, -sc[sc_pay(k)]) * (ps0 - psio[ix(g, rm, I)]);
+    const double e =
+        fma(sc[sc_rpy(k)], ir2, -sc[sc_pay(k)]) * (CACHED ? dpy[ix(g, r, I)] : ps0 - psio[ix(g, rm, I)]);
     egy[ix(g, r, I)] = e;
     qy[ix(g, r, I)] = fma(sc[sc_pdy(k)], ws, e);
   }
@@ -1540,11 +1553,14 @@ __global__ void __cluster_dims__(kTdmCluster, 1, 1) __launch_bounds__(128)
 //   come per column (cnew / HXXF(I), cold / HXXF(I) / pax), the y ones per case
 // thread (I, J): I = 1..nx
 // ---------------------------------------------------------------------------
-template <bool PRES>
+// DP: also stores psi_new's differences across the faces for the next
+// substage's predictor (dpx, dpy; the fused step)
+template <bool PRES, bool DP>
 __global__ void __launch_bounds__(BX *BY)
     k_correct(Grid g, const double *__restrict__ sc, const double *__restrict__ coltab, int k,
               double *__restrict__ ux, double *__restrict__ uy, const double *__restrict__ psin,
-              const double *__restrict__ egx, const double *__restrict__ egy, double *__restrict__ p) {
+              const double *__restrict__ egx, const double *__restrict__ egy, double *__restrict__ p,
+              double *__restrict__ dpx, double *__restrict__ dpy) {
   pdl_entry();
   sc += (size_t)blockIdx.z * (kScalars);
   const double *__restrict__ ct = coltab + (size_t)blockIdx.z * 3 * kColTabs * g.ct;
@@ -1558,13 +1574,17 @@ __global__ void __launch_bounds__(BX *BY)
   const double pn0 = psin[ix(g, r, I)];
   if (I >= 2) {
     double u = ux[ix(g, r, I - 1)];
-    u = fma(-cn[I], pn0 - psin[ix(g, r, I - 1)], u);
+    const double d = pn0 - psin[ix(g, r, I - 1)];
+    if (DP) dpx[ix(g, r, I - 1)] = d;
+    u = fma(-cn[I], d, u);
     u = fma(co[I], egx[ix(g, r, I - 1)], u);
     ux[ix(g, r, I - 1)] = u;
   }
   {
     double u = uy[ix(g, r, I)];
-    u = fma(-cnewy, pn0 - psin[ix(g, rm, I)], u);
+    const double d = pn0 - psin[ix(g, rm, I)];
+    if (DP) dpy[ix(g, r, I)] = d;
+    u = fma(-cnewy, d, u);
     u = fma(coldyp, egy[ix(g, r, I)], u);
     uy[ix(g, r, I)] = u;
   }
@@ -2228,10 +2248,11 @@ void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
                        const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
                        const double *den0, const double *den1, const double *psi_old, double *srcux_a,
                        const double *srcux_b, double *srcuy_a, const double *srcuy_b, const double *ifx,
-                       const double *ify) {
-  launch_pdl(k_predict_mf, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g,
-             m, ph, sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, ifx, ify, den0, den1,
-             psi_old, srcux_a, srcux_b, srcuy_a, srcuy_b, b.egx, b.egy, b.coltab, b.qx, b.qy);
+                       const double *ify, bool cached) {
+  auto kern = cached ? k_predict_mf<true> : k_predict_mf<false>;
+  launch_pdl(kern, tile_grid(b.tiles, TK_PREDICT, g.nx, g.ny, g.nc), tile_block(b.tiles, TK_PREDICT), 0, s, g, m, ph,
+             sc, k, ux, uy, ux_out, uy_out, b.pxx, b.pyy, b.pxy, b.pyx, b.p, ifx, ify, den0, den1, psi_old, srcux_a,
+             srcux_b, srcuy_a, srcuy_b, b.egx, b.egy, b.coltab, b.qx, b.qy, b.rhofx, b.rhofy, b.dpsix, b.dpsiy);
 }
 
 void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, const double *sc,
@@ -2326,12 +2347,11 @@ void launch_poisson(cudaStream_t s, const Grid &g, const Bufs &b, const double *
 }
 
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
-                    double *ux, double *uy, const double *psi_new, bool pressure) {
+                    double *ux, double *uy, const double *psi_new, bool pressure, bool dpsi) {
   const dim3 gr = tile_grid(b.tiles, TK_CORRECT, g.nx, g.ny, g.nc), bl = tile_block(b.tiles, TK_CORRECT);
-  if (pressure)
-    launch_pdl(k_correct<true>, gr, bl, 0, s, g, sc, b.coltab, k, ux, uy, psi_new, b.egx, b.egy, b.p);
-  else
-    launch_pdl(k_correct<false>, gr, bl, 0, s, g, sc, b.coltab, k, ux, uy, psi_new, b.egx, b.egy, b.p);
+  auto kern = pressure ? (dpsi ? k_correct<true, true> : k_correct<true, false>)
+                       : (dpsi ? k_correct<false, true> : k_correct<false, false>);
+  launch_pdl(kern, gr, bl, 0, s, g, sc, b.coltab, k, ux, uy, psi_new, b.egx, b.egy, b.p, b.dpsix, b.dpsiy);
 }
 
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new) {

@@ -51,6 +51,10 @@ struct Bufs {
   // the fused step's Poisson right-hand side at the faces, pd u* + e grad
   // psi_old (k_predict_mf writes them, the transform differences them)
   double *qx, *qy;
+  // the fused step's 2 rho at the faces (the last predictor's den1 sums) and
+  // psi's differences across the faces (the last correction's), which the
+  // next substage's predictor reads instead of forming them again
+  double *rhofx, *rhofy, *dpsix, *dpsiy;
   // Poisson: spectrum [nx][ny/2+1] complex, Thomas factors, twiddles
   double2 *spec;
   double2 *tdm_fac[3];  // (w, v, P, Q) per row for 1, 2, 4 warps per system, see k_poisson_tdm
@@ -124,7 +128,7 @@ void launch_predict_mf(cudaStream_t s, const Grid &g, const Metrics &m, const Ph
                        const double *sc, int k, const double *ux, const double *uy, double *ux_out, double *uy_out,
                        const double *den0, const double *den1, const double *psi_old, double *srcux_a,
                        const double *srcux_b, double *srcuy_a, const double *srcuy_b, const double *ifx,
-                       const double *ify);
+                       const double *ify, bool cached);
 // fused step with the interface geometry ahead of the velocity: curvature,
 // interface-cell list and the cells' THINC factors from vof and the corner
 // normals alone (counts reset first)
@@ -146,9 +150,10 @@ void launch_poisson_fwd(cudaStream_t s, const Grid &g, const Bufs &b, const doub
 void launch_poisson_fwd_q(cudaStream_t s, const Grid &g, const Bufs &b, const double *sc, int k);
 void launch_poisson_tdm(cudaStream_t s, const Grid &g, const Bufs &b);
 void launch_poisson_inv(cudaStream_t s, const Grid &g, const Bufs &b, double *psi_new);
-// velocity correction (+ pressure); reads b.egx, b.egy
+// velocity correction (+ pressure); reads b.egx, b.egy; dpsi: also stores
+// psi_new's face differences (b.dpsix, b.dpsiy) for the next predictor
 void launch_correct(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, const double *sc, int k,
-                    double *ux, double *uy, const double *psi_new, bool pressure);
+                    double *ux, double *uy, const double *psi_new, bool pressure, bool dpsi);
 void launch_pressure(cudaStream_t s, const Grid &g, const Bufs &b, const double *psi_new);
 // decide_dt: the column and domain maxima, then the finishing kernel (dt, the
 // scalars and, with a coltab, the column tables); acc holds nx + 8 zero
