@@ -67,11 +67,11 @@ ALG_DOUBLES_PER_CELL = {
     "k_flux_force": 5 + 4,     # ux, uy, vof, den, curv -> fluxx, fluxy, ifrcx, ifrcy
     "k_vof_advance": 6 + 5,    # fluxx, fluxy, vof, src_b, ux, uy -> src_a, vof, den1, mflux(2)
     "k_momflux": 6 + 4,        # ux, uy, visux, visuy, mflux(2) -> momentum fluxes (4)
-    "k_predict_mf": 14 + 8,    # ux, uy, fluxes(4), p, ifrc(2), den(2), psi_old, src_b(2) -> u*(2), src_a(2), e grad psi(2), q(2)
+    "k_predict_mf": 16 + 10,   # ux, uy, fluxes(4), p, ifrc(2), den1, 2rho(2), dpsi(2), src_b(2) -> u*(2), src_a(2), e grad psi(2), q(2), 2rho(2)
     "k_poisson_fwd": 2 + 1,    # q(2) -> spectrum
     "k_poisson_tdm": 2 + 1,    # spectrum, pivots -> spectrum
     "k_poisson_inv": 1 + 1,    # spectrum -> psi
-    "k_correct": 6 + 3,        # u*(2), psi, e grad psi(2), p -> u(2), p
+    "k_correct": 6 + 5,        # u*(2), psi, e grad psi(2), p -> u(2), p, dpsi(2)
     "k_decide_dt": 2,          # ux, uy
     "k_csf_force": 3 + 2,      # vof, den, curv -> ifrcx, ifrcy
     "k_face_flux": 0,          # listed cells only
