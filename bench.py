@@ -499,7 +499,8 @@ def metric_arms(args, lib):
             per_grid[key].append(ms / steps)
     one_ms = sum(sum(per_grid[(w.nx, w.ny)]) / len(per_grid[(w.nx, w.ny)]) for w in wls)
     t0 = time.perf_counter()
-    _, params, hist = L.train_default(lib, seed=0)
+    tstats = {}
+    _, params, hist = L.train_default(lib, seed=0, stats=tstats)
     train_s = time.perf_counter() - t0
     lib.mlp_set_params(params)
     learned = batched(1)
@@ -520,6 +521,9 @@ def metric_arms(args, lib):
             "learned_batched_over_plain_one_at_a_time": round(learned / (cells / one_ms * 1e3 / 1e6), 3),
             "learned_batched_over_plain_batched": round(learned / plain, 4),
             "steps": steps, "train_s": round(train_s, 1), "train_final_loss": hist[-1],
+            "training": dict(tstats, note="the closure's training on the GPU: data generation (exact-area and "
+                             "solver-advected circles, relaxed drops) and the Adam epochs (1024-row batches, "
+                             "one gradient and one update launch each); rows_per_s = epochs x rows / training s"),
             "static_drop_64": dict(drop, steps=nsteps, note="kappa: rms relative error of the curvature the "
                                    "last substage used in the interface cells (exact 1/r = 4); umax_mean: "
                                    "max |u| sampled 20 times over the run, averaged (parasitic currents); "

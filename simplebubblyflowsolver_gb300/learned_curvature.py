@@ -418,13 +418,24 @@ def training_set(lib, ncircles=200000, advected=True, relaxed=True, n=1024, nfie
     return features(symmetries(st)), np.tile(lab, 8).astype(np.float32)
 
 
-def train_default(lib, ncircles=200000, epochs=40, seed=0, advected=True, relaxed=True, log=None, rmax=128.0):
+def train_default(lib, ncircles=200000, epochs=40, seed=0, advected=True, relaxed=True, log=None, rmax=128.0,
+                  stats=None):
     """train the closure on the default data set on the GPU (radii up to rmax
-    cells, see training_set); returns (model, parameters, loss history)"""
+    cells, see training_set); returns (model, parameters, loss history).
+    stats (a dict, optional) receives the rows, the epochs, the seconds of
+    data generation and of training, and the training rows per second
+    (epochs x rows over the training time)"""
+    import time
+    t0 = time.perf_counter()
     X, Y = training_set(lib, ncircles, advected=advected, relaxed=relaxed, seed=seed, log=log, rmax=rmax)
+    t1 = time.perf_counter()
     m = GpuCurvatureModel(lib, X, Y)
     m.set_params(init_params(seed))
     hist = m.train(epochs=epochs, seed=seed, log=log)
+    t2 = time.perf_counter()
+    if stats is not None:
+        stats.update(rows=int(X.shape[0]), epochs=epochs, data_s=round(t1 - t0, 2), train_s=round(t2 - t1, 2),
+                     rows_per_s=round(epochs * X.shape[0] / (t2 - t1)))
     return m, m.params(), hist
 
 
