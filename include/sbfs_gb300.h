@@ -81,7 +81,9 @@ int sbfs_free_state(domain_t *domain, fluid_t *fluid, interface_t *interface);
  *     them (and psi[1]) back on exit;
  *   SBFS_SYNC_ALL: as STATE, and also write back every other array the
  *     reference leaves filled (den, viscosities, stresses, sources, fluxes,
- *     interface geometry);
+ *     interface geometry), as the steps taken in this mode leave them (the
+ *     other modes keep some of them in their own form: viscosities
+ *     pre-scaled, the next step's interface geometry formed ahead);
  *   SBFS_SYNC_NONE: device-resident; the state is uploaded on the first call
  *     (or after sbfs_invalidate_device) and stays on the GPU between calls;
  *     call sbfs_sync_to_host before reading host arrays and

@@ -268,7 +268,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   const int nx = c.nx, n = nx + 3;
   const double hy = d->hy;
   const double dx = d->hxxc[0];
-  constexpr int NCOL = 13;
+  constexpr int NCOL = 15;
   std::vector<double> h(NCOL * (size_t)n * c.nc, 0.);
   for (int k = 0; k < c.nc; ++k) {
     const double nu = 1. / Re[k];
@@ -283,6 +283,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
       A(8, I) = 0.5 * (1. / hf);
       A(10, I) = dx / hf;
       A(12, I) = 2. * (nu / hf);
+      A(14, I) = 0.5 * (hy / hf);
     }
     for (int I = 1; I <= nx; ++I) {
       const double ihc = 1. / d->hxxc[I - 1];
@@ -291,6 +292,7 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
       A(7, I) = 0.25 * ihc;
       A(9, I) = 0.5 * ihc;
       A(11, I) = 4. * (nu * ihc);
+      A(13, I) = 2. * (hy * ihc);
     }
   }
   c.g.cm = c.nc > 1 ? NCOL * n : 0;
@@ -313,6 +315,8 @@ int upload_metrics(Ctx &c, const domain_t *d, const double *Re) {
   c.m.rq = b + 10 * n;
   c.m.c4nuc = b + 11 * n;
   c.m.c2nuf = b + 12 * n;
+  c.m.c4nucs = b + 13 * n;
+  c.m.c2nufs = b + 14 * n;
   c.Re = Re[0];
   return 0;
 }
@@ -345,6 +349,17 @@ void finish_phys(Phys &p, const Grid &g) {
   p.qfy = p.qf * g.ihy;
   p.nuy2 = 2. * p.nuy;
   p.nuy4 = 4. * p.nuy;
+  p.vsx_c = p.vm1 * p.nuy2;
+  p.vsx_c2 = p.hvm1 * p.nuy2;
+  p.vsx_1 = p.nuy2;
+  p.vsx_lo = p.vis_lo * p.nuy2;
+  p.vsx_hi = p.vis_hi * p.nuy2;
+  p.vsy_c2 = p.hvm1 * p.nuy4;
+  p.vsy_1 = p.nuy4;
+  p.vsy_lo = p.vis_lo * p.nuy4;
+  p.vsy_hi = p.vis_hi * p.nuy4;
+  p.inuy2 = 1. / p.nuy2;
+  p.inuy4 = 1. / p.nuy4;
 }
 
 void set_phys(Ctx &c, const fluid_t *f, const interface_t *itf) {
@@ -709,8 +724,12 @@ int g_curv_model = 0;
 // curvature model and the closure's parameters and range
 unsigned long long geo_cfg() {
   return (unsigned long long)g_curv_model | ((unsigned long long)g_geo_ahead << 1) |
-         ((unsigned long long)g_mlp_epoch << 8);
+         ((unsigned long long)(g_sync_mode == SBFS_SYNC_ALL) << 2) | ((unsigned long long)g_mlp_epoch << 8);
 }
+
+// the fused step keeps its viscosities pre-scaled for k_momflux, except when
+// every array is synchronised to the host (the reference's visux, visuy)
+bool scaled_vis() { return g_sync_mode != SBFS_SYNC_ALL; }
 
 // the device state or its configuration changes outside a step: a first
 // substage geometry formed ahead by the last step is stale
@@ -869,7 +888,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
         launch_bulk_flux(c.s2, c.g, c.m, c.ph, b, ux, uy);
         cudaEventRecord(c.evx, c.s2);
       }
-      timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+      timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr, scaled_vis()); });
       timed(c, KC_CURV_LIST, [&] { launch_geometry(c.s, c.g, c.m, b); });
       if (learned) timed(c, KC_MLP_CURV, [&] { launch_mlp_curv(c.s, c.g, b); });
       if (par) {
@@ -896,7 +915,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
       cudaStreamWaitEvent(c.s, c.evp, 0);
       c.props_ahead = false;
     } else {
-      timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr); });
+      timed(c, KC_PROPS, [&] { launch_props(c.s, c.g, c.m, c.ph, b, false, true, true, nullptr, scaled_vis()); });
     }
     if (c.link && k == 0) cudaStreamWaitEvent(c.s, c.evh[1], 0);  // the velocity is in
     timed(c, KC_CURV_LIST, [&] { launch_interface_stage(c.s, c.g, c.m, c.ph, b, ux, uy, den0, 0); });
@@ -925,7 +944,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
   // txx, txy, tyy when every array is synchronised), as the reference's
   // fluid_t holds the stress of its last predictor
   const int stress = k < 2 ? 0 : (g_sync_mode == SBFS_SYNC_ALL ? 2 : 1);
-  timed(c, KC_MOMFLUX, [&] { launch_momflux(c.s, c.g, c.m, c.ph, b, ux, uy, stress); });
+  timed(c, KC_MOMFLUX, [&] { launch_momflux(c.s, c.g, c.m, c.ph, b, ux, uy, stress, scaled_vis()); });
   if (par && (k < 2 || (ahead && c.make_next))) {
     // the next substage's viscosities and corner normals (and, ahead, its
     // geometry and force from the new vof and density) need only the new
@@ -935,7 +954,7 @@ void enqueue_substage(Ctx &c, int k, bool par, bool wait_dt) {
     // substage's (force into IFX[2]; the step joins them at its end)
     cudaEventRecord(c.evf, c.s);
     cudaStreamWaitEvent(c.s2, c.evf, 0);
-    launch_props(c.s2, c.g, c.m, c.ph, b, false, true, true, nullptr);
+    launch_props(c.s2, c.g, c.m, c.ph, b, false, true, true, nullptr, scaled_vis());
     if (ahead) {
       const int nb = k < 2 ? (k + 1) & 1 : 2;
       launch_geometry(c.s2, c.g, c.m, b);

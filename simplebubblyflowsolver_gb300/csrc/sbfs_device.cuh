@@ -39,6 +39,10 @@ struct Metrics {
   const double *rq;     // HXXC / HXXF(I)       (metric ratio of the ux advection along y)
   const double *c4nuc;  // 4 (1 / Re) / HXXC(I) (4 nu txx)
   const double *c2nuf;  // 2 (1 / Re) / HXXF(I) (4 nu txy)
+  // the same with the viscosities pre-scaled (k_props<..., true>): c4nuc / nuy2
+  // and c2nuf / nuy4, which no longer depend on the case
+  const double *c4nucs;  // 2 hy / HXXC(I)
+  const double *c2nufs;  // hy / (2 HXXF(I))
 };
 
 struct Grid {
@@ -77,6 +81,11 @@ struct Phys {
   double nuy;         // nu / hy
   double qf, qfy;     // force_coef / 4, force_coef / 4 / hy
   double nuy2, nuy4;  // 2 nu / hy, 4 nu / hy (k_momflux)
+  // the fused step's viscosities pre-scaled for k_momflux, visux by nuy2 and
+  // visuy by nuy4: visr - 1, (visr - 1) / 2, 1 and the clip bounds scaled alike
+  double vsx_c, vsx_c2, vsx_1, vsx_lo, vsx_hi;
+  double vsy_c2, vsy_1, vsy_lo, vsy_hi;
+  double inuy2, inuy4;  // 1 / nuy2, 1 / nuy4 (the wall stress from scaled sums)
 };
 
 // x / 2 for a positive normal x (x >= 2^-1021), exactly: the exponent field

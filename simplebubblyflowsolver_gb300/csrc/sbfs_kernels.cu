@@ -103,8 +103,11 @@ __device__ __forceinline__ void corner_normal(const Grid &g, const Metrics &m, c
 
 // compact: the corners with a gradient are handed to the block's first
 // threads (see the interface-branch compaction below); otherwise each thread
-// does its own.  The same arithmetic either way.
-template <bool DEN, bool VIS, bool GRAD>
+// does its own.  The same arithmetic either way.  SCALED: the fused step's
+// viscosities, visux times 2 nu / hy and visuy times 4 nu / hy (the factors
+// k_momflux would otherwise apply per cell), formed with the constants and
+// clip bounds scaled alike: the same two FP64 operations per face
+template <bool DEN, bool VIS, bool GRAD, bool SCALED = false>
 __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, const double *__restrict__ vof,
                                                   double *__restrict__ den, double *__restrict__ visux,
                                                   double *__restrict__ visuy, double *__restrict__ dvof,
@@ -124,15 +127,16 @@ __global__ void __launch_bounds__(BX *BY) k_props(Grid g, Metrics m, Phys ph0, c
     if (DEN) den[ix(g, r, I)] = clip_pos(fma(ph.dm1, v, 1.), ph.den_lo, ph.den_hi);
     if (VIS) {
       // 1 + (visr - 1) 0.5 (a + b) = 1 + c2 (a + b), c2 = (visr - 1) / 2
-      const double c = ph.vm1, c2 = ph.hvm1;
+      const double c = SCALED ? ph.vsx_c : ph.vm1, c2 = SCALED ? ph.vsx_c2 : ph.hvm1, one = SCALED ? ph.vsx_1 : 1.;
       if (I >= 1) {
         double vis;
-        if (I == 1) vis = fma(c, vof[ix(g, r, 0)], 1.);
-        else if (I == g.nx + 1) vis = fma(c, v, 1.);
-        else vis = fma(c2, vof[ix(g, r, I - 1)] + v, 1.);
-        visux[ix(g, r, I - 1)] = clip_pos(vis, ph.vis_lo, ph.vis_hi);
+        if (I == 1) vis = fma(c, vof[ix(g, r, 0)], one);
+        else if (I == g.nx + 1) vis = fma(c, v, one);
+        else vis = fma(c2, vof[ix(g, r, I - 1)] + v, one);
+        visux[ix(g, r, I - 1)] = SCALED ? clip_pos(vis, ph.vsx_lo, ph.vsx_hi) : clip_pos(vis, ph.vis_lo, ph.vis_hi);
       }
-      visuy[ix(g, r, I)] = clip_pos(fma(c2, vof[ix(g, rm, I)] + v, 1.), ph.vis_lo, ph.vis_hi);
+      const double vy = SCALED ? fma(ph.vsy_c2, vof[ix(g, rm, I)] + v, ph.vsy_1) : fma(c2, vof[ix(g, rm, I)] + v, 1.);
+      visuy[ix(g, r, I)] = SCALED ? clip_pos(vy, ph.vsy_lo, ph.vsy_hi) : clip_pos(vy, ph.vis_lo, ph.vis_hi);
     }
     if (GRAD && I >= 1) {
       // zero where the four values are bitwise equal (single-phase bulk)
@@ -832,11 +836,13 @@ __global__ void __launch_bounds__(BX *BY)
 // Poisson face fluxes below) against 16 + 61 for k_stress + k_predict.
 // STRESS 1: also txy at the wall columns I = 1, nx + 1 (what the wall-stress
 // log reads, src/logging/stress.c); 2: the whole of txx, txy, tyy, in the
-// reference's form
+// reference's form.  SCALED: visux, visuy come times nuy2 and nuy4
+// (k_props<..., true>), so 4 nu txy = sx du + sy dw hy / (2 HXXF) and
+// 4 nu tyy = sy dw: two FP64 multiplies per cell fewer (STRESS 0 or 1)
 // thread (I, J): I = 1..nx+1 handles the corner (I, J - 1/2) and, for I <= nx,
 // the centre (I, J)
 // ---------------------------------------------------------------------------
-template <int STRESS>
+template <int STRESS, bool SCALED>
 __global__ void __launch_bounds__(BX *BY)
     k_momflux(Grid g, Metrics m, Phys ph0, const double *__restrict__ ux, const double *__restrict__ uy,
               const double *__restrict__ visux, const double *__restrict__ visuy, const double *__restrict__ mfx,
@@ -845,8 +851,9 @@ __global__ void __launch_bounds__(BX *BY)
               double *__restrict__ tyy) {
   pdl_entry();
   const Phys ph = zphys(g, ph0);
-  const double *__restrict__ c4nuc = m.c4nuc + (size_t)blockIdx.z * g.cm;
-  const double *__restrict__ c2nuf = m.c2nuf + (size_t)blockIdx.z * g.cm;
+  static_assert(!(SCALED && STRESS == 2), "the reference-form stresses take unscaled viscosities");
+  const double *__restrict__ c4nuc = SCALED ? m.c4nucs : m.c4nuc + (size_t)blockIdx.z * g.cm;
+  const double *__restrict__ c2nuf = SCALED ? m.c2nufs : m.c2nuf + (size_t)blockIdx.z * g.cm;
   const int I = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (I > g.nx + 1 || J > g.ny) return;
@@ -862,13 +869,14 @@ __global__ void __launch_bounds__(BX *BY)
     const double sx = visux[ix(g, rm, I - 1)] + vx0;
     const double sy = visuy[ix(g, r, I - 1)] + vy0;
     const double du = u0 - us, dw = w0 - ww;
-    const double t4 = fma(sx, du * ph.nuy2, sy * (dw * c2nuf[I]));  // 4 nu txy
+    const double t4 = SCALED ? fma(sx, du, sy * (dw * c2nuf[I])) : fma(sx, du * ph.nuy2, sy * (dw * c2nuf[I]));  // 4 nu txy
     const double fy = mfy[ix(g, r, I - 1)] + mfy[ix(g, r, I)];
     const double fx = mfx[ix(g, rm, I - 1)] + mfx[ix(g, r, I - 1)];
     pxy[ix(g, r, I - 1)] = fma(-(m.rq[I] * fy), us + u0, t4);
     pyx[ix(g, r, I - 1)] = fma(-fx, ww + w0, t4);
     if (STRESS == 2 || (STRESS == 1 && (I == 1 || I == g.nx + 1)))
-      txy[ix(g, r, I - 1)] = fma(sx, du * g.hihy, sy * (dw * m.hihxxf[I]));
+      txy[ix(g, r, I - 1)] = SCALED ? fma(sx, du * (g.hihy * ph.inuy2), sy * (dw * (m.hihxxf[I] * ph.inuy4)))
+                                    : fma(sx, du * g.hihy, sy * (dw * m.hihxxf[I]));
   }
   if (I <= g.nx) {
     // centre (I, J): txx = (mu_l + mu_r) du/dx, tyy = (mu_s + mu_n) dv/dy
@@ -876,7 +884,7 @@ __global__ void __launch_bounds__(BX *BY)
     const double sx = vx0 + visux[ix(g, r, I)], sy = vy0 + visuy[ix(g, rp, I)];
     const double du = u1 - u0, dw = w1 - w0;
     pxx[ix(g, r, I - 1)] = fma(-(mfx[ix(g, r, I - 1)] + mfx[ix(g, r, I)]), u0 + u1, sx * (du * c4nuc[I]));
-    pyy[ix(g, r, I - 1)] = fma(-(mfy[ix(g, r, I)] + mfy[ix(g, rp, I)]), w0 + w1, sy * (dw * ph.nuy4));
+    pyy[ix(g, r, I - 1)] = fma(-(mfy[ix(g, r, I)] + mfy[ix(g, rp, I)]), w0 + w1, SCALED ? sy * dw : sy * (dw * ph.nuy4));
     if (STRESS == 2) {
       txx[ix(g, r, I - 1)] = sx * (du * m.ihxxc[I]);
       tyy[ix(g, r, I - 1)] = sy * (dw * g.ihy);
@@ -2114,9 +2122,12 @@ cudaError_t configure_kernels() {
 }
 
 void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b, bool den, bool vis,
-                  bool grad, double *den_out) {
+                  bool grad, double *den_out, bool scaled) {
   const dim3 gr = tile_grid(b.tiles, TK_PROPS, g.nx + 2, g.ny, g.nc), bl = tile_block(b.tiles, TK_PROPS);
-  if (den && vis && grad)
+  if (scaled && vis && grad && !den)
+    launch_pdl(k_props<false, true, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
+               compaction(b.tiles));
+  else if (den && vis && grad)
     launch_pdl(k_props<true, true, true>, gr, bl, 0, s, g, m, ph, b.vof, den_out, b.visux, b.visuy, b.dvof,
                compaction(b.tiles));
   else if (vis && grad)
@@ -2237,9 +2248,11 @@ void launch_stress(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &
 }
 
 void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                    const double *ux, const double *uy, int stress) {
+                    const double *ux, const double *uy, int stress, bool scaled) {
   const dim3 gr = tile_grid(b.tiles, TK_MOMFLUX, g.nx + 1, g.ny, g.nc), bl = tile_block(b.tiles, TK_MOMFLUX);
-  auto k = stress == 2 ? k_momflux<2> : (stress == 1 ? k_momflux<1> : k_momflux<0>);
+  auto k = stress == 2 ? k_momflux<2, false>
+                       : (scaled ? (stress == 1 ? k_momflux<1, true> : k_momflux<0, true>)
+                                 : (stress == 1 ? k_momflux<1, false> : k_momflux<0, false>));
   launch_pdl(k, gr, bl, 0, s, g, m, ph, ux, uy, b.visux, b.visuy, b.mfluxx, b.mfluxy, b.pxx, b.pyy, b.pxy, b.pyx,
              b.txx, b.txy, b.tyy);
 }

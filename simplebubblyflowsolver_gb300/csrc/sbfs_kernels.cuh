@@ -87,8 +87,9 @@ struct Bufs {
 };
 
 // ---- launch helpers (defined in sbfs_kernels.cu), all on stream `s`
+// scaled: the fused step's viscosities, pre-scaled for k_momflux (k_props<..., true>)
 void launch_props(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                  bool den, bool vis, bool grad, double *den_out);
+                  bool den, bool vis, bool grad, double *den_out, bool scaled = false);
 // store_k: normal[2] = 1/phi - 1 (fused step) instead of the intercept
 void launch_normal_curv(cudaStream_t s, const Grid &g, const Metrics &m, const Bufs &b, bool normal, bool curv,
                         bool store_k);
@@ -120,7 +121,7 @@ void launch_predict(cudaStream_t s, const Grid &g, const Metrics &m, const Phys 
 // stress = 1 also writes txy at the two wall columns (the wall-stress log
 // reads it), 2 the whole of txx, txy, tyy
 void launch_momflux(cudaStream_t s, const Grid &g, const Metrics &m, const Phys &ph, const Bufs &b,
-                    const double *ux, const double *uy, int stress);
+                    const double *ux, const double *uy, int stress, bool scaled);
 // fused step: the predictor from those fluxes and the CSF force ifx, ify;
 // also writes e grad psi_old at the faces (b.egx, b.egy) for the correction
 // and the Poisson right-hand side's face values (b.qx, b.qy)
