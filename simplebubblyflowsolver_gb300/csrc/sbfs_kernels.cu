@@ -832,8 +832,9 @@ __global__ void __launch_bounds__(BX *BY)
 // 4 nu (0.25 / H), the reference's diffusion minus advection
 //   ux face I:    0.25 / HXXF(I) (Pxx_I - Pxx_I-1) + 0.25 / hy (Pxy_J+1/2 - Pxy_J-1/2)
 //   uy face J-1/2: 0.25 / HXXC(I) (Pyx_I+1 - Pyx_I) + 0.25 / hy (Pyy_J - Pyy_J-1)
-// FP64 operations per cell: 29 here and 39 in k_predict_mf (with the
-// Poisson face fluxes below) against 16 + 61 for k_stress + k_predict.
+// FP64 operations per cell: 29 here (27 with the viscosities pre-scaled)
+// and 33 in k_predict_mf (with the Poisson face values it also writes)
+// against 16 + 61 for k_stress + k_predict.
 // STRESS 1: also txy at the wall columns I = 1, nx + 1 (what the wall-stress
 // log reads, src/logging/stress.c); 2: the whole of txx, txy, tyy, in the
 // reference's form.  SCALED: visux, visuy come times nuy2 and nuy4
